@@ -1,0 +1,77 @@
+#!/usr/bin/env python3
+"""Regenerates the golden fixtures in tests/golden/ from the reference itself.
+
+Builds the reference's own C++ sources (oracle/build_ref.sh, stand-in FFTW and
+Boost headers) into oracle/_ref/golay_ref, runs it under LC_ALL=C, and stores:
+
+* n16/, n26/   -- every stage file of `main N -c 2 1 all` (small, verbatim);
+* manifest.json -- line counts and SHA-256 of those files, plus of the larger
+  outputs that are not stored verbatim (n=34 gen, the n=57 lambda=-2 c=3
+  shard 7 of 1000).
+
+Needs the reference sources; run in the build container only:
+    python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF_BIN = os.path.join(REPO, "oracle", "_ref", "golay_ref")
+
+# (name, argv after the binary, files to record, keep verbatim)
+RUNS = [
+    ("n16", ["16", "-c", "2", "1", "all"],
+     ["16-filtered-a#0", "16-filtered-b#0", "16-filtered_sorted-a", "16-filtered_sorted-b",
+      "16-pairs-2", "16-pairs-1", "16-unique"], True),
+    ("n26", ["26", "-c", "2", "1", "all"],
+     ["26-filtered-a#0", "26-filtered-b#0", "26-filtered_sorted-a", "26-filtered_sorted-b",
+      "26-pairs-2", "26-pairs-1", "26-unique"], True),
+    ("n34", ["34", "-c", "2", "gen"], ["34-filtered-a#0", "34-filtered-b#0"], False),
+    ("n57_shard7of1000", ["57", "-c", "3", "1", "--paf", "-2", "-n", "1000", "-j", "7", "gen"],
+     ["57-filtered-a#7", "57-filtered-b#7"], False),
+]
+
+
+def sha256(path):
+    h = hashlib.sha256()
+    with open(path, "rb") as f:
+        h.update(f.read())
+    return h.hexdigest()
+
+
+def main():
+    subprocess.run(["bash", os.path.join(REPO, "oracle", "build_ref.sh")], check=True)
+    if not os.path.exists(REF_BIN):
+        sys.exit("reference binary missing (no reference sources here)")
+    env = dict(os.environ, LC_ALL="C")
+    manifest = {"generator": "reference sources built by oracle/build_ref.sh, LC_ALL=C", "runs": {}}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, args, files, keep in RUNS:
+            d = os.path.join(tmp, name)
+            subprocess.run([REF_BIN] + args[:-1] + ["--dir", d, args[-1]], check=True, env=env,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            order = args[0]
+            wd = os.path.join(d, f"order-{order}")
+            rec = {"argv": args, "files": {}}
+            for fn in files:
+                p = os.path.join(wd, fn)
+                with open(p, "rb") as f:
+                    nlines = f.read().count(b"\n")
+                rec["files"][fn] = {"lines": nlines, "sha256": sha256(p)}
+                if keep:
+                    os.makedirs(os.path.join(HERE, name), exist_ok=True)
+                    shutil.copy(p, os.path.join(HERE, name, fn.replace("#", "_")))
+            manifest["runs"][name] = rec
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+    print("golden fixtures written")
+
+
+if __name__ == "__main__":
+    main()

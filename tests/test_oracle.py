@@ -1,0 +1,109 @@
+"""Pins the CPU oracle against the reference's own outputs (golden fixtures
+generated by tests/golden/make_golden.py from the reference sources)."""
+import ctypes
+import hashlib
+import math
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, GenStats, read
+
+ENV = dict(os.environ, LC_ALL="C")
+
+
+def run_oracle(oracle_bin, tmp_path, argv):
+    d = str(tmp_path / "res")
+    subprocess.run([oracle_bin] + argv[:-1] + ["--dir", d, argv[-1]], check=True, env=ENV,
+                   stdout=subprocess.DEVNULL)
+    return os.path.join(d, f"order-{argv[0]}")
+
+
+@pytest.mark.parametrize("name", ["n16", "n26"])
+def test_oracle_full_pipeline_matches_reference(oracle_bin, tmp_path, golden_manifest, name):
+    rec = golden_manifest["runs"][name]
+    wd = run_oracle(oracle_bin, tmp_path, rec["argv"])
+    for fn, meta in rec["files"].items():
+        got = read(os.path.join(wd, fn))
+        assert got == read(os.path.join(GOLDEN, name, fn.replace("#", "_"))), fn
+        assert got.count(b"\n") == meta["lines"]
+
+
+@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000"])
+def test_oracle_generation_matches_reference_hash(oracle_bin, tmp_path, golden_manifest, name):
+    rec = golden_manifest["runs"][name]
+    wd = run_oracle(oracle_bin, tmp_path, rec["argv"])
+    for fn, meta in rec["files"].items():
+        got = read(os.path.join(wd, fn))
+        assert hashlib.sha256(got).hexdigest() == meta["sha256"], fn
+        assert got.count(b"\n") == meta["lines"]
+
+
+def _units(L):
+    return [u for u in range(1, L) if math.gcd(u, L) == 1] if L > 1 else [1]
+
+
+@pytest.mark.parametrize("L", list(range(1, 41)) + [45, 57])
+def test_orderly_generators_are_affine_and_dihedral(oracle_lib, L):
+    """constructGenerators(0, L) is the affine group i -> u*i + t (u a unit),
+    constructGenerators(1, L) the dihedral group i -> +-i + t; the GPU
+    canonical check relies on this characterisation."""
+    for flag in (0, 1):
+        n = oracle_lib.gpo_orderly_generators(L, flag, None, 0)
+        buf = (ctypes.c_int * (n * L))()
+        oracle_lib.gpo_orderly_generators(L, flag, buf, n)
+        got = {tuple(buf[i * L:(i + 1) * L]) for i in range(n)}
+        mults = _units(L) if flag == 0 else [1, L - 1 if L > 1 else 1]
+        want = {tuple((u * i + t) % L for i in range(L)) for u in mults for t in range(L)}
+        assert got == want
+
+
+def test_necklace_counts(oracle_lib):
+    assert oracle_lib.gpo_necklace_count(8, 3) == 834
+    assert oracle_lib.gpo_necklace_count(13, 3) == 122643
+    assert oracle_lib.gpo_necklace_count(17, 3) == 7596483
+
+
+@pytest.mark.parametrize("order,compress,paf,nwin", [(16, 2, 0, 7), (26, 2, 0, 5), (34, 2, 0, 3)])
+def test_window_union_equals_full_enumeration(oracle_lib, tmp_path, order, compress, paf, nwin):
+    """Rank windows that partition the word space reproduce the full run."""
+    L = order // compress
+    k = len([v for v in range(-compress, compress + 1, 2) if compress % 2 == 0 or v % 2 != 0])
+    total = k ** L
+    full_a, full_b = str(tmp_path / "fa"), str(tmp_path / "fb")
+    st = GenStats()
+    assert oracle_lib.gpo_generate(order, compress, paf, full_a.encode(), full_b.encode(), 0, 1,
+                                   ctypes.byref(st)) == 0
+    bounds = [0] + sorted(np.random.default_rng(1).integers(1, total, nwin - 1).tolist()) + [total]
+    cat_a, cat_b = b"", b""
+    for w in range(nwin):
+        lo, hi = bounds[w], bounds[w + 1]
+        pa, pb = str(tmp_path / f"a{w}"), str(tmp_path / f"b{w}")
+        oracle_lib.gpo_generate_window(order, compress, paf, pa.encode(), pb.encode(), lo >> 64,
+                                       lo & (2**64 - 1), hi >> 64, hi & (2**64 - 1), None)
+        cat_a += read(pa)
+        cat_b += read(pb)
+    assert cat_a == read(full_a)
+    assert cat_b == read(full_b)
+
+
+def test_pair_generator_sizes(oracle_lib):
+    # printed by the reference's generateExhaust for n=16, c=1 (65536 items)
+    assert oracle_lib.gpo_pair_generator_count(16, 1) == 65536
+
+
+def test_psd_batch_matches_scalar(oracle_lib):
+    rng = np.random.default_rng(0)
+    L, order = 13, 26
+    seqs = rng.choice(np.array([-2, 0, 2], dtype=np.int8), size=(500, L))
+    ver = np.zeros(500, dtype=np.uint8)
+    n = oracle_lib.gpo_psd_filter_batch(seqs.ctypes.data, 500, L, order, 0, ver.ctypes.data, 3)
+    psd = (ctypes.c_double * L)()
+    for i in range(500):
+        s = (ctypes.c_int * L)(*seqs[i].tolist())
+        oracle_lib.gpo_psd(s, L, psd)
+        ok = all(psd[k] <= 2 * order + 0.001 for k in range(1, L // 2 + 1))
+        assert ver[i] == ok
+    assert n == ver.sum()
