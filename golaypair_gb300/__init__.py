@@ -1,0 +1,162 @@
+"""GB300-native (sm_103a) implementation of GolayPair's candidate-generation ->
+PSD-filter -> sorted-PSD-matching path.
+
+The product is the C ABI in include/golaypair_gb300.h, implemented by
+golaypair_gb300/_build/libgolaypair_gb300.so (CUDA kernels + host runtime),
+and the `golay` command line driver next to it, which mirrors the
+reference's `main`.  This module is a thin ctypes binding used by tests and
+benchmarks.  There is no CPU fallback: every call fails loudly when the
+library is missing or no GB300 is present.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libgolaypair_gb300.so")
+CLI_PATH = os.path.join(PKG, "_build", "golay")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "golaypair_gb300.h")
+
+GP_PSD_FP64 = 0
+GP_PSD_TC_GUARDED = 1
+
+_lib = None
+
+
+class GPError(RuntimeError):
+    pass
+
+
+class PsdStats(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("n_pass", ctypes.c_int64), ("n_unsure", ctypes.c_int64),
+                ("guard", ctypes.c_float), ("err_coef", ctypes.c_float)]
+
+
+class GenStats(ctypes.Structure):
+    _fields_ = [("necklaces", ctypes.c_int64), ("candidates", ctypes.c_int64), ("psd_pass", ctypes.c_int64),
+                ("written_a", ctypes.c_int64), ("written_b", ctypes.c_int64), ("unsure", ctypes.c_int64),
+                ("seconds", ctypes.c_double)]
+
+
+def build():
+    from . import native_build
+    return native_build.build()
+
+
+def lib():
+    """Loads the in-tree native library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise GPError(f"native library missing: {LIB_PATH} (run golaypair_gb300.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    P, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+    cp = ctypes.c_char_p
+    L.gp_ctx_create.argtypes = [ctypes.POINTER(P), i32]
+    L.gp_ctx_destroy.argtypes = [P]
+    L.gp_last_error.argtypes = [P]
+    L.gp_last_error.restype = cp
+    L.gp_device_sm_count.argtypes = [P]
+    L.gp_psd_filter.argtypes = [P, P, i64, i32, i32, i32, i32, P, P]
+    L.gp_psd_filter_device.argtypes = [P, P, i64, i32, i32, i32, i32, P, P, P]
+    L.gp_psd_tc_values.argtypes = [P, P, i64, i32, P]
+    L.gp_psd_fp64_values.argtypes = [P, P, i64, i32, P]
+    for name, args in _STAGE_SIGS.items():
+        fn = getattr(L, name, None)
+        if fn is not None:
+            fn.argtypes = args
+    _lib = L
+    return L
+
+
+_P, _i32, _i64, _u64, _cp = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, ctypes.c_char_p
+_STAGE_SIGS = {
+    "gp_generate": [_P, _i32, _i32, _i32, _i32, _i32, _cp, _cp, _P],
+    "gp_generate_window": [_P, _i32, _i32, _i32, _u64, _u64, _u64, _u64, _cp, _cp, _P],
+    "gp_sort": [_P, _P, _i32, _cp],
+    "gp_match": [_P, _i32, _i32, _i32, _cp, _cp, _cp, _i32, _P],
+    "gp_uncompress": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp],
+    "gp_equiv_filter": [_P, _i32, _i32, _cp, _cp],
+}
+
+
+def header_symbols():
+    """Names of the functions include/golaypair_gb300.h declares."""
+    import re
+    with open(HEADER) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(gp_\w+)\s*\(", text, re.M)))
+
+
+class Context:
+    """One gp_ctx on one GPU."""
+
+    def __init__(self, device=0):
+        self._lib = lib()
+        self._h = ctypes.c_void_p()
+        rc = self._lib.gp_ctx_create(ctypes.byref(self._h), device)
+        if rc != 0:
+            raise GPError(f"gp_ctx_create failed ({rc}): CUDA device {device} is not an sm_103a GPU or unusable")
+
+    def close(self):
+        if self._h:
+            self._lib.gp_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, rc, what):
+        if rc != 0:
+            msg = self._lib.gp_last_error(self._h)
+            raise GPError(f"{what} -> {rc}: {msg.decode() if msg else ''}")
+        return rc
+
+    @property
+    def sm_count(self):
+        return self._lib.gp_device_sm_count(self._h)
+
+    def psd_filter(self, seqs, order, paf=0, mode=GP_PSD_TC_GUARDED):
+        """Host-buffer batched PSD filter; returns (bool verdicts, PsdStats)."""
+        seqs = np.ascontiguousarray(seqs, dtype=np.int8)
+        n, L = seqs.shape
+        mask = np.zeros((n + 31) // 32, dtype=np.uint32)
+        st = PsdStats()
+        self.check(self._lib.gp_psd_filter(self._h, seqs.ctypes.data, n, L, order, paf, mode, mask.ctypes.data,
+                                           ctypes.byref(st)), "gp_psd_filter")
+        return unpack_mask(mask, n), st
+
+    def psd_tc_values(self, seqs):
+        seqs = np.ascontiguousarray(seqs, dtype=np.int8)
+        n, L = seqs.shape
+        out = np.zeros((n, L // 2), dtype=np.float32)
+        self.check(self._lib.gp_psd_tc_values(self._h, seqs.ctypes.data, n, L, out.ctypes.data), "gp_psd_tc_values")
+        return out
+
+    def psd_fp64_values(self, seqs):
+        seqs = np.ascontiguousarray(seqs, dtype=np.int8)
+        n, L = seqs.shape
+        out = np.zeros((n, L), dtype=np.float64)
+        self.check(self._lib.gp_psd_fp64_values(self._h, seqs.ctypes.data, n, L, out.ctypes.data),
+                   "gp_psd_fp64_values")
+        return out
+
+
+def unpack_mask(mask, n):
+    bits = np.unpackbits(mask.view(np.uint8), bitorder="little")
+    return bits[:n].astype(bool)

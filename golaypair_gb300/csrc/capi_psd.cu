@@ -1,0 +1,308 @@
+// capi_psd.cu -- context management and the batched PSD filter entry points.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "ctx.h"
+
+namespace {
+
+constexpr int64_t kChunkRows = int64_t(1) << 25;  // rows per pipelined chunk (multiple of 128)
+
+double threshold(int order, int paf) { return 2.0 * order - paf + 0.001; }
+
+// configured guard band: 1e-3 * 2n (absolute PSD units)
+float guard_band(int order) { return (float)(2e-3 * order); }
+
+}  // namespace
+
+const void* gp_ctx::twiddle_image(int L) {
+    auto it = twiddles.find(L);
+    if (it != twiddles.end()) return it->second.p;
+    const int K = gp::tc_k_for_len(L);
+    if (!K) return nullptr;
+    const size_t bytes = gp::build_twiddle_image(L, K, nullptr);
+    std::vector<uint8_t> img(bytes);
+    gp::build_twiddle_image(L, K, img.data());
+    DevBuf& b = twiddles[L];
+    if (!b.ensure(bytes)) return nullptr;
+    if (cudaMemcpy(b.p, img.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    return b.p;
+}
+
+int gp_ctx::check_status(const char* what) {
+    int st = 0;
+    cudaError_t e = cudaMemcpy(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (st == 0) return GP_OK;
+    cudaMemset(status.p, 0, sizeof(int));
+    if (st >= GP_KSTATUS_TIMEOUT_BASE && st < GP_KSTATUS_OVERFLOW)
+        return fail(GP_ERR_TIMEOUT, "%s: device wait timed out at site %d", what, st - GP_KSTATUS_TIMEOUT_BASE);
+    if (st == GP_KSTATUS_OVERFLOW) return fail(GP_ERR_OVERFLOW, "%s: device output list overflow", what);
+    return fail(GP_ERR_CUDA, "%s: kernel status %d", what, st);
+}
+
+extern "C" {
+
+int gp_ctx_create(gp_ctx** out, int device) {
+    if (!out) return GP_ERR_ARG;
+    *out = nullptr;
+    gp_ctx* c = new gp_ctx();
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    int major = 0, minor = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return GP_ERR_CUDA;
+    }
+    if (major != 10 || minor != 3) {
+        // kernels are built for sm_103a only
+        delete c;
+        return GP_ERR_UNSUPPORTED;
+    }
+    if (cudaStreamCreateWithFlags(&c->s_comp, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->s_copy, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return GP_ERR_CUDA;
+    }
+    for (int i = 0; i < 2; ++i) {
+        cudaEventCreateWithFlags(&c->ev_h2d[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&c->ev_done[i], cudaEventDisableTiming);
+    }
+    if (!c->status.ensure(sizeof(int)) || !c->counts.ensure(64 * sizeof(unsigned long long)) ||
+        !c->h_counts.ensure(64 * sizeof(unsigned long long))) {
+        delete c;
+        return GP_ERR_NOMEM;
+    }
+    cudaMemset(c->status.p, 0, sizeof(int));
+    cudaMemset(c->counts.p, 0, 64 * sizeof(unsigned long long));
+    cudaDeviceSynchronize();
+    *out = c;
+    return GP_OK;
+}
+
+int gp_ctx_destroy(gp_ctx* c) {
+    if (!c) return GP_OK;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    c->status.release();
+    c->counts.release();
+    c->h_counts.release();
+    for (int i = 0; i < 2; ++i) {
+        c->seq_buf[i].release();
+        c->mask_buf[i].release();
+        c->unsure_buf[i].release();
+        if (c->ev_h2d[i]) cudaEventDestroy(c->ev_h2d[i]);
+        if (c->ev_done[i]) cudaEventDestroy(c->ev_done[i]);
+    }
+    for (auto& kv : c->twiddles) kv.second.release();
+    for (auto& b : c->scratch) b.release();
+    for (auto& b : c->hscratch) b.release();
+    if (c->s_comp) cudaStreamDestroy(c->s_comp);
+    if (c->s_copy) cudaStreamDestroy(c->s_copy);
+    delete c;
+    return GP_OK;
+}
+
+const char* gp_last_error(const gp_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+int gp_device_sm_count(const gp_ctx* c) { return c ? c->num_sms : 0; }
+
+// Enqueues the filter of one device-resident batch (n < 2^31) on `st`.
+// unsure/unsure_count: scratch for the TC mode.
+static int enqueue_filter(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int order, int paf, int mode,
+                          uint32_t* d_mask, uint32_t* d_unsure, unsigned long long* d_ucount, cudaStream_t st) {
+    const int64_t words = (n + 31) / 32;
+    if (mode == GP_PSD_FP64) {
+        gp::PsdF64Args a{d_seqs, n, L, threshold(order, paf), d_mask, words};
+        GP_CUDA_TRY(c, gp::launch_psd_fp64(a, st));
+        return GP_OK;
+    }
+    const void* img = c->twiddle_image(L);
+    if (!img) return c->fail(GP_ERR_UNSUPPORTED, "tensor-core filter: unsupported length %d", L);
+    GP_CUDA_TRY(c, cudaMemsetAsync(d_ucount, 0, sizeof(unsigned long long), st));
+    gp::PsdTcArgs a;
+    a.seqs = d_seqs;
+    a.n = n;
+    a.L = L;
+    a.bimage = img;
+    a.thr = (float)threshold(order, paf);
+    a.guard_cfg = guard_band(order);
+    a.err_coef = gp::tc_err_coef(gp::tc_k_for_len(L));
+    a.mask = d_mask;
+    a.mask_words = words;
+    a.unsure = d_unsure;
+    a.unsure_count = d_ucount;
+    a.unsure_cap = n;
+    a.psd_out = nullptr;
+    a.status = c->status.as<int>();
+    GP_CUDA_TRY(c, gp::launch_psd_tc(a, c->num_sms, st));
+    GP_CUDA_TRY(c, gp::launch_psd_recheck(d_seqs, L, threshold(order, paf), d_unsure, d_ucount, n, d_mask, st));
+    return GP_OK;
+}
+
+static int64_t popcount_words(const uint32_t* w, int64_t nwords) {
+    int64_t s = 0;
+    for (int64_t i = 0; i < nwords; ++i) s += __builtin_popcount(w[i]);
+    return s;
+}
+
+static int check_args(gp_ctx* c, int64_t n, int L, int mode) {
+    if (!c) return GP_ERR_ARG;
+    if (n < 0 || L < 1 || L > gp::kMaxLen) return c->fail(GP_ERR_ARG, "bad n=%lld or L=%d", (long long)n, L);
+    if (mode != GP_PSD_FP64 && mode != GP_PSD_TC_GUARDED) return c->fail(GP_ERR_ARG, "bad mode %d", mode);
+    if (mode == GP_PSD_TC_GUARDED && !gp::tc_k_for_len(L))
+        return c->fail(GP_ERR_UNSUPPORTED, "tensor-core filter supports 2 <= L <= %d", gp::kMaxTcK);
+    return GP_OK;
+}
+
+int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, int paf, int mode,
+                  uint32_t* pass_mask, gp_psd_stats* stats) {
+    int rc = check_args(c, n, L, mode);
+    if (rc) return rc;
+    if (n > 0 && (!seqs || !pass_mask)) return c->fail(GP_ERR_ARG, "null buffer");
+    cudaSetDevice(c->device);
+    const int64_t chunk = std::min<int64_t>(kChunkRows, std::max<int64_t>(n, 1));
+    for (int b = 0; b < 2; ++b) {
+        if (!c->seq_buf[b].ensure((size_t)chunk * L + 16) || !c->mask_buf[b].ensure((size_t)(chunk + 31) / 32 * 4) ||
+            !c->unsure_buf[b].ensure((size_t)chunk * 4))
+            return c->fail(GP_ERR_NOMEM, "psd filter: device allocation failed");
+    }
+    auto* d_counts = c->counts.as<unsigned long long>();
+    auto* h_counts = c->h_counts.as<unsigned long long>();
+    const int64_t nchunks = (n + chunk - 1) / chunk;
+    int64_t unsure_total = 0;
+    for (int64_t ci = 0; ci < nchunks; ++ci) {
+        const int b = (int)(ci & 1);
+        const int64_t r0 = ci * chunk;
+        const int64_t rows = std::min(chunk, n - r0);
+        if (ci >= 2) GP_CUDA_TRY(c, cudaStreamWaitEvent(c->s_copy, c->ev_done[b], 0));
+        GP_CUDA_TRY(c, cudaMemcpyAsync(c->seq_buf[b].p, seqs + r0 * L, (size_t)rows * L, cudaMemcpyHostToDevice,
+                                       c->s_copy));
+        GP_CUDA_TRY(c, cudaEventRecord(c->ev_h2d[b], c->s_copy));
+        GP_CUDA_TRY(c, cudaStreamWaitEvent(c->s_comp, c->ev_h2d[b], 0));
+        rc = enqueue_filter(c, c->seq_buf[b].as<int8_t>(), rows, L, order, paf, mode, c->mask_buf[b].as<uint32_t>(),
+                            c->unsure_buf[b].as<uint32_t>(), d_counts + b, c->s_comp);
+        if (rc) return rc;
+        GP_CUDA_TRY(c, cudaMemcpyAsync(pass_mask + r0 / 32, c->mask_buf[b].p, (size_t)(rows + 31) / 32 * 4,
+                                       cudaMemcpyDeviceToHost, c->s_comp));
+        if (mode == GP_PSD_TC_GUARDED)
+            GP_CUDA_TRY(c, cudaMemcpyAsync(h_counts + 2 + ci % 62, d_counts + b, sizeof(unsigned long long),
+                                           cudaMemcpyDeviceToHost, c->s_comp));
+        GP_CUDA_TRY(c, cudaEventRecord(c->ev_done[b], c->s_comp));
+        if (mode == GP_PSD_TC_GUARDED && (ci % 62) == 61) {
+            GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_comp));
+            for (int k = 0; k < 62; ++k) unsure_total += (int64_t)h_counts[2 + k];
+        }
+    }
+    GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_comp));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_copy));
+    if (mode == GP_PSD_TC_GUARDED)
+        for (int64_t k = 0; k < nchunks % 62; ++k) unsure_total += (int64_t)h_counts[2 + k];
+    rc = c->check_status("gp_psd_filter");
+    if (rc) return rc;
+    if (stats) {
+        stats->n = n;
+        stats->n_pass = popcount_words(pass_mask, (n + 31) / 32);
+        stats->n_unsure = unsure_total;
+        stats->guard = guard_band(order);
+        stats->err_coef = mode == GP_PSD_TC_GUARDED ? gp::tc_err_coef(gp::tc_k_for_len(L)) : 0.f;
+    }
+    return GP_OK;
+}
+
+int gp_psd_filter_device(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int order, int paf, int mode,
+                         uint32_t* d_mask, void* stream, gp_psd_stats* stats) {
+    int rc = check_args(c, n, L, mode);
+    if (rc) return rc;
+    if (n >= (int64_t(1) << 31)) return c->fail(GP_ERR_ARG, "device batch too large (n < 2^31)");
+    cudaSetDevice(c->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->s_comp;
+    if (mode == GP_PSD_TC_GUARDED && !c->unsure_buf[0].ensure((size_t)std::max<int64_t>(n, 1) * 4))
+        return c->fail(GP_ERR_NOMEM, "psd filter: device allocation failed");
+    rc = enqueue_filter(c, d_seqs, n, L, order, paf, mode, d_mask, c->unsure_buf[0].as<uint32_t>(),
+                        c->counts.as<unsigned long long>(), st);
+    if (rc) return rc;
+    if (stats) {
+        GP_CUDA_TRY(c, cudaStreamSynchronize(st));
+        rc = c->check_status("gp_psd_filter_device");
+        if (rc) return rc;
+        std::vector<uint32_t> m((size_t)(n + 31) / 32);
+        GP_CUDA_TRY(c, cudaMemcpy(m.data(), d_mask, m.size() * 4, cudaMemcpyDeviceToHost));
+        unsigned long long u = 0;
+        GP_CUDA_TRY(c, cudaMemcpy(&u, c->counts.p, sizeof u, cudaMemcpyDeviceToHost));
+        stats->n = n;
+        stats->n_pass = popcount_words(m.data(), (int64_t)m.size());
+        stats->n_unsure = mode == GP_PSD_TC_GUARDED ? (int64_t)u : 0;
+        stats->guard = guard_band(order);
+        stats->err_coef = mode == GP_PSD_TC_GUARDED ? gp::tc_err_coef(gp::tc_k_for_len(L)) : 0.f;
+    }
+    return GP_OK;
+}
+
+int gp_psd_tc_values(gp_ctx* c, const int8_t* seqs, int64_t n, int L, float* out) {
+    int rc = check_args(c, n, L, GP_PSD_TC_GUARDED);
+    if (rc) return rc;
+    if (n >= (int64_t(1) << 31)) return c->fail(GP_ERR_ARG, "batch too large");
+    if (n == 0) return GP_OK;
+    cudaSetDevice(c->device);
+    const int K = gp::tc_k_for_len(L);
+    DevBuf& ds = c->scratch[0];
+    DevBuf& dm = c->scratch[1];
+    DevBuf& du = c->scratch[2];
+    DevBuf& dp = c->scratch[3];
+    if (!ds.ensure((size_t)n * L + 16) || !dm.ensure((size_t)(n + 31) / 32 * 4) || !du.ensure((size_t)n * 4) ||
+        !dp.ensure((size_t)n * (K / 2) * 4))
+        return c->fail(GP_ERR_NOMEM, "allocation failed");
+    GP_CUDA_TRY(c, cudaMemcpy(ds.p, seqs, (size_t)n * L, cudaMemcpyHostToDevice));
+    const void* img = c->twiddle_image(L);
+    if (!img) return c->fail(GP_ERR_UNSUPPORTED, "length %d", L);
+    GP_CUDA_TRY(c, cudaMemset(c->counts.p, 0, sizeof(unsigned long long)));
+    gp::PsdTcArgs a;
+    a.seqs = ds.as<int8_t>();
+    a.n = n;
+    a.L = L;
+    a.bimage = img;
+    a.thr = 1e30f;
+    a.guard_cfg = 0.f;
+    a.err_coef = 0.f;
+    a.mask = dm.as<uint32_t>();
+    a.mask_words = (n + 31) / 32;
+    a.unsure = du.as<uint32_t>();
+    a.unsure_count = c->counts.as<unsigned long long>();
+    a.unsure_cap = n;
+    a.psd_out = dp.as<float>();
+    a.status = c->status.as<int>();
+    GP_CUDA_TRY(c, gp::launch_psd_tc(a, c->num_sms, c->s_comp));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_comp));
+    rc = c->check_status("gp_psd_tc_values");
+    if (rc) return rc;
+    std::vector<float> full((size_t)n * (K / 2));
+    GP_CUDA_TRY(c, cudaMemcpy(full.data(), dp.p, full.size() * 4, cudaMemcpyDeviceToHost));
+    const int H = L / 2;
+    for (int64_t i = 0; i < n; ++i) std::memcpy(out + i * H, full.data() + i * (K / 2), (size_t)H * 4);
+    return GP_OK;
+}
+
+int gp_psd_fp64_values(gp_ctx* c, const int8_t* seqs, int64_t n, int L, double* out) {
+    int rc = check_args(c, n, L, GP_PSD_FP64);
+    if (rc) return rc;
+    if (n == 0) return GP_OK;
+    cudaSetDevice(c->device);
+    DevBuf& ds = c->scratch[0];
+    DevBuf& dv = c->scratch[4];
+    if (!ds.ensure((size_t)n * L + 16) || !dv.ensure((size_t)n * L * 8))
+        return c->fail(GP_ERR_NOMEM, "allocation failed");
+    GP_CUDA_TRY(c, cudaMemcpy(ds.p, seqs, (size_t)n * L, cudaMemcpyHostToDevice));
+    GP_CUDA_TRY(c, gp::launch_psd_fp64_values(ds.as<int8_t>(), n, L, dv.as<double>(), c->s_comp));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_comp));
+    GP_CUDA_TRY(c, cudaMemcpy(out, dv.p, (size_t)n * L * 8, cudaMemcpyDeviceToHost));
+    return GP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,111 @@
+// ctx.h -- the context behind gp_ctx: device, streams, grow-only device
+// buffers, cached twiddle images.  Host-side runtime, not public.
+#pragma once
+#include <cstdarg>
+#include <cstdint>
+#include <map>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/golaypair_gb300.h"
+#include "gp_internal.h"
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    // Grows to at least `bytes` (contents not preserved).  false on failure.
+    bool ensure(size_t bytes) {
+        if (bytes <= cap) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes < 256 ? 256 : bytes;
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        cap = want;
+        return true;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+struct HostPinned {
+    void* p = nullptr;
+    size_t cap = 0;
+    bool ensure(size_t bytes) {
+        if (bytes <= cap) return true;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        cap = bytes;
+        return true;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+struct gp_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t s_comp = nullptr;
+    cudaStream_t s_copy = nullptr;
+    cudaEvent_t ev_h2d[2] = {nullptr, nullptr};
+    cudaEvent_t ev_done[2] = {nullptr, nullptr};
+    std::string err;
+    // status word and counters (device)
+    DevBuf status;          // int
+    DevBuf counts;          // unsigned long long [8]
+    HostPinned h_counts;    // mirror of counts, per chunk
+    // PSD filter staging
+    DevBuf seq_buf[2];
+    DevBuf mask_buf[2];
+    DevBuf unsure_buf[2];
+    std::map<int, DevBuf> twiddles;  // by L
+    // generic scratch arenas used by the stage pipelines
+    DevBuf scratch[16];
+    HostPinned hscratch[4];
+
+    int fail(int code, const char* fmt, ...) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char* what) {
+        return fail(GP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+    // device twiddle image for length L (tensor-core filter)
+    const void* twiddle_image(int L);
+    // reads the kernel status word; resets it; returns a GP code
+    int check_status(const char* what);
+};
+
+#define GP_CUDA_TRY(ctx, expr)                                  \
+    do {                                                        \
+        cudaError_t _e = (expr);                                \
+        if (_e != cudaSuccess) return (ctx)->cuda_fail(_e, #expr); \
+    } while (0)
