@@ -62,6 +62,8 @@ def lib():
     L.gp_psd_filter.argtypes = [P, P, i64, i32, i32, i32, i32, P, P]
     L.gp_psd_filter_device.argtypes = [P, P, i64, i32, i32, i32, i32, P, P, P]
     L.gp_psd_tc_values.argtypes = [P, P, i64, i32, P]
+    L.gp_kernel_timing.argtypes = [P, i32]
+    L.gp_kernel_time.argtypes = [P, P, P]
     L.gp_psd_fp64_values.argtypes = [P, P, i64, i32, P]
     for name, args in _STAGE_SIGS.items():
         fn = getattr(L, name, None)
@@ -140,6 +142,30 @@ class Context:
         self.check(self._lib.gp_psd_filter(self._h, seqs.ctypes.data, n, L, order, paf, mode, mask.ctypes.data,
                                            ctypes.byref(st)), "gp_psd_filter")
         return unpack_mask(mask, n), st
+
+    def psd_filter_device(self, d_seqs_ptr, n, L, order, paf, mode, d_mask_ptr, stream_ptr=None, stats=False):
+        """Device-buffer filter (pointers as ints); enqueued on stream_ptr."""
+        st = PsdStats() if stats else None
+        self.check(self._lib.gp_psd_filter_device(self._h, d_seqs_ptr, n, L, order, paf, mode, d_mask_ptr,
+                                                  stream_ptr, ctypes.byref(st) if st is not None else None),
+                   "gp_psd_filter_device")
+        return st
+
+    def psd_filter_host_raw(self, seqs_ptr, n, L, order, paf, mode, mask_ptr):
+        """Host-buffer filter on raw pointers (e.g. pinned memory)."""
+        st = PsdStats()
+        self.check(self._lib.gp_psd_filter(self._h, seqs_ptr, n, L, order, paf, mode, mask_ptr, ctypes.byref(st)),
+                   "gp_psd_filter")
+        return st
+
+    def kernel_timing(self, enable=True):
+        self._lib.gp_kernel_timing(self._h, 1 if enable else 0)
+
+    def kernel_time(self):
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        self._lib.gp_kernel_time(self._h, ctypes.byref(ms), ctypes.byref(n))
+        return ms.value, n.value
 
     def psd_tc_values(self, seqs):
         seqs = np.ascontiguousarray(seqs, dtype=np.int8)

@@ -111,6 +111,31 @@ int gp_ctx_destroy(gp_ctx* c) {
 
 const char* gp_last_error(const gp_ctx* c) { return c ? c->err.c_str() : "no context"; }
 
+int gp_kernel_timing(gp_ctx* c, int enable) {
+    if (!c) return GP_ERR_ARG;
+    c->timing = enable != 0;
+    return GP_OK;
+}
+
+int gp_kernel_time(gp_ctx* c, double* total_ms, int64_t* launches) {
+    if (!c) return GP_ERR_ARG;
+    double tot = 0;
+    int64_t n = 0;
+    for (auto& pr : c->timed) {
+        float ms = 0;
+        if (cudaEventSynchronize(pr.second) == cudaSuccess && cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) {
+            tot += ms;
+            ++n;
+        }
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    c->timed.clear();
+    if (total_ms) *total_ms = tot;
+    if (launches) *launches = n;
+    return GP_OK;
+}
+
 int gp_device_sm_count(const gp_ctx* c) { return c ? c->num_sms : 0; }
 
 // Enqueues the filter of one device-resident batch (n < 2^31) on `st`.
@@ -120,7 +145,10 @@ static int enqueue_filter(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int
     const int64_t words = (n + 31) / 32;
     if (mode == GP_PSD_FP64) {
         gp::PsdF64Args a{d_seqs, n, L, threshold(order, paf), d_mask, words};
+        cudaEvent_t tb;
+        c->time_begin(st, &tb);
         GP_CUDA_TRY(c, gp::launch_psd_fp64(a, st));
+        c->time_end(st, tb);
         return GP_OK;
     }
     const void* img = c->twiddle_image(L);
@@ -141,7 +169,10 @@ static int enqueue_filter(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int
     a.unsure_cap = n;
     a.psd_out = nullptr;
     a.status = c->status.as<int>();
+    cudaEvent_t tb;
+    c->time_begin(st, &tb);
     GP_CUDA_TRY(c, gp::launch_psd_tc(a, c->num_sms, st));
+    c->time_end(st, tb);
     GP_CUDA_TRY(c, gp::launch_psd_recheck(d_seqs, L, threshold(order, paf), d_unsure, d_ucount, n, d_mask, st));
     return GP_OK;
 }

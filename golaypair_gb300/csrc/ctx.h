@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <map>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -82,6 +84,22 @@ struct gp_ctx {
     DevBuf mask_buf[2];
     DevBuf unsure_buf[2];
     std::map<int, DevBuf> twiddles;  // by L
+    // optional CUDA-event timing of the main filter kernel (profiling)
+    bool timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;
+    void time_begin(cudaStream_t st, cudaEvent_t* b) {
+        *b = nullptr;
+        if (!timing) return;
+        cudaEventCreate(b);
+        cudaEventRecord(*b, st);
+    }
+    void time_end(cudaStream_t st, cudaEvent_t b) {
+        if (!timing || !b) return;
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        timed.emplace_back(b, e);
+    }
     // generic scratch arenas used by the stage pipelines
     DevBuf scratch[16];
     HostPinned hscratch[4];

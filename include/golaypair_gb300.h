@@ -70,6 +70,12 @@ int gp_psd_filter(gp_ctx* ctx, const int8_t* seqs, int64_t n, int L, int order, 
 int gp_psd_filter_device(gp_ctx* ctx, const int8_t* d_seqs, int64_t n, int L, int order, int paf, int mode,
                          uint32_t* d_pass_mask, void* stream, gp_psd_stats* stats);
 
+/* Profiling: when enabled, CUDA events bracket every launch of the main
+ * filter kernel (tensor-core or FP64) on its stream.  gp_kernel_time waits
+ * for them, returns the summed device time and launch count, and clears. */
+int gp_kernel_timing(gp_ctx* ctx, int enable);
+int gp_kernel_time(gp_ctx* ctx, double* total_ms, int64_t* launches);
+
 /* Tensor-core PSD values (fp32, bins 1..L/2) of n rows, for error analysis.
  * out: n x (L/2) floats, HOST memory. */
 int gp_psd_tc_values(gp_ctx* ctx, const int8_t* seqs, int64_t n, int L, float* out);

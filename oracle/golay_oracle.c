@@ -973,7 +973,7 @@ int gpo_uncompress(int order, int compress, int new_compress, int pafc, const ch
                    const char* out_pairs, const char* work_dir, const char* prefix) {
     if (compress <= 1) return 0;
     const int L = order / compress;
-    char fa[4096], fb[4096], fas[4096], fbs[4096];
+    char fa[4096], fb[4096], fas[4200], fbs[4200];
     snprintf(fa, sizeof fa, "%s/%suncompress_tmp_a", work_dir, prefix ? prefix : "");
     snprintf(fb, sizeof fb, "%s/%suncompress_tmp_b", work_dir, prefix ? prefix : "");
     snprintf(fas, sizeof fas, "%s.sorted", fa);
