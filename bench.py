@@ -210,8 +210,12 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     ctx = gp.Context(local)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated (non-default) stream: the library enqueues on exactly this
+    # stream, so CUDA events recorded on it bracket the kernels
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     sptr = stream.cuda_stream
+    assert sptr != 0
 
     global ROWS
     ROWS = args.rows
@@ -343,7 +347,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--rows", type=int, default=1 << 28, help="batch rows (profiling runs only)")

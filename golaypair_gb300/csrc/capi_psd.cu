@@ -31,6 +31,62 @@ const void* gp_ctx::twiddle_image(int L) {
     return b.p;
 }
 
+const double* gp_ctx::twiddle64(int L) {
+    auto it = twiddles64.find(L);
+    if (it != twiddles64.end()) return it->second.as<double>();
+    std::vector<double> t(2 * (size_t)L);
+    gp::build_twiddle64(L, t.data());
+    DevBuf& b = twiddles64[L];
+    if (!b.ensure(t.size() * 8)) return nullptr;
+    if (cudaMemcpy(b.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    return b.as<double>();
+}
+
+int gp_ctx::enqueue_filter(const gp::RowSrc& src, int64_t n, int order, int paf, int mode, uint32_t* d_mask,
+                           uint32_t* d_unsure, unsigned long long* d_ucount, cudaStream_t st) {
+    const int L = src.L;
+    const int64_t words = (n + 31) / 32;
+    const double* tw = twiddle64(L);
+    if (!tw) return fail(GP_ERR_NOMEM, "twiddle table");
+    if (mode == GP_PSD_FP64) {
+        gp::PsdF64Args a{src, tw, n, threshold(order, paf), d_mask, words};
+        cudaEvent_t tb;
+        time_begin(st, &tb);
+        GP_CUDA_TRY(this, gp::launch_psd_fp64(a, st));
+        time_end(st, tb);
+        return GP_OK;
+    }
+    const void* img = twiddle_image(L);
+    if (!img) return fail(GP_ERR_UNSUPPORTED, "tensor-core filter: unsupported length %d", L);
+    if (src.words && !gp::tc_packed_supported(L, src.pack_bits))
+        return fail(GP_ERR_UNSUPPORTED, "tensor-core filter: packed length %d x %d bits", L, src.pack_bits);
+    GP_CUDA_TRY(this, cudaMemsetAsync(d_ucount, 0, sizeof(unsigned long long), st));
+    gp::PsdTcArgs a;
+    a.seqs = src.seqs;
+    a.words = src.words;
+    a.pack_bits = src.pack_bits;
+    a.alpha_c = src.alpha_c;
+    a.n = n;
+    a.L = L;
+    a.bimage = img;
+    a.thr = (float)threshold(order, paf);
+    a.guard_cfg = guard_band(order);
+    a.err_coef = gp::tc_err_coef(gp::tc_k_for_len(L));
+    a.mask = d_mask;
+    a.mask_words = words;
+    a.unsure = d_unsure;
+    a.unsure_count = d_ucount;
+    a.unsure_cap = n;
+    a.psd_out = nullptr;
+    a.status = status.as<int>();
+    cudaEvent_t tb;
+    time_begin(st, &tb);
+    GP_CUDA_TRY(this, gp::launch_psd_tc(a, num_sms, st));
+    time_end(st, tb);
+    GP_CUDA_TRY(this, gp::launch_psd_recheck(src, tw, threshold(order, paf), d_unsure, d_ucount, n, d_mask, num_sms, st));
+    return GP_OK;
+}
+
 int gp_ctx::check_status(const char* what) {
     int st = 0;
     cudaError_t e = cudaMemcpy(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost);
@@ -101,6 +157,7 @@ int gp_ctx_destroy(gp_ctx* c) {
         if (c->ev_done[i]) cudaEventDestroy(c->ev_done[i]);
     }
     for (auto& kv : c->twiddles) kv.second.release();
+    for (auto& kv : c->twiddles64) kv.second.release();
     for (auto& b : c->scratch) b.release();
     for (auto& b : c->hscratch) b.release();
     if (c->s_comp) cudaStreamDestroy(c->s_comp);
@@ -138,43 +195,14 @@ int gp_kernel_time(gp_ctx* c, double* total_ms, int64_t* launches) {
 
 int gp_device_sm_count(const gp_ctx* c) { return c ? c->num_sms : 0; }
 
-// Enqueues the filter of one device-resident batch (n < 2^31) on `st`.
-// unsure/unsure_count: scratch for the TC mode.
-static int enqueue_filter(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int order, int paf, int mode,
-                          uint32_t* d_mask, uint32_t* d_unsure, unsigned long long* d_ucount, cudaStream_t st) {
-    const int64_t words = (n + 31) / 32;
-    if (mode == GP_PSD_FP64) {
-        gp::PsdF64Args a{d_seqs, n, L, threshold(order, paf), d_mask, words};
-        cudaEvent_t tb;
-        c->time_begin(st, &tb);
-        GP_CUDA_TRY(c, gp::launch_psd_fp64(a, st));
-        c->time_end(st, tb);
-        return GP_OK;
-    }
-    const void* img = c->twiddle_image(L);
-    if (!img) return c->fail(GP_ERR_UNSUPPORTED, "tensor-core filter: unsupported length %d", L);
-    GP_CUDA_TRY(c, cudaMemsetAsync(d_ucount, 0, sizeof(unsigned long long), st));
-    gp::PsdTcArgs a;
-    a.seqs = d_seqs;
-    a.n = n;
-    a.L = L;
-    a.bimage = img;
-    a.thr = (float)threshold(order, paf);
-    a.guard_cfg = guard_band(order);
-    a.err_coef = gp::tc_err_coef(gp::tc_k_for_len(L));
-    a.mask = d_mask;
-    a.mask_words = words;
-    a.unsure = d_unsure;
-    a.unsure_count = d_ucount;
-    a.unsure_cap = n;
-    a.psd_out = nullptr;
-    a.status = c->status.as<int>();
-    cudaEvent_t tb;
-    c->time_begin(st, &tb);
-    GP_CUDA_TRY(c, gp::launch_psd_tc(a, c->num_sms, st));
-    c->time_end(st, tb);
-    GP_CUDA_TRY(c, gp::launch_psd_recheck(d_seqs, L, threshold(order, paf), d_unsure, d_ucount, n, d_mask, st));
-    return GP_OK;
+static gp::RowSrc int8_src(const int8_t* d, int L) {
+    gp::RowSrc r;
+    r.seqs = d;
+    r.words = nullptr;
+    r.L = L;
+    r.pack_bits = 0;
+    r.alpha_c = 0;
+    return r;
 }
 
 static int64_t popcount_words(const uint32_t* w, int64_t nwords) {
@@ -217,8 +245,8 @@ int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, in
                                        c->s_copy));
         GP_CUDA_TRY(c, cudaEventRecord(c->ev_h2d[b], c->s_copy));
         GP_CUDA_TRY(c, cudaStreamWaitEvent(c->s_comp, c->ev_h2d[b], 0));
-        rc = enqueue_filter(c, c->seq_buf[b].as<int8_t>(), rows, L, order, paf, mode, c->mask_buf[b].as<uint32_t>(),
-                            c->unsure_buf[b].as<uint32_t>(), d_counts + b, c->s_comp);
+        rc = c->enqueue_filter(int8_src(c->seq_buf[b].as<int8_t>(), L), rows, order, paf, mode,
+                               c->mask_buf[b].as<uint32_t>(), c->unsure_buf[b].as<uint32_t>(), d_counts + b, c->s_comp);
         if (rc) return rc;
         GP_CUDA_TRY(c, cudaMemcpyAsync(pass_mask + r0 / 32, c->mask_buf[b].p, (size_t)(rows + 31) / 32 * 4,
                                        cudaMemcpyDeviceToHost, c->s_comp));
@@ -256,8 +284,8 @@ int gp_psd_filter_device(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int 
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->s_comp;
     if (mode == GP_PSD_TC_GUARDED && !c->unsure_buf[0].ensure((size_t)std::max<int64_t>(n, 1) * 4))
         return c->fail(GP_ERR_NOMEM, "psd filter: device allocation failed");
-    rc = enqueue_filter(c, d_seqs, n, L, order, paf, mode, d_mask, c->unsure_buf[0].as<uint32_t>(),
-                        c->counts.as<unsigned long long>(), st);
+    rc = c->enqueue_filter(int8_src(d_seqs, L), n, order, paf, mode, d_mask, c->unsure_buf[0].as<uint32_t>(),
+                           c->counts.as<unsigned long long>(), st);
     if (rc) return rc;
     if (stats) {
         GP_CUDA_TRY(c, cudaStreamSynchronize(st));
@@ -296,6 +324,9 @@ int gp_psd_tc_values(gp_ctx* c, const int8_t* seqs, int64_t n, int L, float* out
     GP_CUDA_TRY(c, cudaMemset(c->counts.p, 0, sizeof(unsigned long long)));
     gp::PsdTcArgs a;
     a.seqs = ds.as<int8_t>();
+    a.words = nullptr;
+    a.pack_bits = 0;
+    a.alpha_c = 0;
     a.n = n;
     a.L = L;
     a.bimage = img;
@@ -330,7 +361,9 @@ int gp_psd_fp64_values(gp_ctx* c, const int8_t* seqs, int64_t n, int L, double* 
     if (!ds.ensure((size_t)n * L + 16) || !dv.ensure((size_t)n * L * 8))
         return c->fail(GP_ERR_NOMEM, "allocation failed");
     GP_CUDA_TRY(c, cudaMemcpy(ds.p, seqs, (size_t)n * L, cudaMemcpyHostToDevice));
-    GP_CUDA_TRY(c, gp::launch_psd_fp64_values(ds.as<int8_t>(), n, L, dv.as<double>(), c->s_comp));
+    const double* tw = c->twiddle64(L);
+    if (!tw) return c->fail(GP_ERR_NOMEM, "twiddle table");
+    GP_CUDA_TRY(c, gp::launch_psd_fp64_values(int8_src(ds.as<int8_t>(), L), tw, n, dv.as<double>(), c->s_comp));
     GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_comp));
     GP_CUDA_TRY(c, cudaMemcpy(out, dv.p, (size_t)n * L * 8, cudaMemcpyDeviceToHost));
     return GP_OK;

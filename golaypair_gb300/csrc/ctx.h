@@ -83,7 +83,8 @@ struct gp_ctx {
     DevBuf seq_buf[2];
     DevBuf mask_buf[2];
     DevBuf unsure_buf[2];
-    std::map<int, DevBuf> twiddles;  // by L
+    std::map<int, DevBuf> twiddles;    // tensor-core B images, by L
+    std::map<int, DevBuf> twiddles64;  // FP64 (cos, sin) tables, by L
     // optional CUDA-event timing of the main filter kernel (profiling)
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;
@@ -118,6 +119,12 @@ struct gp_ctx {
     }
     // device twiddle image for length L (tensor-core filter)
     const void* twiddle_image(int L);
+    // device FP64 twiddle table for length L
+    const double* twiddle64(int L);
+    // Enqueues the PSD filter of a device batch (int8 rows or packed words)
+    // on st: mask bit = pass; TC mode rechecks its unsure rows in FP64.
+    int enqueue_filter(const gp::RowSrc& src, int64_t n, int order, int paf, int mode, uint32_t* d_mask,
+                       uint32_t* d_unsure, unsigned long long* d_ucount, cudaStream_t st);
     // reads the kernel status word; resets it; returns a GP code
     int check_status(const char* what);
 };

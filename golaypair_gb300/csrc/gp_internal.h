@@ -18,7 +18,10 @@ constexpr int kMaxLen = 512;    // longest sequence any kernel takes
 
 // ------------------------------------------------------------ PSD filter
 struct PsdTcArgs {
-    const int8_t* seqs;      // n x L, row-major
+    const int8_t* seqs;      // n x L, row-major (int8 input), or nullptr
+    const uint4* words;      // n packed words (packed input), or nullptr
+    int pack_bits;           // packed: bits per digit (1..4)
+    int alpha_c;             // packed: value = 2*digit - alpha_c (also bounds |value|)
     int64_t n;
     int L;
     const void* bimage;      // twiddles: hi tile then lo tile, UMMA smem image
@@ -38,27 +41,40 @@ struct PsdTcArgs {
 // Returns its size in bytes; writes it to out when out != nullptr.
 size_t build_twiddle_image(int L, int K, void* out);
 int tc_k_for_len(int L);               // padded K (multiple of 16), or 0 if unsupported
+bool tc_packed_supported(int L, int b);  // packed-word input with b bits per digit
 float tc_err_coef(int K);              // |X| error per unit of sum|x|
 
 cudaError_t launch_psd_tc(const PsdTcArgs& a, int num_sms, cudaStream_t st);
 
-struct PsdF64Args {
+// Where the FP64 kernels read candidate rows: int8 rows or packed words.
+struct RowSrc {
     const int8_t* seqs;
-    int64_t n;
+    const uint4* words;
     int L;
+    int pack_bits;
+    int alpha_c;
+};
+
+// FP64 twiddle table: tw[m] = (cos, sin)(2 pi m / L), m = 0..L-1
+void build_twiddle64(int L, double* out /* 2L doubles */);
+
+struct PsdF64Args {
+    RowSrc src;
+    const double* tw;
+    int64_t n;
     double thr;
     uint32_t* mask;
     int64_t mask_words;
 };
 cudaError_t launch_psd_fp64(const PsdF64Args& a, cudaStream_t st);
 
-// FP64 recheck of the unsure list: clears the mask bit of every unsure
-// candidate that fails the exact filter.
-cudaError_t launch_psd_recheck(const int8_t* seqs, int L, double thr, const uint32_t* unsure,
+// FP64 recheck of the unsure list (one warp per row): clears the mask bit of
+// every unsure candidate that fails the exact filter.
+cudaError_t launch_psd_recheck(const RowSrc& src, const double* tw, double thr, const uint32_t* unsure,
                                const unsigned long long* unsure_count, int64_t cap, uint32_t* mask,
-                               cudaStream_t st);
+                               int num_sms, cudaStream_t st);
 
-// Exact FP64 PSD values (all L bins) for a list of rows (testing/signatures)
-cudaError_t launch_psd_fp64_values(const int8_t* seqs, int64_t n, int L, double* out, cudaStream_t st);
+// Exact FP64 PSD values (all L bins) of rows 0..n-1 (testing)
+cudaError_t launch_psd_fp64_values(const RowSrc& src, const double* tw, int64_t n, double* out, cudaStream_t st);
 
 }  // namespace gp

@@ -1,14 +1,18 @@
 // psd_fp64.cu -- plain FP64 CUDA-core PSD kernels.
 //
 // Restates src/utils/fourier.cpp:25-52 in double precision as a direct DFT
-// whose twiddle for (j, k) is exp(-2 pi i ((j k) mod L) / L), kept in shared
-// memory.  Three uses:
+// whose twiddle for (j, k) is exp(-2 pi i ((j k) mod L) / L), read from a
+// table kept in shared memory.  Three uses:
 //   * psd_fp64_filter: the plain FP64 filter (the comparator of the
 //     tensor-core path): one candidate per thread, bins k = 1..L/2 in order,
 //     stopping at the first bin above the bound;
-//   * psd_recheck: exact verdict for the tensor core's "unsure" candidates;
-//   * psd_fp64_values: every bin of a batch (signatures and tests).
-#include "gp_internal.h"
+//   * psd_recheck: exact verdict for the tensor core's "unsure" candidates,
+//     one warp per candidate (lanes split the bins);
+//   * psd_fp64_values: every bin of a batch (tests).
+#include <cmath>
+
+#include "gp_device.cuh"
+#include "rows.cuh"
 
 namespace gp {
 
@@ -16,132 +20,139 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__device__ __forceinline__ void load_twiddles(double* cs, double* sn, int L) {
-    const double two_pi = 6.283185307179586476925286766559;
-    for (int m = threadIdx.x; m < L; m += blockDim.x) {
-        double s, c;
-        sincospi(2.0 * (double)m / (double)L, &s, &c);
-        cs[m] = c;
-        sn[m] = s;
-        (void)two_pi;
-    }
+__device__ __forceinline__ void load_tw(double2* stw, const double* tw, int L) {
+    for (int m = threadIdx.x; m < L; m += blockDim.x) stw[m] = make_double2(tw[2 * m], tw[2 * m + 1]);
 }
 
-// Stages a block's rows (blockDim x L bytes) into shared memory with
-// coalesced loads; returns the row of this thread.
-__device__ __forceinline__ const int8_t* stage_rows(const int8_t* seqs, int64_t n, int L, int8_t* srows) {
-    const int64_t row0 = (int64_t)blockIdx.x * blockDim.x;
-    int64_t rows = n - row0;
-    if (rows > blockDim.x) rows = blockDim.x;
-    const int64_t bytes = rows * L;
-    const int8_t* src = seqs + row0 * L;
-    for (int64_t i = threadIdx.x; i < bytes; i += blockDim.x) srows[i] = src[i];
-    __syncthreads();
-    return srows + (int64_t)threadIdx.x * L;
-}
-
-__device__ __forceinline__ bool fp64_pass(const int8_t* x, int L, const double* cs, const double* sn, double thr) {
-    const int H = L / 2;
-    for (int k = 1; k <= H; ++k) {
-        double re = 0.0, im = 0.0;
-        int m = 0;
-        for (int j = 0; j < L; ++j) {
-            const double v = (double)x[j];
-            re = fma(v, cs[m], re);
-            im = fma(-v, sn[m], im);
-            m += k;
-            if (m >= L) m -= L;
-        }
-        if (re * re + im * im > thr) return false;
+__device__ __forceinline__ double bin_power(const int8_t* x, int L, int k, const double2* tw) {
+    double re = 0.0, im = 0.0;
+    int m = 0;
+    for (int j = 0; j < L; ++j) {
+        const double v = (double)x[j];
+        const double2 w = tw[m];
+        re = fma(v, w.x, re);
+        im = fma(-v, w.y, im);
+        m += k;
+        if (m >= L) m -= L;
     }
-    return true;
+    return re * re + im * im;
 }
 
 __global__ void __launch_bounds__(kBlock) psd_fp64_filter_kernel(PsdF64Args a) {
-    extern __shared__ double sh64[];
-    double* cs = sh64;
-    double* sn = sh64 + a.L;
-    int8_t* srows = reinterpret_cast<int8_t*>(sn + a.L);
-    load_twiddles(cs, sn, a.L);
-    const int8_t* x = stage_rows(a.seqs, a.n, a.L, srows);
-    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = row < a.n;
-    const bool pass = valid && fp64_pass(x, a.L, cs, sn, a.thr);
+    extern __shared__ double2 sh_tw[];
+    const int L = a.src.L;
+    int8_t* srows = reinterpret_cast<int8_t*>(sh_tw + L);
+    load_tw(sh_tw, a.tw, L);
+    const int64_t row0 = (int64_t)blockIdx.x * blockDim.x;
+    int64_t rows = a.n - row0;
+    if (rows > blockDim.x) rows = blockDim.x;
+    // stage this block's rows (coalesced)
+    if (a.src.seqs) {
+        const int8_t* src = a.src.seqs + row0 * L;
+        for (int64_t i = threadIdx.x; i < rows * L; i += blockDim.x) srows[i] = src[i];
+    } else {
+        for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) decode_row(a.src, row0 + r, srows + r * L);
+    }
+    __syncthreads();
+    const int64_t row = row0 + threadIdx.x;
+    bool pass = false;
+    if (row < a.n) {
+        const int8_t* x = srows + (int64_t)threadIdx.x * L;
+        pass = true;
+        for (int k = 1; k <= L / 2; ++k)
+            if (bin_power(x, L, k, sh_tw) > a.thr) {
+                pass = false;
+                break;
+            }
+    }
     const uint32_t bits = __ballot_sync(0xFFFFFFFFu, pass);
     const int64_t word = row >> 5;
     if ((threadIdx.x & 31) == 0 && word < a.mask_words) a.mask[word] = bits;
 }
 
-__global__ void __launch_bounds__(kBlock) psd_recheck_kernel(const int8_t* seqs, int L, double thr,
+// one warp per unsure row; lane l computes bins l+1, l+33, ...
+__global__ void __launch_bounds__(kBlock) psd_recheck_kernel(RowSrc src, const double* tw, double thr,
                                                              const uint32_t* unsure,
                                                              const unsigned long long* unsure_count, int64_t cap,
                                                              uint32_t* mask) {
-    extern __shared__ double sh64[];
-    double* cs = sh64;
-    double* sn = sh64 + L;
-    load_twiddles(cs, sn, L);
+    extern __shared__ double2 sh_tw[];
+    const int L = src.L;
+    int8_t* xs = reinterpret_cast<int8_t*>(sh_tw + L) + (threadIdx.x >> 5) * kMaxLen;
+    load_tw(sh_tw, tw, L);
     __syncthreads();
     int64_t cnt = (int64_t)*unsure_count;
     if (cnt > cap) cnt = cap;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < cnt; i += warps) {
         const uint32_t row = unsure[i];
-        if (!fp64_pass(seqs + (int64_t)row * L, L, cs, sn, thr)) atomicAnd(&mask[row >> 5], ~(1u << (row & 31)));
+        if (src.seqs) {
+            for (int j = lane; j < L; j += 32) xs[j] = src.seqs[(int64_t)row * L + j];
+        } else if (lane == 0) {
+            decode_row(src, row, xs);
+        }
+        __syncwarp();
+        bool fail = false;
+        for (int k = lane + 1; k <= L / 2; k += 32) fail |= bin_power(xs, L, k, sh_tw) > thr;
+        fail = __any_sync(0xFFFFFFFFu, fail);
+        if (fail && lane == 0) atomicAnd(&mask[row >> 5], ~(1u << (row & 31)));
+        __syncwarp();
     }
 }
 
-__global__ void __launch_bounds__(kBlock) psd_values_kernel(const int8_t* seqs, int64_t n, int L, double* out) {
-    extern __shared__ double sh64[];
-    double* cs = sh64;
-    double* sn = sh64 + L;
-    int8_t* srows = reinterpret_cast<int8_t*>(sn + L);
-    load_twiddles(cs, sn, L);
-    const int8_t* x = stage_rows(seqs, n, L, srows);
+__global__ void __launch_bounds__(kBlock) psd_values_kernel(RowSrc src, const double* tw, int64_t n, double* out) {
+    extern __shared__ double2 sh_tw[];
+    const int L = src.L;
+    int8_t* xs = reinterpret_cast<int8_t*>(sh_tw + L) + (int64_t)threadIdx.x * L;
+    load_tw(sh_tw, tw, L);
+    __syncthreads();
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= n) return;
-    for (int k = 0; k < L; ++k) {
-        double re = 0.0, im = 0.0;
-        int m = 0;
-        for (int j = 0; j < L; ++j) {
-            const double v = (double)x[j];
-            re = fma(v, cs[m], re);
-            im = fma(-v, sn[m], im);
-            m += k;
-            if (m >= L) m -= L;
-        }
-        out[row * L + k] = re * re + im * im;
-    }
+    decode_row(src, row, xs);
+    for (int k = 0; k < L; ++k) out[row * L + k] = bin_power(xs, L, k, sh_tw);
 }
 
 }  // namespace
 
+void build_twiddle64(int L, double* out) {
+    for (int m = 0; m < L; ++m) {
+        const long double ang = 6.283185307179586476925286766559L * (long double)m / (long double)L;
+        out[2 * m] = (double)std::cos(ang);
+        out[2 * m + 1] = (double)std::sin(ang);
+    }
+}
+
 cudaError_t launch_psd_fp64(const PsdF64Args& a, cudaStream_t st) {
     if (a.n == 0) return cudaSuccess;
     const int64_t blocks = (a.n + kBlock - 1) / kBlock;
-    const size_t smem = 2 * sizeof(double) * a.L + (size_t)kBlock * a.L + 16;
-    cudaError_t e = cudaFuncSetAttribute(psd_fp64_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = sizeof(double2) * a.src.L + (size_t)kBlock * a.src.L + 16;
+    cudaError_t e =
+        cudaFuncSetAttribute(psd_fp64_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     psd_fp64_filter_kernel<<<(unsigned)blocks, kBlock, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_psd_recheck(const int8_t* seqs, int L, double thr, const uint32_t* unsure,
-                               const unsigned long long* unsure_count, int64_t cap, uint32_t* mask,
+cudaError_t launch_psd_recheck(const RowSrc& src, const double* tw, double thr, const uint32_t* unsure,
+                               const unsigned long long* unsure_count, int64_t cap, uint32_t* mask, int num_sms,
                                cudaStream_t st) {
     if (cap <= 0) return cudaSuccess;
-    int64_t blocks = (cap + kBlock - 1) / kBlock;
-    if (blocks > 4096) blocks = 4096;
-    const size_t smem = 2 * sizeof(double) * L;
-    psd_recheck_kernel<<<(unsigned)blocks, kBlock, smem, st>>>(seqs, L, thr, unsure, unsure_count, cap, mask);
+    int64_t blocks = (cap + (kBlock / 32) - 1) / (kBlock / 32);
+    if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
+    const size_t smem = sizeof(double2) * src.L + (size_t)(kBlock / 32) * kMaxLen;
+    cudaError_t e = cudaFuncSetAttribute(psd_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    psd_recheck_kernel<<<(unsigned)blocks, kBlock, smem, st>>>(src, tw, thr, unsure, unsure_count, cap, mask);
     return cudaGetLastError();
 }
 
-cudaError_t launch_psd_fp64_values(const int8_t* seqs, int64_t n, int L, double* out, cudaStream_t st) {
+cudaError_t launch_psd_fp64_values(const RowSrc& src, const double* tw, int64_t n, double* out, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     const int64_t blocks = (n + kBlock - 1) / kBlock;
-    const size_t smem = 2 * sizeof(double) * L + (size_t)kBlock * L + 16;
+    const size_t smem = sizeof(double2) * src.L + (size_t)kBlock * src.L + 16;
     cudaError_t e = cudaFuncSetAttribute(psd_values_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    psd_values_kernel<<<(unsigned)blocks, kBlock, smem, st>>>(seqs, n, L, out);
+    psd_values_kernel<<<(unsigned)blocks, kBlock, smem, st>>>(src, tw, n, out);
     return cudaGetLastError();
 }
 

@@ -8,7 +8,8 @@
 //       one fp32 TMEM accumulator)   ->   re_k, im_k  ->  p_k = re^2 + im^2.
 //
 // Row n < N/2 of W is the cosine of bin n+1, row N/2 + n the sine of bin n+1;
-// bins above L/2 are zero rows.  K = N = L rounded up to 16.
+// bins above L/2 and columns j >= L are zero, so the padding columns of X
+// never contribute.  K = N = L rounded up to 16.
 //
 // Each candidate is classified against T = 2n - paf + 0.001 with a guard g
 // (the configured band, widened per row to a rigorous bound on the fp32
@@ -16,11 +17,17 @@
 // appended to a list that an FP64 kernel rechecks exactly.  The pass mask
 // bit is set for pass and unsure; the recheck clears the failing unsure ones.
 //
+// Two input forms:
+//   int8 rows    n x L bytes (the batched filter's input);
+//   packed words one 16-byte word per candidate, digit j in bits
+//                [b(L-1-j), b(L-j)), value = 2*digit - c (the enumerator's
+//                and the uncompression expander's output).
+//
 // Persistent kernel, one 128-candidate tile per step, warp roles:
-//   warps 0-3  convert: int8 rows (staged by the bulk-copy engine) -> fp16
-//              A tile in the UMMA canonical K-major layout, plus sum |x|
+//   warps 0-3  convert: staged tile -> fp16 A tile in the UMMA canonical
+//              K-major layout (+ sum x^2 for the int8 error bound)
 //   warps 4-7  epilogue: TMEM -> registers -> PSD max -> mask / unsure list
-//   warp 8     producer: cp.async.bulk of each 128 x L byte tile
+//   warp 8     producer: cp.async.bulk of each tile into a deep ring
 //   warp 9     MMA issuer (one lane) and TMEM owner
 #include <cmath>
 #include <cstring>
@@ -34,6 +41,10 @@ namespace {
 
 constexpr int kThreads = 320;
 constexpr int kRawSlack = 64;
+constexpr int kMaxRawStages = 12;
+constexpr uint32_t kSmemBudget2Cta = 112 * 1024;  // two CTAs per SM
+constexpr uint32_t kSmemBudget1Cta = 220 * 1024;
+constexpr int kLutBytes = 4096;
 
 template <int K>
 struct TcCfg {
@@ -45,19 +56,19 @@ struct TcCfg {
     static constexpr int A_KSTRIDE = (M / 8) * 128;    // bytes between K-adjacent core matrices
     static constexpr int B_BYTES = N * K * 2;
     static constexpr int B_KSTRIDE = (N / 8) * 128;
-    static constexpr int STAGES = K <= 64 ? 4 : 2;
+    static constexpr int A_STAGES = K <= 64 ? 3 : 2;
     static constexpr int NACC = (256 / N) < 4 ? (256 / N) : 4;
-    static constexpr int RING = STAGES + NACC;         // sum|x| stash slots
+    static constexpr int RING = A_STAGES + NACC;       // sum x^2 stash slots
     static constexpr int TMEM_COLS = 256;
     static constexpr int MIN_BLOCKS = K <= 64 ? 2 : 1;
 };
 
 struct SmemLayout {
-    uint32_t b_off, a_off, raw_off, raw_stride, stash_off, bar_off, misc_off, total;
+    uint32_t b_off, a_off, lut_off, raw_off, raw_stride, raw_stages, stash_off, bar_off, misc_off, total;
 };
 
 template <int K>
-SmemLayout smem_layout(int L) {
+SmemLayout smem_layout(int row_bytes) {
     using C = TcCfg<K>;
     SmemLayout s;
     uint32_t off = 0;
@@ -65,24 +76,95 @@ SmemLayout smem_layout(int L) {
     off += 2 * C::B_BYTES;
     off = (off + 1023) & ~1023u;
     s.a_off = off;
-    off += C::STAGES * C::A_BYTES;
-    s.raw_stride = (uint32_t)((kTileM * L + kRawSlack + 127) & ~127);
-    s.raw_off = off;
-    off += C::STAGES * s.raw_stride;
+    off += C::A_STAGES * C::A_BYTES;
+    s.lut_off = off;
+    off += kLutBytes;
     s.stash_off = off;
     off += C::RING * kTileM * 4;
-    off = (off + 7) & ~7u;
     s.bar_off = off;
-    off += (4 * C::STAGES + 2 * C::NACC + C::RING + 2) * 8;
+    off += (2 * kMaxRawStages + 2 * C::A_STAGES + 2 * C::NACC + C::RING + 2) * 8;
     s.misc_off = off;
     off += 16;
+    off = (off + 127) & ~127u;
+    s.raw_stride = (uint32_t)((kTileM * row_bytes + kRawSlack + 127) & ~127);
+    s.raw_off = off;
+    const uint32_t budget = (C::MIN_BLOCKS == 2 ? kSmemBudget2Cta : kSmemBudget1Cta) - 1024;
+    int st = budget > off ? (int)((budget - off) / s.raw_stride) : 0;
+    if (st > kMaxRawStages) st = kMaxRawStages;
+    if (st < 2) st = 2;
+    s.raw_stages = (uint32_t)st;
+    off += st * s.raw_stride;
     s.total = off + 1024;  // slack for the 1024-byte alignment of the base
     // At most two CTAs per SM: each holds 256 TMEM columns (512 per SM).
     if (s.total < 96 * 1024) s.total = 96 * 1024;
     return s;
 }
 
-template <int K, bool WRITE_PSD>
+// Builds the packed-digit lookup table: for b in {1,2,4} a byte of 8/b
+// digits maps to 8/b halves; for b = 3 six bits (two digits) map to a half2.
+// Value of a digit: 2*digit - c.
+__device__ void build_lut(uint8_t* lut, int b, int c) {
+    const int entries = b == 3 ? 64 : 256;
+    const int per = b == 3 ? 2 : 8 / b;  // digits per entry
+    const int bits = b == 3 ? 6 : 8;
+    for (int e = threadIdx.x; e < entries; e += blockDim.x) {
+        for (int d = 0; d < per; ++d) {
+            const int digit = (e >> (bits - b * (d + 1))) & ((1 << b) - 1);
+            reinterpret_cast<__half*>(lut)[e * per + d] = __int2half_rn(2 * digit - c);
+        }
+    }
+}
+
+// 8 halves of digits 8*ch .. 8*ch+7 from the normalised word (digit 0 at bit
+// 127).  w[0] holds bits 0-31 ... w[3] bits 96-127.
+template <int B, int CH>
+__device__ __forceinline__ uint4 packed_chunk(const uint32_t (&w)[4], const uint8_t* lut) {
+    constexpr int WIDTH = 8 * B;
+    constexpr int HI = 128 - WIDTH * CH;  // exclusive top bit of the field
+    constexpr int LO = HI - WIDTH;
+    uint32_t field;
+    if constexpr (HI <= 0) {
+        field = 0;
+    } else if constexpr (LO >= 0) {
+        constexpr int wi = LO >> 5, sh = LO & 31;
+        const uint32_t lo = w[wi];
+        const uint32_t hi = (wi + 1 < 4) ? w[(wi + 1 < 4) ? wi + 1 : 3] : 0u;
+        const uint64_t v = ((uint64_t)hi << 32) | lo;
+        field = (uint32_t)(v >> sh);
+        if constexpr (WIDTH < 32) field &= (1u << WIDTH) - 1u;
+    } else {
+        // field straddles bit 0: the digits below it are padding
+        const uint32_t top = w[0] & ((HI >= 32) ? 0xFFFFFFFFu : ((1u << (HI & 31)) - 1u));
+        field = top << ((-LO) & 31);
+    }
+    uint4 out;
+    if constexpr (B == 1) {
+        out = reinterpret_cast<const uint4*>(lut)[field & 0xFF];
+    } else if constexpr (B == 2) {
+        const uint2 x = reinterpret_cast<const uint2*>(lut)[(field >> 8) & 0xFF];
+        const uint2 y = reinterpret_cast<const uint2*>(lut)[field & 0xFF];
+        out = make_uint4(x.x, x.y, y.x, y.y);
+    } else if constexpr (B == 3) {
+        const uint32_t* l = reinterpret_cast<const uint32_t*>(lut);
+        out = make_uint4(l[(field >> 18) & 63], l[(field >> 12) & 63], l[(field >> 6) & 63], l[field & 63]);
+    } else {
+        const uint32_t* l = reinterpret_cast<const uint32_t*>(lut);
+        out = make_uint4(l[(field >> 24) & 255], l[(field >> 16) & 255], l[(field >> 8) & 255], l[field & 255]);
+    }
+    return out;
+}
+
+template <int B, int KCH, int CH = 0>
+__device__ __forceinline__ void packed_row(const uint32_t (&w)[4], const uint8_t* lut, uint8_t* A, int r,
+                                           int kstride) {
+    if constexpr (CH < KCH) {
+        *reinterpret_cast<uint4*>(A + CH * kstride + r * 16) = packed_chunk<B, CH>(w, lut);
+        packed_row<B, KCH, CH + 1>(w, lut, A, r, kstride);
+    }
+}
+
+// B = 0: int8 rows; B = 1..4: packed words with B bits per digit.
+template <int K, int B, bool WRITE_PSD>
 __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(PsdTcArgs a, SmemLayout lay) {
     using C = TcCfg<K>;
     extern __shared__ uint8_t smem_raw_base[];
@@ -90,18 +172,19 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
 
     uint8_t* sB = smem + lay.b_off;
     uint8_t* sA = smem + lay.a_off;
+    uint8_t* sLut = smem + lay.lut_off;
     uint8_t* sRaw = smem + lay.raw_off;
     float* stash = reinterpret_cast<float*>(smem + lay.stash_off);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bar_off);
     uint64_t* raw_full = bars;
-    uint64_t* raw_empty = bars + C::STAGES;
-    uint64_t* a_full = bars + 2 * C::STAGES;
-    uint64_t* a_empty = bars + 3 * C::STAGES;
-    uint64_t* acc_full = bars + 4 * C::STAGES;
+    uint64_t* raw_empty = bars + kMaxRawStages;
+    uint64_t* a_full = bars + 2 * kMaxRawStages;
+    uint64_t* a_empty = a_full + C::A_STAGES;
+    uint64_t* acc_full = a_empty + C::A_STAGES;
     uint64_t* acc_empty = acc_full + C::NACC;
     uint64_t* b_full = acc_empty + C::NACC;
     uint64_t* final_bar = b_full + 1;
-    uint64_t* stash_full = final_bar + 1;  // RING barriers: sum|x| of a tile is written
+    uint64_t* stash_full = final_bar + 1;  // RING barriers: sum x^2 of a tile is written
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + lay.misc_off);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + lay.misc_off + 4);
 
@@ -110,12 +193,17 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     const int L = a.L;
     const int64_t n = a.n;
     const int64_t ntiles = (n + kTileM - 1) / kTileM;
-    const bool aligned = (reinterpret_cast<uintptr_t>(a.seqs) & 15) == 0;
+    const int RS = (int)lay.raw_stages;
+    const int row_bytes = B == 0 ? L : 16;
+    const bool aligned =
+        (reinterpret_cast<uintptr_t>(B == 0 ? (const void*)a.seqs : (const void*)a.words) & 15) == 0;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < C::STAGES; ++i) {
+        for (int i = 0; i < RS; ++i) {
             mbar_init(&raw_full[i], 1);
             mbar_init(&raw_empty[i], 4);
+        }
+        for (int i = 0; i < C::A_STAGES; ++i) {
             mbar_init(&a_full[i], 4);
             mbar_init(&a_empty[i], 1);
         }
@@ -129,6 +217,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         *abort_flag = 0;
         mbar_fence_init();
     }
+    if constexpr (B != 0) build_lut(sLut, B, a.alpha_c);
     if (warp == 9) {
         tmem_alloc(tmem_slot, C::TMEM_COLS);
         tc_fence_before();
@@ -143,67 +232,95 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         uint32_t mlo[C::KCH], mhi[C::KCH];
 #pragma unroll
         for (int c = 0; c < C::KCH; ++c) {
-            int v = L - 8 * c;
+            const int v = L - 8 * c;
             mlo[c] = v >= 4 ? 0xFFFFFFFFu : (v <= 0 ? 0u : ((1u << (8 * v)) - 1u));
             mhi[c] = v >= 8 ? 0xFFFFFFFFu : (v <= 4 ? 0u : ((1u << (8 * (v - 4))) - 1u));
         }
+        const int norm = 128 - B * L;  // packed: left shift that puts digit 0 at bit 127
         int64_t it = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
-            const int s = (int)(it % C::STAGES);
-            const uint32_t ph = (uint32_t)((it / C::STAGES) & 1);
-            if (!mbar_wait(&raw_full[s], ph, abort_flag, a.status, 1)) break;
-            if (!mbar_wait(&a_empty[s], ph ^ 1u, abort_flag, a.status, 2)) break;
-            uint8_t* A = sA + s * C::A_BYTES;
+            const int rs = (int)(it % RS);
+            const uint32_t rph = (uint32_t)((it / RS) & 1);
+            const int as = (int)(it % C::A_STAGES);
+            const uint32_t aph = (uint32_t)((it / C::A_STAGES) & 1);
+            if (!mbar_wait(&raw_full[rs], rph, abort_flag, a.status, 1)) break;
+            if (!mbar_wait(&a_empty[as], aph ^ 1u, abort_flag, a.status, 2)) break;
+            uint8_t* A = sA + as * C::A_BYTES;
             const int64_t row = t * kTileM + r;
             const bool full_tile = aligned && (t + 1) * kTileM <= n;
-            uint32_t sabs = 0;
-            if (full_tile) {
-                const uint8_t* raw = sRaw + s * lay.raw_stride;
-                const int off = r * L;
+            int sumsq = 0;
+            if constexpr (B == 0) {
+                if (full_tile) {
+                    const uint8_t* raw = sRaw + rs * lay.raw_stride;
+                    const int off = r * L;
 #pragma unroll
-                for (int c = 0; c < C::KCH; ++c) {
-                    const int o = off + 8 * c;
-                    const int base = o & ~3;
-                    const uint32_t sh = (uint32_t)(o & 3) * 8u;
-                    const uint32_t w0 = *reinterpret_cast<const uint32_t*>(raw + base);
-                    const uint32_t w1 = *reinterpret_cast<const uint32_t*>(raw + base + 4);
-                    const uint32_t w2 = *reinterpret_cast<const uint32_t*>(raw + base + 8);
-                    const uint32_t lo = __funnelshift_r(w0, w1, sh) & mlo[c];
-                    const uint32_t hi = __funnelshift_r(w1, w2, sh) & mhi[c];
-                    sabs = __dp4a(__vabs4(lo), 0x01010101u, sabs);
-                    sabs = __dp4a(__vabs4(hi), 0x01010101u, sabs);
-                    uint4 h;
-                    i8x4_to_h2x2(lo, h.x, h.y);
-                    i8x4_to_h2x2(hi, h.z, h.w);
-                    *reinterpret_cast<uint4*>(A + c * C::A_KSTRIDE + r * 16) = h;
+                    for (int c = 0; c < C::KCH; ++c) {
+                        const int o = off + 8 * c;
+                        const int base = o & ~3;
+                        const uint32_t sh = (uint32_t)(o & 3) * 8u;
+                        const uint32_t w0 = *reinterpret_cast<const uint32_t*>(raw + base);
+                        const uint32_t w1 = *reinterpret_cast<const uint32_t*>(raw + base + 4);
+                        const uint32_t w2 = *reinterpret_cast<const uint32_t*>(raw + base + 8);
+                        const uint32_t lo = __funnelshift_r(w0, w1, sh) & mlo[c];
+                        const uint32_t hi = __funnelshift_r(w1, w2, sh) & mhi[c];
+                        sumsq = __dp4a((int)lo, (int)lo, sumsq);
+                        sumsq = __dp4a((int)hi, (int)hi, sumsq);
+                        uint4 h;
+                        i8x4_to_h2x2(lo, h.x, h.y);
+                        i8x4_to_h2x2(hi, h.z, h.w);
+                        *reinterpret_cast<uint4*>(A + c * C::A_KSTRIDE + r * 16) = h;
+                    }
+                } else {
+                    const bool valid = row < n;
+                    const int8_t* src = a.seqs + (valid ? row : 0) * (int64_t)L;
+#pragma unroll
+                    for (int c = 0; c < C::KCH; ++c) {
+                        uint32_t w[2] = {0u, 0u};
+#pragma unroll
+                        for (int bb = 0; bb < 8; ++bb) {
+                            const int j = 8 * c + bb;
+                            const uint32_t v = (valid && j < L) ? (uint32_t)(uint8_t)src[j] : 0u;
+                            w[bb >> 2] |= v << (8 * (bb & 3));
+                        }
+                        sumsq = __dp4a((int)w[0], (int)w[0], sumsq);
+                        sumsq = __dp4a((int)w[1], (int)w[1], sumsq);
+                        uint4 h;
+                        i8x4_to_h2x2(w[0], h.x, h.y);
+                        i8x4_to_h2x2(w[1], h.z, h.w);
+                        *reinterpret_cast<uint4*>(A + c * C::A_KSTRIDE + r * 16) = h;
+                    }
                 }
             } else {
-                const bool valid = row < n;
-                const int8_t* src = a.seqs + (valid ? row : 0) * (int64_t)L;
-#pragma unroll
-                for (int c = 0; c < C::KCH; ++c) {
-                    uint32_t w[2] = {0u, 0u};
-#pragma unroll
-                    for (int b = 0; b < 8; ++b) {
-                        const int j = 8 * c + b;
-                        const uint32_t v = (valid && j < L) ? (uint32_t)(uint8_t)src[j] : 0u;
-                        w[b >> 2] |= v << (8 * (b & 3));
-                    }
-                    sabs = __dp4a(__vabs4(w[0]), 0x01010101u, sabs);
-                    sabs = __dp4a(__vabs4(w[1]), 0x01010101u, sabs);
-                    uint4 h;
-                    i8x4_to_h2x2(w[0], h.x, h.y);
-                    i8x4_to_h2x2(w[1], h.z, h.w);
-                    *reinterpret_cast<uint4*>(A + c * C::A_KSTRIDE + r * 16) = h;
+                uint4 wv;
+                if (full_tile) {
+                    wv = *reinterpret_cast<const uint4*>(sRaw + rs * lay.raw_stride + r * 16);
+                } else {
+                    wv = row < n ? a.words[row] : make_uint4(0, 0, 0, 0);
                 }
+                // normalise: 128-bit left shift by `norm` puts digit 0 at bit 127
+                const uint32_t w[4] = {wv.x, wv.y, wv.z, wv.w};
+                uint32_t s[4];
+                const int ws = norm >> 5, bs = norm & 31;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int si = i - ws;
+                    uint32_t cur = 0u, prev = 0u;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        cur = (si == k) ? w[k] : cur;
+                        prev = (si - 1 == k) ? w[k] : prev;
+                    }
+                    s[i] = bs ? ((cur << bs) | (prev >> (32 - bs))) : cur;
+                }
+                packed_row<B, C::KCH>(s, sLut, A, r, C::A_KSTRIDE);
             }
-            stash[(int)(it % C::RING) * kTileM + r] = (float)sabs;
+            if constexpr (B == 0) stash[(int)(it % C::RING) * kTileM + r] = (float)sumsq;
             fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) {
-                mbar_arrive(&stash_full[(int)(it % C::RING)]);
-                mbar_arrive(&a_full[s]);
-                mbar_arrive(&raw_empty[s]);
+                if constexpr (B == 0) mbar_arrive(&stash_full[(int)(it % C::RING)]);
+                mbar_arrive(&a_full[as]);
+                mbar_arrive(&raw_empty[rs]);
             }
         }
     } else if (warp < 8) {
@@ -211,6 +328,9 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         const int q = warp - 4;  // TMEM lane quarter
         const float thr = a.thr;
         const float sq = sqrtf(thr);
+        // packed rows: |value| <= c, so sum|x| <= L c for every row
+        const float d_const = a.err_coef * (float)L * (float)a.alpha_c;
+        const float g_const = fmaxf(a.guard_cfg, 2.f * sq * d_const + 3.f * d_const * d_const + 1e-4f);
         int64_t it = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             const int b = (int)(it % C::NACC);
@@ -223,26 +343,32 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             for (int c = 0; c < C::N / 16; ++c) tmem_ld16(taddr + 16 * c, v + 16 * c);
             tmem_wait_ld();
             const int r = q * 32 + lane;
-            // The converters wrote sum|x| for this tile before the A tile was
-            // released to the MMA, and cannot lap the RING slots: the MMA of
-            // a later use waits for this epilogue to free its accumulator.
-            const int slot = (int)(it % C::RING);
-            if (!mbar_wait(&stash_full[slot], (uint32_t)((it / C::RING) & 1), abort_flag, a.status, 11)) break;
-            const float sabs = stash[slot * kTileM + r];
+            float g = g_const;
+            if constexpr (B == 0) {
+                // The converters wrote sum x^2 for this tile before the A tile
+                // was released to the MMA, and cannot lap the RING slots: the
+                // MMA of a later use waits for this epilogue to free its
+                // accumulator.
+                const int slot = (int)(it % C::RING);
+                if (!mbar_wait(&stash_full[slot], (uint32_t)((it / C::RING) & 1), abort_flag, a.status, 11)) break;
+                // sum|x| <= sqrt(L * sum x^2)
+                const float d = a.err_coef * sqrtf((float)L * stash[slot * kTileM + r]);
+                g = fmaxf(a.guard_cfg, 2.f * sq * d + 3.f * d * d + 1e-4f);
+            }
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[b]);
 
             float pmax = 0.f;
 #pragma unroll
-            for (int k = 0; k < C::N / 2; ++k) {
-                const float p = fmaf(v[k], v[k], v[C::N / 2 + k] * v[C::N / 2 + k]);
-                pmax = fmaxf(pmax, p);
+            for (int k = 0; k < C::N / 2; k += 2) {
+                const float2 cs = make_float2(v[k], v[k + 1]);
+                const float2 sn = make_float2(v[C::N / 2 + k], v[C::N / 2 + k + 1]);
+                const float2 p = __ffma2_rn(cs, cs, __fmul2_rn(sn, sn));
+                pmax = fmaxf(pmax, fmaxf(p.x, p.y));
             }
             const int64_t row = t * kTileM + r;
             const bool valid = row < n;
-            const float d = sabs * a.err_coef;
-            const float g = fmaxf(a.guard_cfg, 2.f * sq * d + 3.f * d * d + 1e-4f);
             const bool sure = valid && pmax < thr - g;
             const bool unsure = valid && !sure && pmax <= thr + g;
             const uint32_t bits = __ballot_sync(0xFFFFFFFFu, sure || unsure);
@@ -275,28 +401,30 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         if (lane == 0) {
             mbar_arrive_expect_tx(b_full, 2 * C::B_BYTES);
             bulk_g2s(sB, a.bimage, 2 * C::B_BYTES, b_full);
+            const uint8_t* src = B == 0 ? reinterpret_cast<const uint8_t*>(a.seqs)
+                                        : reinterpret_cast<const uint8_t*>(a.words);
             for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
-                const int s = (int)(it % C::STAGES);
-                const uint32_t ph = (uint32_t)((it / C::STAGES) & 1);
-                if (!mbar_wait(&raw_empty[s], ph ^ 1u, abort_flag, a.status, 4)) break;
+                const int rs = (int)(it % RS);
+                const uint32_t ph = (uint32_t)((it / RS) & 1);
+                if (!mbar_wait(&raw_empty[rs], ph ^ 1u, abort_flag, a.status, 4)) break;
                 const bool full_tile = aligned && (t + 1) * kTileM <= n;
                 if (full_tile) {
-                    const uint32_t bytes = (uint32_t)(kTileM * L);
-                    mbar_arrive_expect_tx(&raw_full[s], bytes);
-                    bulk_g2s(sRaw + s * lay.raw_stride, a.seqs + t * kTileM * (int64_t)L, bytes, &raw_full[s]);
+                    const uint32_t bytes = (uint32_t)(kTileM * row_bytes);
+                    mbar_arrive_expect_tx(&raw_full[rs], bytes);
+                    bulk_g2s(sRaw + rs * lay.raw_stride, src + t * kTileM * (int64_t)row_bytes, bytes, &raw_full[rs]);
                 } else {
-                    mbar_arrive(&raw_full[s]);
+                    mbar_arrive(&raw_full[rs]);
                 }
             }
             // Do not leave the CTA with copies in flight: wait (bounded, even
             // after an abort) for the last phase issued on every stage.
-            int issued = (int)(it < C::STAGES ? it : C::STAGES);
+            const int issued = (int)(it < RS ? it : RS);
             for (int k = 0; k < issued; ++k) {
                 const int64_t j = it - 1 - k;
-                const int s = (int)(j % C::STAGES);
-                const uint32_t ph = (uint32_t)((j / C::STAGES) & 1);
+                const int rs = (int)(j % RS);
+                const uint32_t ph = (uint32_t)((j / RS) & 1);
                 const uint64_t t0 = globaltimer_ns();
-                while (!mbar_try_wait(&raw_full[s], ph)) {
+                while (!mbar_try_wait(&raw_full[rs], ph)) {
                     if (globaltimer_ns() - t0 > kWaitTimeoutNs) {
                         atomicCAS(a.status, 0, GP_KSTATUS_TIMEOUT_BASE + 7);
                         break;
@@ -320,15 +448,15 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             bool ok = mbar_wait(b_full, 0, abort_flag, a.status, 5);
             int64_t it = 0;
             for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++it) {
-                const int s = (int)(it % C::STAGES);
-                const uint32_t ph = (uint32_t)((it / C::STAGES) & 1);
+                const int as = (int)(it % C::A_STAGES);
+                const uint32_t aph = (uint32_t)((it / C::A_STAGES) & 1);
                 const int b = (int)(it % C::NACC);
-                const uint32_t aph = (uint32_t)((it / C::NACC) & 1);
-                if (!mbar_wait(&a_full[s], ph, abort_flag, a.status, 6)) break;
-                if (!mbar_wait(&acc_empty[b], aph ^ 1u, abort_flag, a.status, 9)) break;
+                const uint32_t bph = (uint32_t)((it / C::NACC) & 1);
+                if (!mbar_wait(&a_full[as], aph, abort_flag, a.status, 6)) break;
+                if (!mbar_wait(&acc_empty[b], bph ^ 1u, abort_flag, a.status, 9)) break;
                 tc_fence_after();
                 const uint32_t d = tmem_base + (uint32_t)(b * C::N);
-                const uint32_t aS = aBase + (uint32_t)(s * C::A_BYTES);
+                const uint32_t aS = aBase + (uint32_t)(as * C::A_BYTES);
 #pragma unroll
                 for (int pass = 0; pass < 2; ++pass) {
 #pragma unroll
@@ -339,7 +467,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         umma_f16(d, ad, bd, idesc, (pass | ks) != 0 ? 1u : 0u);
                     }
                 }
-                umma_commit(&a_empty[s]);
+                umma_commit(&a_empty[as]);
                 umma_commit(&acc_full[b]);
             }
             // every MMA this thread issued is complete before TMEM is freed
@@ -361,19 +489,41 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     }
 }
 
-template <int K>
-cudaError_t launch_k(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
-    const SmemLayout lay = smem_layout<K>(a.L);
+template <int K, int B, bool WP>
+cudaError_t launch_kb(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
+    const SmemLayout lay = smem_layout<K>(B == 0 ? a.L : 16);
     const int64_t ntiles = (a.n + kTileM - 1) / kTileM;
     if (ntiles == 0) return cudaSuccess;
-    const bool wpsd = a.psd_out != nullptr;
-    auto kern = wpsd ? psd_tc_kernel<K, true> : psd_tc_kernel<K, false>;
+    auto kern = psd_tc_kernel<K, B, WP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
     if (e != cudaSuccess) return e;
     int64_t grid = (int64_t)num_sms * TcCfg<K>::MIN_BLOCKS;
     if (grid > ntiles) grid = ntiles;
     kern<<<(unsigned)grid, kThreads, lay.total, st>>>(a, lay);
     return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t launch_k(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
+    if (a.words == nullptr) {
+        if (a.psd_out) return launch_kb<K, 0, true>(a, num_sms, st);
+        return launch_kb<K, 0, false>(a, num_sms, st);
+    }
+    if (a.psd_out) return cudaErrorInvalidValue;
+    switch (a.pack_bits) {
+        case 1: return launch_kb<K, 1, false>(a, num_sms, st);
+        case 2:
+            if constexpr (K <= 64) return launch_kb<K, 2, false>(a, num_sms, st);
+            break;
+        case 3:
+            if constexpr (K <= 48) return launch_kb<K, 3, false>(a, num_sms, st);
+            break;
+        case 4:
+            if constexpr (K <= 32) return launch_kb<K, 4, false>(a, num_sms, st);
+            break;
+        default: break;
+    }
+    return cudaErrorInvalidValue;
 }
 
 // IEEE binary16 round-to-nearest-even from double (host side).
@@ -413,6 +563,15 @@ double half_value(uint16_t h) {
 int tc_k_for_len(int L) {
     if (L < 2 || L > kMaxTcK) return 0;
     return (L + 15) / 16 * 16;
+}
+
+bool tc_packed_supported(int L, int b) {
+    const int K = tc_k_for_len(L);
+    if (!K || b < 1 || b > 4 || b * L > 128) return false;
+    if (b == 2) return K <= 64;
+    if (b == 3) return K <= 48;
+    if (b == 4) return K <= 32;
+    return true;
 }
 
 // |X_k - X^_k| <= sum|x| * err_coef:  twiddle residual after the hi + lo
