@@ -268,9 +268,22 @@ def run_gpu(args):
     clk = clocks.stop()
     if args.profile:
         # profiling run: the tensor-core filter only (no comparator, no e2e)
+        trace = None
+        if args.trace:
+            ctx.tc_trace(True)
+            for _ in range(3):
+                step(gp.GP_PSD_TC_GUARDED)
+            torch.cuda.synchronize()
+            tr = ctx.tc_trace(False)
+            tiles = max(tr["tiles"], 1)
+            # per tile: converter / epilogue counters cover 4 warps each
+            trace = {k: round(v / tiles / (4 if k.startswith(("conv", "epi")) else 1), 1)
+                     for k, v in tr.items() if k != "tiles"}
+            trace["tiles"] = tr["tiles"]
         if rank == 0:
             print(json.dumps({"profile_run": True, "rows": ROWS, "ms_per_step": ms / args.steps,
-                              "kernel_ms": kms / max(klaunch, 1), "verdicts_exact_vs_fp64_kernel": verdicts_equal}))
+                              "kernel_ms": kms / max(klaunch, 1), "verdicts_exact_vs_fp64_kernel": verdicts_equal,
+                              "cycles_per_tile_per_role": trace}))
         ctx.close()
         return 0
     ms_step = ms / args.steps
@@ -352,6 +365,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--rows", type=int, default=1 << 28, help="batch rows (profiling runs only)")
     ap.add_argument("--profile", action="store_true", help="time the tensor-core filter only")
+    ap.add_argument("--trace", action="store_true", help="with --profile: per-role cycle counters")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

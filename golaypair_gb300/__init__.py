@@ -64,6 +64,7 @@ def lib():
     L.gp_psd_tc_values.argtypes = [P, P, i64, i32, P]
     L.gp_kernel_timing.argtypes = [P, i32]
     L.gp_kernel_time.argtypes = [P, P, P]
+    L.gp_debug_tc_trace.argtypes = [P, i32, P, i32]
     L.gp_psd_fp64_values.argtypes = [P, P, i64, i32, P]
     for name, args in _STAGE_SIGS.items():
         fn = getattr(L, name, None)
@@ -166,6 +167,16 @@ class Context:
         n = ctypes.c_int64()
         self._lib.gp_kernel_time(self._h, ctypes.byref(ms), ctypes.byref(n))
         return ms.value, n.value
+
+    TRACE_NAMES = ["conv_wait_raw", "conv_wait_a", "conv_work", "epi_wait_acc", "epi_wait_stash", "epi_work",
+                   "mma_wait_a", "mma_wait_acc", "mma_issue", "prod_wait", "prod_issue", "tiles", "conv_fence",
+                   "mma_commit"]
+
+    def tc_trace(self, enable):
+        """Reads (and resets) the tensor-core filter's per-role cycle counters."""
+        out = (ctypes.c_uint64 * len(self.TRACE_NAMES))()
+        self.check(self._lib.gp_debug_tc_trace(self._h, 1 if enable else 0, out, len(out)), "gp_debug_tc_trace")
+        return dict(zip(self.TRACE_NAMES, list(out)))
 
     def psd_tc_values(self, seqs):
         seqs = np.ascontiguousarray(seqs, dtype=np.int8)

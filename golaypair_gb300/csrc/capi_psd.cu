@@ -79,6 +79,7 @@ int gp_ctx::enqueue_filter(const gp::RowSrc& src, int64_t n, int order, int paf,
     a.unsure_cap = n;
     a.psd_out = nullptr;
     a.status = status.as<int>();
+    a.trace = trace_on ? counts.as<unsigned long long>() + 16 : nullptr;
     cudaEvent_t tb;
     time_begin(st, &tb);
     GP_CUDA_TRY(this, gp::launch_psd_tc(a, num_sms, st));
@@ -171,6 +172,20 @@ const char* gp_last_error(const gp_ctx* c) { return c ? c->err.c_str() : "no con
 int gp_kernel_timing(gp_ctx* c, int enable) {
     if (!c) return GP_ERR_ARG;
     c->timing = enable != 0;
+    return GP_OK;
+}
+
+int gp_debug_tc_trace(gp_ctx* c, int enable, uint64_t* out, int nout) {
+    if (!c) return GP_ERR_ARG;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    if (out && nout > 0) {
+        unsigned long long h[gp::kTrCount];
+        GP_CUDA_TRY(c, cudaMemcpy(h, c->counts.as<unsigned long long>() + 16, sizeof h, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nout && i < gp::kTrCount; ++i) out[i] = h[i];
+    }
+    GP_CUDA_TRY(c, cudaMemset(c->counts.as<unsigned long long>() + 16, 0, sizeof(unsigned long long) * gp::kTrCount));
+    c->trace_on = enable != 0;
     return GP_OK;
 }
 
@@ -340,6 +355,7 @@ int gp_psd_tc_values(gp_ctx* c, const int8_t* seqs, int64_t n, int L, float* out
     a.unsure_cap = n;
     a.psd_out = dp.as<float>();
     a.status = c->status.as<int>();
+    a.trace = nullptr;
     GP_CUDA_TRY(c, gp::launch_psd_tc(a, c->num_sms, c->s_comp));
     GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_comp));
     rc = c->check_status("gp_psd_tc_values");

@@ -1,0 +1,366 @@
+// capi_sortmatch.cu -- sort and match stages.
+//
+// gp_sort replaces GNU_sort (src/core/sort/sort.cpp:7-22), i.e.
+// `sort -S 2G -T dir files | uniq > out` in the C locale: every line becomes
+// a fixed-width key (4 bits per character for the candidate alphabet
+// ' ' '-' '0'-'9' 'D' 'P' 'S', else 8 bits per byte; the pad code sorts
+// below every character, so a prefix sorts first as in a byte compare), the
+// keys are radix-sorted on the device (stable LSD, prims.cu) and adjacent
+// duplicates are dropped.
+//
+// gp_match replaces match_pairs (src/core/match/match_pairs.cpp:15-121):
+// the sorted files are grouped by their first token, equal tokens of A and
+// B are joined, and every pair of the cross product is checked on the device
+// by exact integer PAF (src/utils/golay.cpp:27-44) using per-line PAF
+// vectors.  Pairs are written in the reference's order: token order, then A
+// line order, then B line order.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+#include "prims.h"
+
+namespace {
+
+bool slurp(const char* path, std::string& out) {
+    FILE* f = fopen(path, "rb");
+    if (!f) return false;
+    fseek(f, 0, SEEK_END);
+    long sz = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    out.resize(sz > 0 ? (size_t)sz : 0);
+    size_t got = sz > 0 ? fread(&out[0], 1, (size_t)sz, f) : 0;
+    fclose(f);
+    out.resize(got);
+    return true;
+}
+
+// 4-bit codes preserving byte order; 0 = padding
+__host__ __device__ inline int code4(unsigned char ch) {
+    switch (ch) {
+        case ' ': return 1;
+        case '-': return 2;
+        case 'D': return 13;
+        case 'P': return 14;
+        case 'S': return 15;
+        default: return (ch >= '0' && ch <= '9') ? 3 + (ch - '0') : -1;
+    }
+}
+
+__global__ void build_keys_kernel(const char* text, const uint64_t* start, const uint32_t* len, int64_t n, int W,
+                                  int nibble, uint32_t* keys) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const char* s = text + start[i];
+        const uint32_t l = len[i];
+        uint32_t* k = keys + i * W;
+        const int per = nibble ? 8 : 4;
+        const int bits = nibble ? 4 : 8;
+        for (int w = 0; w < W; ++w) {
+            uint32_t v = 0;
+            for (int c = 0; c < per; ++c) {
+                const uint32_t pos = (uint32_t)(w * per + c);
+                uint32_t code = 0;
+                if (pos < l) {
+                    const unsigned char ch = (unsigned char)s[pos];
+                    code = nibble ? (uint32_t)code4(ch) : (uint32_t)ch;
+                }
+                v = (v << bits) | code;
+            }
+            k[w] = v;
+        }
+    }
+}
+
+// PAF(s) = sum_i x_i x_{(i+s) mod L}, s = 1..L/2 (src/utils/golay.cpp:27-33)
+__global__ void paf_kernel(const int8_t* seqs, int64_t n, int L, int H, int* paf) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int8_t* x = seqs + i * L;
+        for (int s = 1; s <= H; ++s) {
+            int r = 0;
+            int j2 = s;
+            for (int j = 0; j < L; ++j) {
+                r += (int)x[j] * (int)x[j2];
+                if (++j2 == L) j2 = 0;
+            }
+            paf[i * H + (s - 1)] = r;
+        }
+    }
+}
+
+struct GroupPair {
+    uint32_t a0, na, b0, nb;
+    uint64_t first;  // index of this group's first pair in the flattened product
+};
+
+// one thread per candidate pair; flags[w] = 1 if the pair is complementary
+__global__ void pair_check_kernel(const GroupPair* gps, int64_t ng, uint64_t total, const int* pafa, const int* pafb,
+                                  int H, int target, uint32_t* flags) {
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+        int64_t lo = 0, hi = ng - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (gps[mid].first <= w)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const GroupPair g = gps[lo];
+        const uint64_t off = w - g.first;
+        const uint32_t ia = g.a0 + (uint32_t)(off / g.nb);
+        const uint32_t ib = g.b0 + (uint32_t)(off % g.nb);
+        const int* pa = pafa + (int64_t)ia * H;
+        const int* pb = pafb + (int64_t)ib * H;
+        uint32_t ok = 1;
+        for (int s = 0; s < H; ++s)
+            if (pa[s] + pb[s] != target) {
+                ok = 0;
+                break;
+            }
+        flags[w] = ok;
+    }
+}
+
+unsigned grid_for(int64_t n) {
+    int64_t g = (n + 255) / 256;
+    if (g > 65535 * 8) g = 65535 * 8;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+struct Cand {
+    std::vector<uint32_t> tok_off, tok_len;  // first token in the text
+    std::vector<int8_t> seqs;                // L per line
+    size_t n = 0;
+};
+
+// Parses candidate lines: a first token, then exactly L integers.
+bool parse_candidates(const std::string& text, int L, Cand& out, std::string& err) {
+    const char* p = text.data();
+    const char* end = p + text.size();
+    while (p < end) {
+        const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
+        if (!nl) nl = end;
+        const char* q = p;
+        while (q < nl && *q == ' ') ++q;
+        if (q < nl) {
+            const char* t = q;
+            while (q < nl && *q != ' ') ++q;
+            out.tok_off.push_back((uint32_t)(t - text.data()));
+            out.tok_len.push_back((uint32_t)(q - t));
+            int got = 0;
+            while (got < L) {
+                while (q < nl && *q == ' ') ++q;
+                if (q >= nl) break;
+                char* e;
+                const long v = strtol(q, &e, 10);
+                if (e == q) break;
+                out.seqs.push_back((int8_t)v);
+                ++got;
+                q = e;
+            }
+            if (got != L) {
+                err = "candidate line with fewer than L values";
+                return false;
+            }
+            out.n++;
+        }
+        p = nl + 1;
+    }
+    return true;
+}
+
+void put_pair(std::string& s, const int8_t* a, const int8_t* b, int L) {
+    char tmp[8];
+    for (int i = 0; i < L; ++i) {
+        int n = snprintf(tmp, sizeof tmp, "%d ", a[i]);
+        s.append(tmp, (size_t)n);
+    }
+    s.push_back(' ');
+    for (int i = 0; i < L; ++i) {
+        int n = snprintf(tmp, sizeof tmp, "%d ", b[i]);
+        s.append(tmp, (size_t)n);
+    }
+    s.push_back('\n');
+}
+
+}  // namespace
+
+// Shared with the uncompression stage: match two sorted candidate texts and
+// append the pairs to `out`.  Returns GP_EMPTY_INPUT if either is empty.
+int gp_match_texts(gp_ctx* c, int L, int compress, int paf, const std::string& ta, const std::string& tb,
+                   std::string& out, int64_t* n_pairs) {
+    if (ta.empty() || tb.empty()) return GP_EMPTY_INPUT;
+    Cand A, B;
+    std::string err;
+    if (!parse_candidates(ta, L, A, err) || !parse_candidates(tb, L, B, err)) return c->fail(GP_ERR_FORMAT, "match: %s", err.c_str());
+    // group boundaries and the merge on the first token (std::string order)
+    auto tok = [](const std::string& t, const Cand& x, size_t i) {
+        return std::string_view(t.data() + x.tok_off[i], x.tok_len[i]);
+    };
+    std::vector<GroupPair> gps;
+    uint64_t total = 0;
+    size_t i = 0, j = 0;
+    while (i < A.n && j < B.n) {
+        const auto x = tok(ta, A, i), y = tok(tb, B, j);
+        const int cmp = x.compare(y);
+        if (cmp == 0) {
+            size_t i2 = i, j2 = j;
+            while (i2 < A.n && tok(ta, A, i2) == x) ++i2;
+            while (j2 < B.n && tok(tb, B, j2) == y) ++j2;
+            gps.push_back({(uint32_t)i, (uint32_t)(i2 - i), (uint32_t)j, (uint32_t)(j2 - j), total});
+            total += (uint64_t)(i2 - i) * (j2 - j);
+            i = i2;
+            j = j2;
+        } else if (cmp < 0) {
+            ++i;
+        } else {
+            ++j;
+        }
+    }
+    if (n_pairs) *n_pairs = 0;
+    if (total == 0) return GP_OK;
+    cudaStream_t s = c->s_comp;
+    const int H = L / 2;
+    DevBuf da, db, dpa, dpb, dg, df, dpos, dscan, dlist;
+    const int64_t need_flags = (int64_t)total;
+    if (!da.ensure(A.seqs.size() + 16) || !db.ensure(B.seqs.size() + 16) || !dpa.ensure(A.n * (H + 1) * 4) ||
+        !dpb.ensure(B.n * (H + 1) * 4) || !dg.ensure(gps.size() * sizeof(GroupPair)) || !df.ensure(need_flags * 4) ||
+        !dpos.ensure(need_flags * 4) || !dscan.ensure(gp::scan_tmp_bytes(need_flags)) || !dlist.ensure(need_flags * 4 + 4))
+        return c->fail(GP_ERR_NOMEM, "match: device allocation");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(da.p, A.seqs.data(), A.seqs.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(db.p, B.seqs.data(), B.seqs.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dg.p, gps.data(), gps.size() * sizeof(GroupPair), cudaMemcpyHostToDevice, s));
+    if (H > 0) {
+        paf_kernel<<<grid_for((int64_t)A.n), 256, 0, s>>>(da.as<int8_t>(), (int64_t)A.n, L, H, dpa.as<int>());
+        paf_kernel<<<grid_for((int64_t)B.n), 256, 0, s>>>(db.as<int8_t>(), (int64_t)B.n, L, H, dpb.as<int>());
+    }
+    pair_check_kernel<<<grid_for((int64_t)total), 256, 0, s>>>(dg.as<GroupPair>(), (int64_t)gps.size(), total,
+                                                               dpa.as<int>(), dpb.as<int>(), H, paf * compress,
+                                                               df.as<uint32_t>());
+    GP_CUDA_TRY(c, cudaGetLastError());
+    uint32_t* d_cnt = dlist.as<uint32_t>() + need_flags;
+    GP_CUDA_TRY(c, gp::compact_flags(df.as<uint32_t>(), nullptr, dlist.as<uint32_t>(), need_flags, dpos.as<uint32_t>(),
+                                     dscan.as<uint32_t>(), d_cnt, s));
+    uint32_t nk = 0;
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&nk, d_cnt, 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    std::vector<uint32_t> keep(nk);
+    if (nk) GP_CUDA_TRY(c, cudaMemcpy(keep.data(), dlist.p, (size_t)nk * 4, cudaMemcpyDeviceToHost));
+    size_t g = 0;
+    for (uint32_t w : keep) {
+        while (g + 1 < gps.size() && gps[g + 1].first <= w) ++g;
+        const uint64_t off = w - gps[g].first;
+        const uint32_t ia = gps[g].a0 + (uint32_t)(off / gps[g].nb);
+        const uint32_t ib = gps[g].b0 + (uint32_t)(off % gps[g].nb);
+        put_pair(out, A.seqs.data() + (size_t)ia * L, B.seqs.data() + (size_t)ib * L, L);
+    }
+    if (n_pairs) *n_pairs = nk;
+    return GP_OK;
+}
+
+// Sorted, de-duplicated lines of `text` (byte order).
+int gp_sort_text(gp_ctx* c, const std::string& text, std::string& out) {
+    std::vector<uint64_t> start;
+    std::vector<uint32_t> len;
+    size_t maxlen = 0;
+    bool nibble = true;
+    {
+        const char* p = text.data();
+        const char* end = p + text.size();
+        while (p < end) {
+            const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
+            const size_t l = nl ? (size_t)(nl - p) : (size_t)(end - p);
+            start.push_back((uint64_t)(p - text.data()));
+            len.push_back((uint32_t)l);
+            maxlen = std::max(maxlen, l);
+            p += l + 1;
+        }
+        for (unsigned char ch : text)
+            if (ch != '\n' && code4(ch) < 0) {
+                nibble = false;
+                break;
+            }
+    }
+    const int64_t n = (int64_t)start.size();
+    out.clear();
+    if (n == 0) return GP_OK;
+    const int per = nibble ? 8 : 4;
+    const int W = (int)((maxlen + per - 1) / per) + 0;
+    const int Wk = W < 1 ? 1 : W;
+    cudaStream_t s = c->s_comp;
+    DevBuf dt, ds, dl, dk, di, dtmp, dflag, dpos, dscan, dout;
+    if (!dt.ensure(text.size() + 16) || !ds.ensure(n * 8) || !dl.ensure(n * 4) || !dk.ensure((size_t)n * Wk * 4) ||
+        !di.ensure(n * 4) || !dtmp.ensure(gp::radix_sort_tmp_bytes(n)) || !dflag.ensure(n * 4) || !dpos.ensure(n * 4) ||
+        !dscan.ensure(gp::scan_tmp_bytes(n)) || !dout.ensure(n * 4 + 4))
+        return c->fail(GP_ERR_NOMEM, "sort: device allocation");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dt.p, text.data(), text.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(ds.p, start.data(), n * 8, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dl.p, len.data(), n * 4, cudaMemcpyHostToDevice, s));
+    build_keys_kernel<<<grid_for(n), 256, 0, s>>>(dt.as<char>(), ds.as<uint64_t>(), dl.as<uint32_t>(), n, Wk,
+                                                  nibble ? 1 : 0, dk.as<uint32_t>());
+    GP_CUDA_TRY(c, cudaGetLastError());
+    GP_CUDA_TRY(c, gp::iota_u32(di.as<uint32_t>(), n, s));
+    GP_CUDA_TRY(c, gp::radix_sort_keys(dk.as<uint32_t>(), Wk, Wk, di.as<uint32_t>(), n, dtmp.p, s));
+    GP_CUDA_TRY(c, gp::mark_unique(dk.as<uint32_t>(), Wk, di.as<uint32_t>(), n, Wk, dflag.as<uint32_t>(), s));
+    uint32_t* d_cnt = dout.as<uint32_t>() + n;
+    GP_CUDA_TRY(c, gp::compact_flags(dflag.as<uint32_t>(), di.as<uint32_t>(), dout.as<uint32_t>(), n, dpos.as<uint32_t>(),
+                                     dscan.as<uint32_t>(), d_cnt, s));
+    uint32_t nu = 0;
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&nu, d_cnt, 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    std::vector<uint32_t> order(nu);
+    if (nu) GP_CUDA_TRY(c, cudaMemcpy(order.data(), dout.p, (size_t)nu * 4, cudaMemcpyDeviceToHost));
+    out.reserve(text.size() + 1);
+    for (uint32_t i : order) {
+        out.append(text.data() + start[i], len[i]);
+        out.push_back('\n');
+    }
+    return GP_OK;
+}
+
+extern "C" {
+
+int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
+    if (!c || (!in_paths && n_in > 0) || !out_path) return GP_ERR_ARG;
+    cudaSetDevice(c->device);
+    std::string all, one;
+    for (int i = 0; i < n_in; ++i) {
+        if (!slurp(in_paths[i], one)) return c->fail(GP_ERR_IO, "sort: cannot read %s", in_paths[i]);
+        all += one;
+        if (!one.empty() && one.back() != '\n') all.push_back('\n');
+    }
+    std::string sorted;
+    int rc = gp_sort_text(c, all, sorted);
+    if (rc) return rc;
+    FILE* f = fopen(out_path, "w");
+    if (!f) return c->fail(GP_ERR_IO, "sort: cannot write %s", out_path);
+    fwrite(sorted.data(), 1, sorted.size(), f);
+    return fclose(f) == 0 ? GP_OK : c->fail(GP_ERR_IO, "sort: write failed");
+}
+
+int gp_match(gp_ctx* c, int order, int compress, int paf, const char* path_a, const char* path_b, const char* out_path,
+             int append, int64_t* n_pairs) {
+    if (!c || !path_a || !path_b || !out_path) return GP_ERR_ARG;
+    if (compress < 1 || order % compress) return c->fail(GP_ERR_ARG, "order %d not divisible by %d", order, compress);
+    cudaSetDevice(c->device);
+    // the reference opens the pair writer (truncating unless appending)
+    // before looking at the inputs (src/main.cpp:97-101)
+    FILE* f = fopen(out_path, append ? "a" : "w");
+    if (!f) return c->fail(GP_ERR_IO, "match: cannot open %s", out_path);
+    std::string ta, tb, out;
+    const bool okA = slurp(path_a, ta), okB = slurp(path_b, tb);
+    if (n_pairs) *n_pairs = 0;
+    if (!okA || !okB || ta.empty() || tb.empty()) {
+        fclose(f);
+        return GP_EMPTY_INPUT;
+    }
+    int rc = gp_match_texts(c, order / compress, compress, paf, ta, tb, out, n_pairs);
+    fwrite(out.data(), 1, out.size(), f);
+    fclose(f);
+    return rc;
+}
+
+}  // extern "C"

@@ -16,6 +16,10 @@
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
     // Grows to at least `bytes` (contents not preserved).  false on failure.
     bool ensure(size_t bytes) {
         if (bytes <= cap) return true;
@@ -44,6 +48,10 @@ struct DevBuf {
 struct HostPinned {
     void* p = nullptr;
     size_t cap = 0;
+    HostPinned() = default;
+    HostPinned(const HostPinned&) = delete;
+    HostPinned& operator=(const HostPinned&) = delete;
+    ~HostPinned() { release(); }
     bool ensure(size_t bytes) {
         if (bytes <= cap) return true;
         if (p) cudaFreeHost(p);
@@ -87,6 +95,7 @@ struct gp_ctx {
     std::map<int, DevBuf> twiddles64;  // FP64 (cos, sin) tables, by L
     // optional CUDA-event timing of the main filter kernel (profiling)
     bool timing = false;
+    bool trace_on = false;  // per-role cycle counters of the tensor-core filter
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;
     void time_begin(cudaStream_t st, cudaEvent_t* b) {
         *b = nullptr;

@@ -1,0 +1,40 @@
+// finalize.h -- exact FP64 recheck + canonical check + signature records.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "gp_internal.h"
+
+namespace gp {
+
+struct FinalizeArgs {
+    RowSrc src;                 // candidates (packed words)
+    const uint8_t* roles;       // per candidate role bits (bit0 A, bit1 B), or nullptr
+    uint8_t fixed_role;         // role bits when roles == nullptr
+    const uint32_t* idx;        // candidate rows to finalize
+    const unsigned long long* n_idx;
+    int64_t idx_cap;
+    const double* tw;           // FP64 twiddles
+    double thr;                 // 2n - paf + 0.001
+    int bound;                  // 2n - paf (inverted signatures)
+    int invert_roles;           // bit r set: role r writes bound - rint(psd)
+    int check_canonical;
+    const int16_t* units;       // units mod L (affine group multipliers)
+    int n_units;
+    // outputs
+    uint4* rec_words;
+    uint8_t* rec_role;
+    uint16_t* rec_sig;          // (L-1) per record
+    uint32_t* rec_src;          // optional: candidate row of each record
+    unsigned long long* rec_count;
+    int64_t rec_cap;
+    unsigned long long* psd_pass;
+    int* status;
+};
+
+cudaError_t launch_mask_to_list(const uint32_t* mask, int64_t n, uint32_t* out, unsigned long long* count,
+                                int64_t cap, int* status, int num_sms, cudaStream_t st);
+cudaError_t launch_finalize(const FinalizeArgs& a, int64_t max_rows, int num_sms, cudaStream_t st);
+
+}  // namespace gp

@@ -35,6 +35,16 @@ struct PsdTcArgs {
     int64_t unsure_cap;
     float* psd_out;          // optional n x (K/2) PSD values
     int* status;
+    unsigned long long* trace;  // optional per-role cycle counters (diagnostics)
+};
+
+// Diagnostics counters written when PsdTcArgs::trace is set (summed over
+// CTAs, in SM clock cycles, one sample per warp and tile).
+enum TcTrace {
+    kTrConvWaitRaw = 0, kTrConvWaitA, kTrConvWork,
+    kTrEpiWaitAcc, kTrEpiWaitStash, kTrEpiWork,
+    kTrMmaWaitA, kTrMmaWaitAcc, kTrMmaIssue,
+    kTrProdWait, kTrProdIssue, kTrTiles, kTrConvFence, kTrMmaCommit, kTrCount
 };
 
 // Builds the B-operand image (hi tile, lo tile) for length L, K = padded L.

@@ -238,13 +238,19 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         }
         const int norm = 128 - B * L;  // packed: left shift that puts digit 0 at bit 127
         int64_t it = 0;
+        unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             const int rs = (int)(it % RS);
             const uint32_t rph = (uint32_t)((it / RS) & 1);
             const int as = (int)(it % C::A_STAGES);
             const uint32_t aph = (uint32_t)((it / C::A_STAGES) & 1);
+            const long long c0 = clock64();
             if (!mbar_wait(&raw_full[rs], rph, abort_flag, a.status, 1)) break;
+            const long long c1 = clock64();
             if (!mbar_wait(&a_empty[as], aph ^ 1u, abort_flag, a.status, 2)) break;
+            const long long c2 = clock64();
+            tr0 += c1 - c0;
+            tr1 += c2 - c1;
             uint8_t* A = sA + as * C::A_BYTES;
             const int64_t row = t * kTileM + r;
             const bool full_tile = aligned && (t + 1) * kTileM <= n;
@@ -315,6 +321,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 packed_row<B, C::KCH>(s, sLut, A, r, C::A_KSTRIDE);
             }
             if constexpr (B == 0) stash[(int)(it % C::RING) * kTileM + r] = (float)sumsq;
+            const long long c3 = clock64();
+            tr3 += c3 - c2;
             fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) {
@@ -322,6 +330,14 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 mbar_arrive(&a_full[as]);
                 mbar_arrive(&raw_empty[rs]);
             }
+            tr2 += clock64() - c2;
+        }
+        if (a.trace && lane == 0) {
+            atomicAdd(&a.trace[kTrConvWaitRaw], tr0);
+            atomicAdd(&a.trace[kTrConvWaitA], tr1);
+            atomicAdd(&a.trace[kTrConvWork], tr3);
+            atomicAdd(&a.trace[kTrConvFence], tr2 - tr3);
+            if (warp == 0) atomicAdd(&a.trace[kTrTiles], (unsigned long long)it);
         }
     } else if (warp < 8) {
         // ------------------------------------------------ epilogue
@@ -332,10 +348,14 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         const float d_const = a.err_coef * (float)L * (float)a.alpha_c;
         const float g_const = fmaxf(a.guard_cfg, 2.f * sq * d_const + 3.f * d_const * d_const + 1e-4f);
         int64_t it = 0;
+        unsigned long long tr0 = 0, tr1 = 0, tr2 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             const int b = (int)(it % C::NACC);
             const uint32_t ph = (uint32_t)((it / C::NACC) & 1);
+            const long long c0 = clock64();
             if (!mbar_wait(&acc_full[b], ph, abort_flag, a.status, 3)) break;
+            const long long c1 = clock64();
+            tr0 += c1 - c0;
             tc_fence_after();
             float v[C::N];
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * C::N);
@@ -350,7 +370,9 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 // MMA of a later use waits for this epilogue to free its
                 // accumulator.
                 const int slot = (int)(it % C::RING);
+                const long long c3 = clock64();
                 if (!mbar_wait(&stash_full[slot], (uint32_t)((it / C::RING) & 1), abort_flag, a.status, 11)) break;
+                tr1 += clock64() - c3;
                 // sum|x| <= sqrt(L * sum x^2)
                 const float d = a.err_coef * sqrtf((float)L * stash[slot * kTileM + r]);
                 g = fmaxf(a.guard_cfg, 2.f * sq * d + 3.f * d * d + 1e-4f);
@@ -394,6 +416,12 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         a.psd_out[row * (C::N / 2) + k] = fmaf(v[k], v[k], v[C::N / 2 + k] * v[C::N / 2 + k]);
                 }
             }
+            tr2 += clock64() - c1;
+        }
+        if (a.trace && lane == 0) {
+            atomicAdd(&a.trace[kTrEpiWaitAcc], tr0);
+            atomicAdd(&a.trace[kTrEpiWaitStash], tr1);
+            atomicAdd(&a.trace[kTrEpiWork], tr2 - tr1);
         }
     } else if (warp == 8) {
         // ------------------------------------------------ producer
@@ -403,10 +431,14 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             bulk_g2s(sB, a.bimage, 2 * C::B_BYTES, b_full);
             const uint8_t* src = B == 0 ? reinterpret_cast<const uint8_t*>(a.seqs)
                                         : reinterpret_cast<const uint8_t*>(a.words);
+            unsigned long long tr0 = 0, tr1 = 0;
             for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
                 const int rs = (int)(it % RS);
                 const uint32_t ph = (uint32_t)((it / RS) & 1);
+                const long long c0 = clock64();
                 if (!mbar_wait(&raw_empty[rs], ph ^ 1u, abort_flag, a.status, 4)) break;
+                const long long c1 = clock64();
+                tr0 += c1 - c0;
                 const bool full_tile = aligned && (t + 1) * kTileM <= n;
                 if (full_tile) {
                     const uint32_t bytes = (uint32_t)(kTileM * row_bytes);
@@ -415,6 +447,11 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 } else {
                     mbar_arrive(&raw_full[rs]);
                 }
+                tr1 += clock64() - c1;
+            }
+            if (a.trace) {
+                atomicAdd(&a.trace[kTrProdWait], tr0);
+                atomicAdd(&a.trace[kTrProdIssue], tr1);
             }
             // Do not leave the CTA with copies in flight: wait (bounded, even
             // after an abort) for the last phase issued on every stage.
@@ -447,13 +484,19 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const uint32_t bBase = smem_u32(sB);
             bool ok = mbar_wait(b_full, 0, abort_flag, a.status, 5);
             int64_t it = 0;
+            unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
             for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++it) {
                 const int as = (int)(it % C::A_STAGES);
                 const uint32_t aph = (uint32_t)((it / C::A_STAGES) & 1);
                 const int b = (int)(it % C::NACC);
                 const uint32_t bph = (uint32_t)((it / C::NACC) & 1);
+                const long long c0 = clock64();
                 if (!mbar_wait(&a_full[as], aph, abort_flag, a.status, 6)) break;
+                const long long c1 = clock64();
                 if (!mbar_wait(&acc_empty[b], bph ^ 1u, abort_flag, a.status, 9)) break;
+                const long long c2 = clock64();
+                tr0 += c1 - c0;
+                tr1 += c2 - c1;
                 tc_fence_after();
                 const uint32_t d = tmem_base + (uint32_t)(b * C::N);
                 const uint32_t aS = aBase + (uint32_t)(as * C::A_BYTES);
@@ -467,8 +510,18 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         umma_f16(d, ad, bd, idesc, (pass | ks) != 0 ? 1u : 0u);
                     }
                 }
+                const long long c3 = clock64();
                 umma_commit(&a_empty[as]);
                 umma_commit(&acc_full[b]);
+                const long long c4 = clock64();
+                tr2 += c3 - c2;
+                tr3 += c4 - c3;
+            }
+            if (a.trace) {
+                atomicAdd(&a.trace[kTrMmaWaitA], tr0);
+                atomicAdd(&a.trace[kTrMmaWaitAcc], tr1);
+                atomicAdd(&a.trace[kTrMmaIssue], tr2);
+                atomicAdd(&a.trace[kTrMmaCommit], tr3);
             }
             // every MMA this thread issued is complete before TMEM is freed
             umma_commit(final_bar);

@@ -75,12 +75,94 @@ int gp_psd_filter_device(gp_ctx* ctx, const int8_t* d_seqs, int64_t n, int L, in
  * for them, returns the summed device time and launch count, and clears. */
 int gp_kernel_timing(gp_ctx* ctx, int enable);
 int gp_kernel_time(gp_ctx* ctx, double* total_ms, int64_t* launches);
+/* Diagnostics: per-role cycle counters of the tensor-core filter (converter,
+ * epilogue, MMA and producer waits / work, tiles), summed over CTAs since the
+ * previous call.  Copies up to nout counters, resets them, and turns the
+ * counting on (enable != 0) or off for later launches. */
+int gp_debug_tc_trace(gp_ctx* ctx, int enable, uint64_t* out, int nout);
 
 /* Tensor-core PSD values (fp32, bins 1..L/2) of n rows, for error analysis.
  * out: n x (L/2) floats, HOST memory. */
 int gp_psd_tc_values(gp_ctx* ctx, const int8_t* seqs, int64_t n, int L, float* out);
 /* FP64 PSD values (all bins 0..L-1) of n rows.  out: n x L doubles, HOST. */
 int gp_psd_fp64_values(gp_ctx* ctx, const int8_t* seqs, int64_t n, int L, double* out);
+
+/* ---------------------------------------------------------------- stages */
+
+typedef struct {
+    int64_t necklaces;   /* necklaces visited ("Orderly Count") */
+    int64_t candidates;  /* necklaces that passed the row-sum gate */
+    int64_t psd_pass;    /* candidates that passed the exact PSD filter */
+    int64_t written_a;   /* lines written to the A file */
+    int64_t written_b;   /* lines written to the B file */
+    int64_t unsure;      /* candidates the tensor-core filter sent to FP64 */
+    double seconds;
+} gp_gen_stats;
+
+/*
+ * Candidate generation for job proc_id of proc_num.  Replaces
+ *   int generate_hybrid(int ORDER, int COMPRESS, int PAF_CONSTANT,
+ *                       std::ofstream& out_a, std::ofstream& out_b,
+ *                       int PROC_ID, int PROC_NUM)
+ * (src/core/generate/generate_hybrid.h; generate_hybrid.cpp:107-163) with the
+ * job split of src/utils/lyndon.cpp:87-121.  Writes the A and B candidate
+ * files (src/utils/io.cpp:14-36 format) in the reference's line order.
+ * Returns GP_NO_DECOMPOSITION (1) when 2n+(n-1)paf is not a sum of two
+ * squares, as the reference does.
+ */
+int gp_generate(gp_ctx* ctx, int order, int compress, int paf, int proc_id, int proc_num, const char* path_a,
+                const char* path_b, gp_gen_stats* stats);
+
+/* Same over the words whose lexicographic rank (base-|alphabet| number,
+ * first entry most significant) lies in [begin, end), 128-bit bounds as
+ * (hi, lo) pairs.  No counterpart in the reference, which only splits by
+ * prefix; used for windowed searches of orders too large to enumerate. */
+int gp_generate_window(gp_ctx* ctx, int order, int compress, int paf, uint64_t begin_hi, uint64_t begin_lo,
+                       uint64_t end_hi, uint64_t end_lo, const char* path_a, const char* path_b,
+                       gp_gen_stats* stats);
+
+/*
+ * Replaces GNU_sort(const std::vector<std::string>& in, const std::string& out,
+ * const std::string& tmpdir) (src/core/sort/sort.cpp:7-22), which runs
+ * `sort | uniq` over the files: lines of all inputs, byte order (C locale),
+ * adjacent duplicates removed, written to out_path.
+ */
+int gp_sort(gp_ctx* ctx, const char** in_paths, int n_in, const char* out_path);
+
+/*
+ * Replaces int match_pairs(int ORDER, int COMPRESS, int PAF, std::ifstream& a,
+ * std::ifstream& b, IO::PairWriter&) (src/core/match/match_pairs.h:5,
+ * match_pairs.cpp:15-121): merge-join of two sorted candidate files on their
+ * first token, each equal-token cross product checked by exact PAF
+ * (src/utils/golay.cpp:27-44), pairs appended (append != 0) or written to
+ * out_path (src/utils/io.cpp:75-95 format).  Returns GP_EMPTY_INPUT (1) when
+ * an input is empty, after creating/truncating out_path like the reference.
+ */
+int gp_match(gp_ctx* ctx, int order, int compress, int paf, const char* path_a, const char* path_b,
+             const char* out_path, int append, int64_t* n_pairs);
+
+/*
+ * Replaces uncompress_pipeline(int order, int c, int c_new, int paf,
+ * IO::PairReader&, IO::PairWriter&, const std::string& work_dir,
+ * const std::string& prefix, DeviceType) (src/core/uncompression/
+ * uncompression.h:19-29, uncompression.cpp:32-79) for both of its devices:
+ * every pair of in_pairs (compression c) is expanded to compression c_new,
+ * PSD-filtered, sorted and matched; the pairs are written to out_pairs in
+ * input order.  Candidate files of each pair stay in device memory (the
+ * reference's uncompress_tmp_* scratch files are not written; work_dir and
+ * prefix are accepted for interface parity).  A line with the wrong number
+ * of values is GP_ERR_FORMAT (the reference throws, io.cpp:52-55).
+ */
+int gp_uncompress(gp_ctx* ctx, int order, int compress, int new_compress, int paf, const char* in_pairs,
+                  const char* out_pairs, const char* work_dir, const char* prefix);
+
+/*
+ * Replaces int cache_filter(int ORDER, int COMPRESS, const std::string& in,
+ * const std::string& out) (src/core/filter/filter.h, filter.cpp:18-163):
+ * keeps the first pair of every equivalence class (in the reference's set
+ * order and erase rules) and writes them in sorted order.
+ */
+int gp_equiv_filter(gp_ctx* ctx, int order, int compress, const char* in_path, const char* out_path);
 
 #ifdef __cplusplus
 }

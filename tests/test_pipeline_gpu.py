@@ -1,0 +1,127 @@
+"""End-to-end parity of the GPU pipeline (the `golay` driver, i.e. the C ABI
+stage by stage) with the reference's own outputs and with the oracle.
+
+Bar: byte-identical files (candidate files, sorted files, pair files,
+unique pairs) against the golden fixtures produced by the reference, and
+against the oracle for cases the fixtures do not cover.
+"""
+import ctypes
+import hashlib
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import golaypair_gb300 as gp
+from conftest import GOLDEN, GenStats, read
+
+pytestmark = pytest.mark.gpu
+ENV = dict(os.environ, LC_ALL="C")
+
+
+def golay(args, tmp, check=True):
+    d = str(tmp)
+    argv = [gp.CLI_PATH] + args[:-1] + ["--dir", d, args[-1]]
+    r = subprocess.run(argv, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=ENV)
+    if check:
+        assert r.returncode == 0, r.stderr + r.stdout
+    return r, os.path.join(d, f"order-{args[0]}")
+
+
+@pytest.mark.parametrize("name", ["n16", "n26"])
+def test_all_matches_reference(tmp_path, golden_manifest, name):
+    rec = golden_manifest["runs"][name]
+    _, wd = golay(rec["argv"], tmp_path)
+    for fn in rec["files"]:
+        got = read(os.path.join(wd, fn))
+        want = read(os.path.join(GOLDEN, name, fn.replace("#", "_")))
+        assert got == want, fn
+
+
+@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000"])
+def test_gen_matches_reference_hash(tmp_path, golden_manifest, name):
+    rec = golden_manifest["runs"][name]
+    r, wd = golay(rec["argv"], tmp_path)
+    for fn, meta in rec["files"].items():
+        got = read(os.path.join(wd, fn))
+        assert got.count(b"\n") == meta["lines"], fn
+        assert hashlib.sha256(got).hexdigest() == meta["sha256"], fn
+
+
+@pytest.mark.parametrize("order,compress,paf,lo,size", [
+    (50, 2, 0, 123456789012, 1 << 24),      # length 25 over {-2,0,2}
+    (58, 2, 0, 31415926535897, 1 << 22),    # length 29
+    (90, 5, 0, 98765432109876, 1 << 22),    # length 18 over {-5..5 odd}
+    (57, 3, -2, 0, 1 << 23),                # length 19, window at the start
+])
+def test_window_matches_oracle(oracle_lib, tmp_path, order, compress, paf, lo, size):
+    hi = lo + size
+    with gp.Context(0) as ctx:
+        st = gp.GenStats()
+        ga, gb = str(tmp_path / "ga"), str(tmp_path / "gb")
+        ctx.check(ctx._lib.gp_generate_window(ctx.handle, order, compress, paf, lo >> 64, lo & (2**64 - 1), hi >> 64,
+                                              hi & (2**64 - 1), ga.encode(), gb.encode(), ctypes.byref(st)),
+                  "gp_generate_window")
+    oa, ob = str(tmp_path / "oa"), str(tmp_path / "ob")
+    ost = GenStats()
+    oracle_lib.gpo_generate_window(order, compress, paf, oa.encode(), ob.encode(), lo >> 64, lo & (2**64 - 1),
+                                   hi >> 64, hi & (2**64 - 1), ctypes.byref(ost))
+    assert read(ga) == read(oa)
+    assert read(gb) == read(ob)
+    assert st.necklaces == ost.necklaces
+
+
+def test_job_split_union(tmp_path):
+    """-n 3 jobs: each job's files, sorted together, equal the single run."""
+    for j in range(3):
+        golay(["34", "-c", "2", "-n", "3", "-j", str(j), "gen"], tmp_path / "split")
+    golay(["34", "-c", "2", "-n", "3", "sort"], tmp_path / "split")
+    golay(["34", "-c", "2", "all"], tmp_path / "single")  # all: gen sort match (no uncompress step: c list of 1)
+    for ab in "ab":
+        assert read(str(tmp_path / "split" / "order-34" / f"34-filtered_sorted-{ab}")) == \
+            read(str(tmp_path / "single" / "order-34" / f"34-filtered_sorted-{ab}"))
+
+
+def test_stage_by_stage_equals_all(tmp_path):
+    golay(["26", "-c", "2", "1", "gen"], tmp_path)
+    golay(["26", "-c", "2", "1", "sort"], tmp_path)
+    golay(["26", "-c", "2", "1", "match"], tmp_path)
+    golay(["26", "-c", "2", "1", "uncompress"], tmp_path)
+    _, wd = golay(["26", "-c", "2", "1", "filter"], tmp_path)
+    assert read(os.path.join(wd, "26-unique")) == read(os.path.join(GOLDEN, "n26", "26-unique"))
+
+
+def test_no_decomposition_returns_1(tmp_path):
+    r, _ = golay(["3", "gen"], tmp_path, check=False)  # 2*3 = 6 is not a sum of two squares
+    assert r.returncode == 1
+
+
+def test_match_empty_input_returns_1(tmp_path):
+    wd = tmp_path / "order-16"
+    wd.mkdir(parents=True)
+    (wd / "16-filtered_sorted-a").write_text("")
+    (wd / "16-filtered_sorted-b").write_text("PSD1 0 \n")
+    r, _ = golay(["16", "-c", "2", "match"], tmp_path, check=False)
+    assert r.returncode == 1
+    assert (wd / "16-pairs-2").exists() and (wd / "16-pairs-2").read_text() == ""
+
+
+def test_uncompress_malformed_line_fails(tmp_path):
+    wd = tmp_path / "order-16"
+    wd.mkdir(parents=True)
+    (wd / "16-pairs-2").write_text("0 0 0 2 0 0 0 2  -2 0 -2 2 2 0 2\n")  # 15 values, expected 16
+    r, _ = golay(["16", "-c", "2", "1", "uncompress"], tmp_path, check=False)
+    assert r.returncode != 0
+
+
+def test_sort_dedups_and_orders_bytewise(tmp_path):
+    lines = [b"PSD12 0 2 \n", b"PSD123 0 2 \n", b"PSD12 -2 2 \n", b"PSD12 0 2 \n", b"PSD1 2 2 \n"]
+    src = tmp_path / "in"
+    src.write_bytes(b"".join(lines))
+    out = tmp_path / "out"
+    with gp.Context(0) as ctx:
+        arr = (ctypes.c_char_p * 1)(str(src).encode())
+        ctx.check(ctx._lib.gp_sort(ctx.handle, ctypes.cast(arr, ctypes.c_void_p), 1, str(out).encode()), "gp_sort")
+    want = b"".join(sorted(set(lines)))
+    assert out.read_bytes() == want
