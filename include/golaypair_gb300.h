@@ -81,6 +81,26 @@ int gp_kernel_time(gp_ctx* ctx, double* total_ms, int64_t* launches);
  * counting on (enable != 0) or off for later launches. */
 int gp_debug_tc_trace(gp_ctx* ctx, int enable, uint64_t* out, int nout);
 
+/*
+ * The batched tensor-core PSD filter for callers that cannot allocate device
+ * memory (code running under another framework's allocator or memory pool,
+ * allocation-free real-time loops, devices whose memory is reserved by their
+ * owner).  No counterpart in the reference.  Same verdicts as
+ * gp_psd_filter_device in GP_PSD_TC_GUARDED mode, on DEVICE buffers, on
+ * `stream` (a cudaStream_t; NULL = legacy default stream), without a context.
+ * Allocates nothing: its working buffers live in one fixed static device
+ * array (about 4.3 MB, held by every GPU that loads the library until the
+ * process exits).  Limits and rules:
+ *   - n <= 2^20 rows (GP_ERR_ARG beyond, with a message on stderr);
+ *     2 <= L <= 128 (GP_ERR_UNSUPPORTED otherwise);
+ *   - the first call on a device looks up the array's device address there
+ *     (with that device current); make it before any stream capture;
+ *   - all calls share the array: calls that overlap on the GPU race;
+ *   - synchronous: returns after the stream has finished the work.
+ */
+int gp_psd_filter_noalloc(const int8_t* d_seqs, int64_t n, int L, int order, int paf, uint32_t* d_pass_mask,
+                          void* stream);
+
 /* Tensor-core PSD values (fp32, bins 1..L/2) of n rows, for error analysis.
  * out: n x (L/2) floats, HOST memory. */
 int gp_psd_tc_values(gp_ctx* ctx, const int8_t* seqs, int64_t n, int L, float* out);
