@@ -12,8 +12,10 @@
 //           144-165), then the tensor-core PSD filter at the new length,
 //           then finalize_kernel (exact FP64 PSD and signatures: a-side
 //           inverted, b-side plain, uncompression.cpp:195-207);
-//   device  sort + match of the two candidate sets (gp_sort_text /
-//           gp_match_texts), pairs appended in input-pair order.
+//   device  the signature join of the two candidate sets (join.cu) with
+//           exact PAF verification; only the matched pairs come back to
+//           the host, where they are put in the reference's line order
+//           (sorted a-line, then b-line) and appended in input-pair order.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -25,10 +27,7 @@
 #include "ctx.h"
 #include "finalize.h"
 #include "host_math.h"
-
-int gp_sort_text(gp_ctx* c, const std::string& text, std::string& out);
-int gp_match_texts(gp_ctx* c, int L, int compress, int paf, const std::string& ta, const std::string& tb,
-                   std::string& out, int64_t* n_pairs);
+#include "join.h"
 
 namespace {
 
@@ -182,10 +181,26 @@ void put_uint(std::string& s, unsigned v) {
     while (n) s.push_back(tmp[--n]);
 }
 
-// Expands one compressed sequence on the device; appends the candidate lines
-// of every expansion that passes the PSD filter to `text`.
-int expand_one(gp_ctx* c, std::vector<int> orig, int order, int compress, int new_compress, int paf, bool invert,
-               std::string& text, int64_t* n_exp) {
+// Device records of one side: packed words and signatures.
+struct Side {
+    DevBuf words, sig;
+    int64_t n = 0, cap = 0;
+};
+
+__global__ void gather_records_kernel(const uint4* words, const uint16_t* sig, int S, const uint32_t* rows, int64_t n,
+                                      uint4* ow, uint16_t* os) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t r = rows[i];
+        ow[i] = words[r];
+        for (int k = 0; k < S; ++k) os[i * S + k] = sig[(int64_t)r * S + k];
+    }
+}
+
+// Expands one compressed sequence on the device and keeps, in `side`, every
+// expansion that passes the PSD filter, with its signature
+// (uncompression.cpp:195-207; invert selects bound - rint(psd)).
+int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int new_compress, int paf, bool invert,
+                Side& side, int64_t* n_exp) {
     const int L = (int)orig.size();
     Expansion e = plan_expansion(orig, compress, new_compress);
     if (e.overflow) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: more than 2^62 expansions");
@@ -196,22 +211,27 @@ int expand_one(gp_ctx* c, std::vector<int> orig, int order, int compress, int ne
     if (L > kMaxPos || b * Lnew > 128 || !gp::tc_packed_supported(Lnew, b))
         return c->fail(GP_ERR_UNSUPPORTED, "uncompress: length %d over %d letters", Lnew, (int)nalpha.size());
     *n_exp += (int64_t)e.total;
+    side.n = 0;
     if (e.total == 0) return GP_OK;
     cudaStream_t s = c->s_comp;
-    DevBuf dcnt, doff, dvals, dwords, dmask, dunsure, didx, dmisc, drec;
+    DevBuf dcnt, doff, dvals, dwords, dmask, dunsure, didx, dmisc;
     const int64_t chunk = (int64_t)std::min<uint64_t>(e.total, uint64_t(1) << 24);
     if (!dcnt.ensure(L * 4) || !doff.ensure(L * 4) || !dvals.ensure(e.vals.size() + 16) || !dwords.ensure(chunk * 16) ||
         !dmask.ensure((chunk + 31) / 32 * 4) || !dunsure.ensure(chunk * 4) || !didx.ensure(chunk * 4) ||
         !dmisc.ensure(64))
         return c->fail(GP_ERR_NOMEM, "uncompress: device allocation");
+    // record arena: every expansion could pass; capped at 2^26 records
+    side.cap = (int64_t)std::min<uint64_t>(e.total, uint64_t(1) << 26);
+    if (!side.words.ensure((size_t)side.cap * 16) || !side.sig.ensure((size_t)side.cap * 2 * (Lnew - 1) + 16))
+        return c->fail(GP_ERR_NOMEM, "uncompress: record arena");
     GP_CUDA_TRY(c, cudaMemcpyAsync(dcnt.p, e.cnt.data(), L * 4, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(doff.p, e.off.data(), L * 4, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(dvals.p, e.vals.data(), e.vals.size(), cudaMemcpyHostToDevice, s));
     unsigned long long* misc = dmisc.as<unsigned long long>();  // [0] unsure [1] survivors [2] records [3] passes
+    GP_CUDA_TRY(c, cudaMemsetAsync(misc, 0, 64, s));
     const gp::RowSrc src{nullptr, dwords.as<uint4>(), Lnew, b, new_compress};
     const double* tw = c->twiddle64(Lnew);
     if (!tw) return c->fail(GP_ERR_NOMEM, "twiddles");
-    const int bound = 2 * order - paf;
     for (uint64_t r0 = 0; r0 < e.total; r0 += (uint64_t)chunk) {
         const int64_t n = (int64_t)std::min<uint64_t>((uint64_t)chunk, e.total - r0);
         ExpandArgs ea{L, r, Lnew, b, new_compress, r0, n, dcnt.as<int>(), doff.as<int>(), dvals.as<int8_t>(),
@@ -220,21 +240,12 @@ int expand_one(gp_ctx* c, std::vector<int> orig, int order, int compress, int ne
         if (blocks > (int64_t)c->num_sms * 16) blocks = (int64_t)c->num_sms * 16;
         expand_kernel<<<(unsigned)blocks, 256, 0, s>>>(ea);
         GP_CUDA_TRY(c, cudaGetLastError());
-        GP_CUDA_TRY(c, cudaMemsetAsync(misc, 0, 64, s));
+        GP_CUDA_TRY(c, cudaMemsetAsync(misc + 1, 0, 8, s));
         int rc = c->enqueue_filter(src, n, order, paf, GP_PSD_TC_GUARDED, dmask.as<uint32_t>(), dunsure.as<uint32_t>(),
                                    misc + 0, s);
         if (rc) return rc;
         GP_CUDA_TRY(c, gp::launch_mask_to_list(dmask.as<uint32_t>(), n, didx.as<uint32_t>(), misc + 1, n,
                                                c->status.as<int>(), c->num_sms, s));
-        unsigned long long surv = 0;
-        GP_CUDA_TRY(c, cudaMemcpyAsync(&surv, misc + 1, 8, cudaMemcpyDeviceToHost, s));
-        GP_CUDA_TRY(c, cudaStreamSynchronize(s));
-        rc = c->check_status("uncompress filter");
-        if (rc) return rc;
-        if (!surv) continue;
-        const size_t rec_bytes = (size_t)surv * (16 + 1 + 2 * (Lnew - 1)) + 64;
-        if (!drec.ensure(rec_bytes)) return c->fail(GP_ERR_NOMEM, "uncompress: records");
-        uint8_t* rb = drec.as<uint8_t>();
         gp::FinalizeArgs fa;
         fa.src = src;
         fa.roles = nullptr;
@@ -244,48 +255,107 @@ int expand_one(gp_ctx* c, std::vector<int> orig, int order, int compress, int ne
         fa.idx_cap = n;
         fa.tw = tw;
         fa.thr = 2.0 * order - paf + 0.001;
-        fa.bound = bound;
+        fa.bound = 2 * order - paf;
         fa.invert_roles = invert ? 1 : 0;
         fa.check_canonical = 0;
         fa.units = nullptr;
         fa.n_units = 0;
-        fa.rec_words = reinterpret_cast<uint4*>(rb);
-        fa.rec_role = rb + surv * 16;
-        fa.rec_sig = reinterpret_cast<uint16_t*>(rb + surv * 17 + ((surv * 17) & 1));
+        fa.rec_words = side.words.as<uint4>();
+        fa.rec_role = nullptr;
+        fa.rec_sig = side.sig.as<uint16_t>();
         fa.rec_src = nullptr;
-        fa.rec_count = misc + 2;
-        fa.rec_cap = (int64_t)surv;
+        fa.rec_count = misc + 2;  // accumulates over chunks
+        fa.rec_cap = side.cap;
         fa.psd_pass = misc + 3;
         fa.status = c->status.as<int>();
-        GP_CUDA_TRY(c, gp::launch_finalize(fa, (int64_t)surv, c->num_sms, s));
-        unsigned long long nrec = 0;
-        GP_CUDA_TRY(c, cudaMemcpyAsync(&nrec, misc + 2, 8, cudaMemcpyDeviceToHost, s));
-        GP_CUDA_TRY(c, cudaStreamSynchronize(s));
-        rc = c->check_status("uncompress finalize");
-        if (rc) return rc;
-        if (!nrec) continue;
-        std::vector<uint4> w(nrec);
-        std::vector<uint16_t> sg(nrec * (Lnew - 1));
-        GP_CUDA_TRY(c, cudaMemcpy(w.data(), fa.rec_words, nrec * 16, cudaMemcpyDeviceToHost));
-        GP_CUDA_TRY(c, cudaMemcpy(sg.data(), fa.rec_sig, sg.size() * 2, cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < nrec; ++i) {
-            const gp::u128 word = ((gp::u128)w[i].w << 96) | ((gp::u128)w[i].z << 64) | ((gp::u128)w[i].y << 32) | w[i].x;
-            text += "PSD";
-            for (int k = 0; k < Lnew - 1; ++k) put_uint(text, sg[i * (Lnew - 1) + k]);
-            text.push_back(' ');
-            for (int j = 0; j < Lnew; ++j) {
-                const int v = nalpha[gp::word_digit_h(word, b, Lnew, j)];
-                if (v < 0) {
-                    text.push_back('-');
-                    put_uint(text, (unsigned)(-v));
-                } else {
-                    put_uint(text, (unsigned)v);
-                }
-                text.push_back(' ');
-            }
-            text.push_back('\n');
-        }
+        GP_CUDA_TRY(c, gp::launch_finalize(fa, n, c->num_sms, s));
     }
+    unsigned long long nrec = 0;
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&nrec, misc + 2, 8, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    int rc = c->check_status("uncompress");
+    if (rc) return rc;
+    side.n = (int64_t)std::min<unsigned long long>(nrec, (unsigned long long)side.cap);
+    return GP_OK;
+}
+
+void put_seq(std::string& t, const std::vector<int>& alpha, gp::u128 word, int b, int L) {
+    for (int j = 0; j < L; ++j) {
+        const int v = alpha[gp::word_digit_h(word, b, L, j)];
+        if (v < 0) {
+            t.push_back('-');
+            put_uint(t, (unsigned)(-v));
+        } else {
+            put_uint(t, (unsigned)v);
+        }
+        t.push_back(' ');
+    }
+}
+
+// Joins the two sides and appends the matched pairs, in the reference's
+// order, to `out`.
+int join_sides(gp_ctx* c, Side& A, Side& B, int Lnew, int new_compress, int paf, std::string& out) {
+    const std::vector<int> nalpha = gp::alphabet(new_compress);
+    const int b = gp::bits_for((int)nalpha.size());
+    std::vector<std::pair<uint32_t, uint32_t>> m;
+    int rc = gp::device_join(c, gp::JoinSide{A.words.as<uint4>(), A.sig.as<uint16_t>(), A.n},
+                             gp::JoinSide{B.words.as<uint4>(), B.sig.as<uint16_t>(), B.n}, Lnew, b, new_compress,
+                             paf * new_compress, m);
+    if (rc || m.empty()) return rc;
+    const int S = Lnew - 1;
+    const int64_t nm = (int64_t)m.size();
+    std::vector<uint32_t> ra(nm), rb(nm);
+    for (int64_t i = 0; i < nm; ++i) {
+        ra[i] = m[i].first;
+        rb[i] = m[i].second;
+    }
+    cudaStream_t s = c->s_comp;
+    DevBuf dra, drb, wa, wb, sa, sb;
+    if (!dra.ensure(nm * 4) || !drb.ensure(nm * 4) || !wa.ensure(nm * 16) || !wb.ensure(nm * 16) ||
+        !sa.ensure(nm * S * 2 + 16) || !sb.ensure(nm * S * 2 + 16))
+        return c->fail(GP_ERR_NOMEM, "uncompress: gather");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dra.p, ra.data(), nm * 4, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(drb.p, rb.data(), nm * 4, cudaMemcpyHostToDevice, s));
+    const unsigned g = (unsigned)std::min<int64_t>((nm + 255) / 256, 4096);
+    gather_records_kernel<<<g, 256, 0, s>>>(A.words.as<uint4>(), A.sig.as<uint16_t>(), S, dra.as<uint32_t>(), nm,
+                                            wa.as<uint4>(), sa.as<uint16_t>());
+    gather_records_kernel<<<g, 256, 0, s>>>(B.words.as<uint4>(), B.sig.as<uint16_t>(), S, drb.as<uint32_t>(), nm,
+                                            wb.as<uint4>(), sb.as<uint16_t>());
+    GP_CUDA_TRY(c, cudaGetLastError());
+    std::vector<uint4> hwa(nm), hwb(nm);
+    std::vector<uint16_t> hsa((size_t)nm * S), hsb((size_t)nm * S);
+    GP_CUDA_TRY(c, cudaMemcpyAsync(hwa.data(), wa.p, nm * 16, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(hwb.data(), wb.p, nm * 16, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(hsa.data(), sa.p, hsa.size() * 2, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(hsb.data(), sb.p, hsb.size() * 2, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    auto word_of = [](const uint4& w) {
+        return ((gp::u128)w.w << 96) | ((gp::u128)w.z << 64) | ((gp::u128)w.y << 32) | w.x;
+    };
+    struct Item {
+        std::string a_line, b_line, pair_line;
+    };
+    std::vector<Item> items(nm);
+    for (int64_t i = 0; i < nm; ++i) {
+        Item& it = items[i];
+        const gp::u128 x = word_of(hwa[i]), y = word_of(hwb[i]);
+        std::string sa_txt, sb_txt;
+        put_seq(sa_txt, nalpha, x, b, Lnew);
+        put_seq(sb_txt, nalpha, y, b, Lnew);
+        it.a_line = "PSD";
+        for (int k = 0; k < S; ++k) put_uint(it.a_line, hsa[i * S + k]);
+        it.a_line.push_back(' ');
+        it.a_line += sa_txt;
+        it.b_line = "PSD";
+        for (int k = 0; k < S; ++k) put_uint(it.b_line, hsb[i * S + k]);
+        it.b_line.push_back(' ');
+        it.b_line += sb_txt;
+        it.pair_line = sa_txt + " " + sb_txt + "\n";
+    }
+    std::sort(items.begin(), items.end(), [](const Item& p, const Item& q) {
+        return p.a_line != q.a_line ? p.a_line < q.a_line : p.b_line < q.b_line;
+    });
+    for (auto& it : items) out += it.pair_line;
     return GP_OK;
 }
 
@@ -335,6 +405,7 @@ int gp_uncompress(gp_ctx* c, int order, int compress, int new_compress, int paf,
     const char* end = p + text.size();
     long line_no = 0;
     int rc = GP_OK;
+    Side side_a, side_b;
     while (p < end && rc == GP_OK) {
         const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
         if (!nl) nl = end;
@@ -359,22 +430,14 @@ int gp_uncompress(gp_ctx* c, int order, int compress, int new_compress, int paf,
         }
         ++line_no;
         std::vector<int> a(vals.begin(), vals.begin() + L), b(vals.begin() + L, vals.end());
-        std::string ta, tb, sa, sb, pairs;
+        std::string pairs;
         int64_t na = 0, nb = 0;
-        rc = expand_one(c, a, order, compress, new_compress, paf, true, ta, &na);
+        rc = expand_side(c, a, order, compress, new_compress, paf, true, side_a, &na);
         if (rc) break;
-        rc = expand_one(c, b, order, compress, new_compress, paf, false, tb, &nb);
+        rc = expand_side(c, b, order, compress, new_compress, paf, false, side_b, &nb);
         if (rc) break;
-        rc = gp_sort_text(c, ta, sa);
+        rc = join_sides(c, side_a, side_b, order / new_compress, new_compress, paf, pairs);
         if (rc) break;
-        rc = gp_sort_text(c, tb, sb);
-        if (rc) break;
-        int64_t np = 0;
-        const int mrc = gp_match_texts(c, order / new_compress, new_compress, paf, sa, sb, pairs, &np);
-        if (mrc < 0) {
-            rc = mrc;
-            break;
-        }
         fwrite(pairs.data(), 1, pairs.size(), out);
     }
     fclose(out);

@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kWarps * 32) finalize_kernel(FinalizeArgs a) {
             }
             if (lane == 0) {
                 a.rec_words[pos] = a.src.words ? a.src.words[row] : make_uint4(row, 0, 0, 0);
-                a.rec_role[pos] = (uint8_t)(1 << r);
+                if (a.rec_role) a.rec_role[pos] = (uint8_t)(1 << r);
                 if (a.rec_src) a.rec_src[pos] = row;
             }
         }

@@ -51,10 +51,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 // Twiddles built on the device: the tensor-core image in the same canonical
 // layout as build_twiddle_image, and the FP64 (cos, sin) table.
 __global__ void noalloc_twiddles_kernel(unsigned char* scratch, int L, int K) {
-    uint16_t* hi = reinterpret_cast<uint16_t*>(scratch + kOffImage);
-    uint16_t* lo = hi + (size_t)K * K;
+    // B operand image: 2K rows (hi rows 0..K-1, lo rows K..2K-1) x K columns
+    uint16_t* img = reinterpret_cast<uint16_t*>(scratch + kOffImage);
     double* tw = reinterpret_cast<double*>(scratch + kOffTw64);
-    const int N = K, H = L / 2;
+    const int N = K, NT = 2 * K, H = L / 2;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N * K; e += gridDim.x * blockDim.x) {
         const int nrow = e / K, j = e % K;
         const bool is_sin = nrow >= N / 2;
@@ -68,9 +68,11 @@ __global__ void noalloc_twiddles_kernel(unsigned char* scratch, int L, int K) {
         }
         const __half h = __double2half(w);
         const __half l = __double2half(w - (double)__half2float(h));
-        const size_t byte = (size_t)(j / 8) * (N / 8) * 128 + (size_t)(nrow / 8) * 128 + (nrow % 8) * 16 + (j % 8) * 2;
-        hi[byte / 2] = __half_as_ushort(h);
-        lo[byte / 2] = __half_as_ushort(l);
+        for (int part = 0; part < 2; ++part) {
+            const int nn = nrow + part * K;
+            const size_t byte = (size_t)(j / 8) * (NT / 8) * 128 + (size_t)(nn / 8) * 128 + (nn % 8) * 16 + (j % 8) * 2;
+            img[byte / 2] = __half_as_ushort(part ? l : h);
+        }
     }
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < L; m += gridDim.x * blockDim.x) {
         double s, c;

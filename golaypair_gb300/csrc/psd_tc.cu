@@ -4,12 +4,14 @@
 // psd[k] > 2n - paf + 0.001 for k = 1..L/2) as a batched dense contraction:
 //
 //   X[M=128 candidates x K] (fp16, exact small integers)
-//     * W[K x N] (cos/sin twiddles, split hi + lo fp16, both accumulated into
-//       one fp32 TMEM accumulator)   ->   re_k, im_k  ->  p_k = re^2 + im^2.
+//     * [W_hi | W_lo][K x 2K] (cos/sin twiddles split into hi + lo fp16)
+//     -> D[128 x 2K] fp32 in TMEM;  re_k = D_hi + D_lo, p_k = re^2 + im^2.
 //
-// Row n < N/2 of W is the cosine of bin n+1, row N/2 + n the sine of bin n+1;
+// One UMMA of N = 2K per 16-wide K step (hi and lo side by side) instead of
+// two passes of N = K: half the MMA instructions.  Within each half, row
+// n < K/2 of W is the cosine of bin n+1, row K/2 + n the sine of bin n+1;
 // bins above L/2 and columns j >= L are zero, so the padding columns of X
-// never contribute.  K = N = L rounded up to 16.
+// never contribute.  K = L rounded up to 16.
 //
 // Each candidate is classified against T = 2n - paf + 0.001 with a guard g
 // (the configured band, widened per row to a rigorous bound on the fp32
@@ -23,9 +25,14 @@
 //                [b(L-1-j), b(L-j)), value = 2*digit - c (the enumerator's
 //                and the uncompression expander's output).
 //
+// The A operand (the candidates) lives in tensor memory: each converter
+// thread owns one row = one TMEM lane and writes its fp16 pairs with
+// tcgen05.st, so shared memory only carries the raw input (written once by
+// the bulk-copy engine, read once by the converters) and the constant B.
+//
 // Persistent kernel, one 128-candidate tile per step, warp roles:
-//   warps 0-3  convert: staged tile -> fp16 A tile in the UMMA canonical
-//              K-major layout (+ sum x^2 for the int8 error bound)
+//   warps 0-3  convert: staged tile -> fp16 row in TMEM (+ sum x^2 for the
+//              int8 error bound)
 //   warps 4-7  epilogue: TMEM -> registers -> PSD max -> mask / unsure list
 //   warp 8     producer: cp.async.bulk of each tile into a deep ring
 //   warp 9     MMA issuer (one lane) and TMEM owner
@@ -40,27 +47,33 @@ namespace gp {
 namespace {
 
 constexpr int kThreads = 320;
+constexpr int kConvWarps = 4;
 constexpr int kRawSlack = 64;
 constexpr int kMaxRawStages = 12;
 constexpr uint32_t kSmemBudget2Cta = 112 * 1024;  // two CTAs per SM
 constexpr uint32_t kSmemBudget1Cta = 220 * 1024;
 constexpr int kLutBytes = 4096;
 
+// accumulator buffers and TMEM A stages per K (columns: NACC*2K + AS*K/2)
+constexpr int tc_nacc(int K) { return K == 16 ? 4 : K == 32 ? 3 : K == 48 ? 2 : K == 64 ? 3 : K <= 96 ? 2 : K == 112 ? 2 : 1; }
+constexpr int tc_as(int K) { return K == 16 ? 4 : K == 32 ? 3 : K == 48 ? 2 : K <= 80 ? 4 : K == 96 ? 2 : K == 112 ? 1 : 4; }
+
 template <int K>
 struct TcCfg {
     static constexpr int M = kTileM;
-    static constexpr int N = K;
-    static constexpr int KCH = K / 8;                  // core-matrix columns along K
-    static constexpr int KSTEPS = K / 16;              // UMMA instructions per pass
-    static constexpr int A_BYTES = M * K * 2;
-    static constexpr int A_KSTRIDE = (M / 8) * 128;    // bytes between K-adjacent core matrices
-    static constexpr int B_BYTES = N * K * 2;
+    static constexpr int N = 2 * K;                    // UMMA N: hi half then lo half
+    static constexpr int KCH = K / 8;                  // 8-element chunks along K
+    static constexpr int KW = K / 4 + 1;               // 32-bit words covering a row's K bytes + misalignment
+    static constexpr int KSTEPS = K / 16;              // UMMA instructions per tile
+    static constexpr int B_BYTES = N * K * 2;          // whole B image (hi and lo)
     static constexpr int B_KSTRIDE = (N / 8) * 128;
-    static constexpr int A_STAGES = K <= 64 ? 3 : 2;
-    static constexpr int NACC = (256 / N) < 4 ? (256 / N) : 4;
-    static constexpr int RING = A_STAGES + NACC;       // sum x^2 stash slots
-    static constexpr int TMEM_COLS = 256;
-    static constexpr int MIN_BLOCKS = K <= 64 ? 2 : 1;
+    static constexpr int MIN_BLOCKS = K <= 48 ? 2 : 1;
+    static constexpr int TMEM_COLS = MIN_BLOCKS == 2 ? 256 : 512;
+    static constexpr int NACC = tc_nacc(K);
+    static constexpr int AS = tc_as(K);                // A stages in TMEM
+    static constexpr int A_COL0 = NACC * N;            // first TMEM column of the A stages
+    static constexpr int RING = AS + NACC;             // sum x^2 stash slots
+    static_assert(NACC * N + AS * K / 2 <= TMEM_COLS, "TMEM budget");
 };
 
 struct SmemLayout {
@@ -73,16 +86,15 @@ SmemLayout smem_layout(int row_bytes) {
     SmemLayout s;
     uint32_t off = 0;
     s.b_off = off;
-    off += 2 * C::B_BYTES;
+    off += C::B_BYTES;
     off = (off + 1023) & ~1023u;
     s.a_off = off;
-    off += C::A_STAGES * C::A_BYTES;
     s.lut_off = off;
     off += kLutBytes;
     s.stash_off = off;
     off += C::RING * kTileM * 4;
     s.bar_off = off;
-    off += (2 * kMaxRawStages + 2 * C::A_STAGES + 2 * C::NACC + C::RING + 2) * 8;
+    off += (2 * kMaxRawStages + 2 * C::AS + 2 * C::NACC + C::RING + 2) * 8;
     s.misc_off = off;
     off += 16;
     off = (off + 127) & ~127u;
@@ -154,12 +166,15 @@ __device__ __forceinline__ uint4 packed_chunk(const uint32_t (&w)[4], const uint
     return out;
 }
 
-template <int B, int KCH, int CH = 0>
-__device__ __forceinline__ void packed_row(const uint32_t (&w)[4], const uint8_t* lut, uint8_t* A, int r,
-                                           int kstride) {
-    if constexpr (CH < KCH) {
-        *reinterpret_cast<uint4*>(A + CH * kstride + r * 16) = packed_chunk<B, CH>(w, lut);
-        packed_row<B, KCH, CH + 1>(w, lut, A, r, kstride);
+template <int B, int CH, int CHEND>
+__device__ __forceinline__ void packed_row(const uint32_t (&w)[4], const uint8_t* lut, uint32_t* h) {
+    if constexpr (CH < CHEND) {
+        const uint4 v = packed_chunk<B, CH>(w, lut);
+        h[4 * CH] = v.x;
+        h[4 * CH + 1] = v.y;
+        h[4 * CH + 2] = v.z;
+        h[4 * CH + 3] = v.w;
+        packed_row<B, CH + 1, CHEND>(w, lut, h);
     }
 }
 
@@ -171,7 +186,6 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw_base) + 1023) & ~uintptr_t(1023));
 
     uint8_t* sB = smem + lay.b_off;
-    uint8_t* sA = smem + lay.a_off;
     uint8_t* sLut = smem + lay.lut_off;
     uint8_t* sRaw = smem + lay.raw_off;
     float* stash = reinterpret_cast<float*>(smem + lay.stash_off);
@@ -179,8 +193,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     uint64_t* raw_full = bars;
     uint64_t* raw_empty = bars + kMaxRawStages;
     uint64_t* a_full = bars + 2 * kMaxRawStages;
-    uint64_t* a_empty = a_full + C::A_STAGES;
-    uint64_t* acc_full = a_empty + C::A_STAGES;
+    uint64_t* a_empty = a_full + C::AS;
+    uint64_t* acc_full = a_empty + C::AS;
     uint64_t* acc_empty = acc_full + C::NACC;
     uint64_t* b_full = acc_empty + C::NACC;
     uint64_t* final_bar = b_full + 1;
@@ -201,10 +215,10 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     if (threadIdx.x == 0) {
         for (int i = 0; i < RS; ++i) {
             mbar_init(&raw_full[i], 1);
-            mbar_init(&raw_empty[i], 4);
+            mbar_init(&raw_empty[i], kConvWarps);
         }
-        for (int i = 0; i < C::A_STAGES; ++i) {
-            mbar_init(&a_full[i], 4);
+        for (int i = 0; i < C::AS; ++i) {
+            mbar_init(&a_full[i], kConvWarps);
             mbar_init(&a_empty[i], 1);
         }
         for (int i = 0; i < C::NACC; ++i) {
@@ -213,7 +227,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         }
         mbar_init(b_full, 1);
         mbar_init(final_bar, 1);
-        for (int i = 0; i < C::RING; ++i) mbar_init(&stash_full[i], 4);
+        for (int i = 0; i < C::RING; ++i) mbar_init(&stash_full[i], kConvWarps);
         *abort_flag = 0;
         mbar_fence_init();
     }
@@ -226,9 +240,9 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     tc_fence_after();
     const uint32_t tmem_base = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
 
-    if (warp < 4) {
+    if (warp < kConvWarps) {
         // ------------------------------------------------ converters
-        const int r = threadIdx.x;  // row of the tile
+        const int r = threadIdx.x;  // row of the tile = TMEM lane
         uint32_t mlo[C::KCH], mhi[C::KCH];
 #pragma unroll
         for (int c = 0; c < C::KCH; ++c) {
@@ -237,44 +251,43 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             mhi[c] = v >= 8 ? 0xFFFFFFFFu : (v <= 4 ? 0u : ((1u << (8 * (v - 4))) - 1u));
         }
         const int norm = 128 - B * L;  // packed: left shift that puts digit 0 at bit 127
+        const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16) + (uint32_t)C::A_COL0;
         int64_t it = 0;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             const int rs = (int)(it % RS);
             const uint32_t rph = (uint32_t)((it / RS) & 1);
-            const int as = (int)(it % C::A_STAGES);
-            const uint32_t aph = (uint32_t)((it / C::A_STAGES) & 1);
-            const long long c0 = clock64();
+            const int as = (int)(it % C::AS);
+            const uint32_t aph = (uint32_t)((it / C::AS) & 1);
+            const long long c0t = clock64();
             if (!mbar_wait(&raw_full[rs], rph, abort_flag, a.status, 1)) break;
-            const long long c1 = clock64();
+            const long long c1t = clock64();
             if (!mbar_wait(&a_empty[as], aph ^ 1u, abort_flag, a.status, 2)) break;
-            const long long c2 = clock64();
-            tr0 += c1 - c0;
-            tr1 += c2 - c1;
-            uint8_t* A = sA + as * C::A_BYTES;
+            const long long c2t = clock64();
+            tr0 += c1t - c0t;
+            tr1 += c2t - c1t;
+            tc_fence_after();
             const int64_t row = t * kTileM + r;
             const bool full_tile = aligned && (t + 1) * kTileM <= n;
             int sumsq = 0;
+            uint32_t h[K / 2];  // the row as fp16 pairs
             if constexpr (B == 0) {
                 if (full_tile) {
                     const uint8_t* raw = sRaw + rs * lay.raw_stride;
                     const int off = r * L;
+                    const uint32_t* wp = reinterpret_cast<const uint32_t*>(raw + (off & ~3));
+                    const uint32_t sh = (uint32_t)(off & 3) * 8u;
+                    uint32_t wv[C::KW];
+#pragma unroll
+                    for (int i = 0; i < C::KW; ++i) wv[i] = wp[i];
 #pragma unroll
                     for (int c = 0; c < C::KCH; ++c) {
-                        const int o = off + 8 * c;
-                        const int base = o & ~3;
-                        const uint32_t sh = (uint32_t)(o & 3) * 8u;
-                        const uint32_t w0 = *reinterpret_cast<const uint32_t*>(raw + base);
-                        const uint32_t w1 = *reinterpret_cast<const uint32_t*>(raw + base + 4);
-                        const uint32_t w2 = *reinterpret_cast<const uint32_t*>(raw + base + 8);
-                        const uint32_t lo = __funnelshift_r(w0, w1, sh) & mlo[c];
-                        const uint32_t hi = __funnelshift_r(w1, w2, sh) & mhi[c];
+                        const uint32_t lo = __funnelshift_r(wv[2 * c], wv[2 * c + 1], sh) & mlo[c];
+                        const uint32_t hi = __funnelshift_r(wv[2 * c + 1], wv[2 * c + 2], sh) & mhi[c];
                         sumsq = __dp4a((int)lo, (int)lo, sumsq);
                         sumsq = __dp4a((int)hi, (int)hi, sumsq);
-                        uint4 h;
-                        i8x4_to_h2x2(lo, h.x, h.y);
-                        i8x4_to_h2x2(hi, h.z, h.w);
-                        *reinterpret_cast<uint4*>(A + c * C::A_KSTRIDE + r * 16) = h;
+                        i8x4_to_h2x2(lo, h[4 * c], h[4 * c + 1]);
+                        i8x4_to_h2x2(hi, h[4 * c + 2], h[4 * c + 3]);
                     }
                 } else {
                     const bool valid = row < n;
@@ -290,10 +303,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         }
                         sumsq = __dp4a((int)w[0], (int)w[0], sumsq);
                         sumsq = __dp4a((int)w[1], (int)w[1], sumsq);
-                        uint4 h;
-                        i8x4_to_h2x2(w[0], h.x, h.y);
-                        i8x4_to_h2x2(w[1], h.z, h.w);
-                        *reinterpret_cast<uint4*>(A + c * C::A_KSTRIDE + r * 16) = h;
+                        i8x4_to_h2x2(w[0], h[4 * c], h[4 * c + 1]);
+                        i8x4_to_h2x2(w[1], h[4 * c + 2], h[4 * c + 3]);
                     }
                 }
             } else {
@@ -305,7 +316,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 }
                 // normalise: 128-bit left shift by `norm` puts digit 0 at bit 127
                 const uint32_t w[4] = {wv.x, wv.y, wv.z, wv.w};
-                uint32_t s[4];
+                uint32_t sw[4];
                 const int ws = norm >> 5, bs = norm & 31;
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
@@ -316,21 +327,25 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         cur = (si == k) ? w[k] : cur;
                         prev = (si - 1 == k) ? w[k] : prev;
                     }
-                    s[i] = bs ? ((cur << bs) | (prev >> (32 - bs))) : cur;
+                    sw[i] = bs ? ((cur << bs) | (prev >> (32 - bs))) : cur;
                 }
-                packed_row<B, C::KCH>(s, sLut, A, r, C::A_KSTRIDE);
+                packed_row<B, 0, C::KCH>(sw, sLut, h);
             }
+            const uint32_t aaddr = lane_base + (uint32_t)(as * (K / 2));
+#pragma unroll
+            for (int g = 0; g < K / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
             if constexpr (B == 0) stash[(int)(it % C::RING) * kTileM + r] = (float)sumsq;
-            const long long c3 = clock64();
-            tr3 += c3 - c2;
-            fence_proxy_async_smem();
+            const long long c3t = clock64();
+            tr3 += c3t - c2t;
+            tmem_wait_st();
+            tc_fence_before();
             __syncwarp();
             if (lane == 0) {
                 if constexpr (B == 0) mbar_arrive(&stash_full[(int)(it % C::RING)]);
                 mbar_arrive(&a_full[as]);
                 mbar_arrive(&raw_empty[rs]);
             }
-            tr2 += clock64() - c2;
+            tr2 += clock64() - c2t;
         }
         if (a.trace && lane == 0) {
             atomicAdd(&a.trace[kTrConvWaitRaw], tr0);
@@ -339,30 +354,52 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             atomicAdd(&a.trace[kTrConvFence], tr2 - tr3);
             if (warp == 0) atomicAdd(&a.trace[kTrTiles], (unsigned long long)it);
         }
-    } else if (warp < 8) {
+    } else if (warp < kConvWarps + 4) {
         // ------------------------------------------------ epilogue
-        const int q = warp - 4;  // TMEM lane quarter
+        const int q = warp & 3;  // TMEM lane quarter (warps 4..7)
         const float thr = a.thr;
         const float sq = sqrtf(thr);
         // packed rows: |value| <= c, so sum|x| <= L c for every row
         const float d_const = a.err_coef * (float)L * (float)a.alpha_c;
         const float g_const = fmaxf(a.guard_cfg, 2.f * sq * d_const + 3.f * d_const * d_const + 1e-4f);
+        constexpr int HB = K / 2;  // bins per half (cos block then sin block)
         int64_t it = 0;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
             const int b = (int)(it % C::NACC);
             const uint32_t ph = (uint32_t)((it / C::NACC) & 1);
-            const long long c0 = clock64();
+            const long long c0t = clock64();
             if (!mbar_wait(&acc_full[b], ph, abort_flag, a.status, 3)) break;
-            const long long c1 = clock64();
-            tr0 += c1 - c0;
+            const long long c1t = clock64();
+            tr0 += c1t - c0t;
             tc_fence_after();
-            float v[C::N];
-            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * C::N);
-#pragma unroll
-            for (int c = 0; c < C::N / 16; ++c) tmem_ld16(taddr + 16 * c, v + 16 * c);
-            tmem_wait_ld();
             const int r = q * 32 + lane;
+            const int64_t row = t * kTileM + r;
+            const bool valid = row < n;
+            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * C::N);
+            float pmax = 0.f;
+#pragma unroll
+            for (int ch = 0; ch < HB / 8; ++ch) {
+                float chi[8], shi[8], clo[8], slo[8];
+                tmem_ld8(taddr + 8 * ch, chi);
+                tmem_ld8(taddr + HB + 8 * ch, shi);
+                tmem_ld8(taddr + K + 8 * ch, clo);
+                tmem_ld8(taddr + K + HB + 8 * ch, slo);
+                tmem_wait_ld();
+#pragma unroll
+                for (int k = 0; k < 8; k += 2) {
+                    const float2 re = __fadd2_rn(make_float2(chi[k], chi[k + 1]), make_float2(clo[k], clo[k + 1]));
+                    const float2 im = __fadd2_rn(make_float2(shi[k], shi[k + 1]), make_float2(slo[k], slo[k + 1]));
+                    const float2 p = __ffma2_rn(re, re, __fmul2_rn(im, im));
+                    pmax = fmaxf(pmax, fmaxf(p.x, p.y));
+                    if constexpr (WRITE_PSD) {
+                        if (valid) {
+                            a.psd_out[row * HB + 8 * ch + k] = p.x;
+                            a.psd_out[row * HB + 8 * ch + k + 1] = p.y;
+                        }
+                    }
+                }
+            }
             float g = g_const;
             if constexpr (B == 0) {
                 // The converters wrote sum x^2 for this tile before the A tile
@@ -370,27 +407,17 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 // MMA of a later use waits for this epilogue to free its
                 // accumulator.
                 const int slot = (int)(it % C::RING);
-                const long long c3 = clock64();
+                const long long c3t = clock64();
                 if (!mbar_wait(&stash_full[slot], (uint32_t)((it / C::RING) & 1), abort_flag, a.status, 11)) break;
-                tr1 += clock64() - c3;
+                tr1 += clock64() - c3t;
                 // sum|x| <= sqrt(L * sum x^2)
-                const float d = a.err_coef * sqrtf((float)L * stash[slot * kTileM + r]);
+                const float ssq = stash[slot * kTileM + r];
+                const float d = a.err_coef * sqrtf((float)L * ssq);
                 g = fmaxf(a.guard_cfg, 2.f * sq * d + 3.f * d * d + 1e-4f);
             }
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[b]);
-
-            float pmax = 0.f;
-#pragma unroll
-            for (int k = 0; k < C::N / 2; k += 2) {
-                const float2 cs = make_float2(v[k], v[k + 1]);
-                const float2 sn = make_float2(v[C::N / 2 + k], v[C::N / 2 + k + 1]);
-                const float2 p = __ffma2_rn(cs, cs, __fmul2_rn(sn, sn));
-                pmax = fmaxf(pmax, fmaxf(p.x, p.y));
-            }
-            const int64_t row = t * kTileM + r;
-            const bool valid = row < n;
             const bool sure = valid && pmax < thr - g;
             const bool unsure = valid && !sure && pmax <= thr + g;
             const uint32_t bits = __ballot_sync(0xFFFFFFFFu, sure || unsure);
@@ -409,26 +436,19 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
                 }
             }
-            if constexpr (WRITE_PSD) {
-                if (valid) {
-#pragma unroll
-                    for (int k = 0; k < C::N / 2; ++k)
-                        a.psd_out[row * (C::N / 2) + k] = fmaf(v[k], v[k], v[C::N / 2 + k] * v[C::N / 2 + k]);
-                }
-            }
-            tr2 += clock64() - c1;
+            tr2 += clock64() - c1t;
         }
         if (a.trace && lane == 0) {
             atomicAdd(&a.trace[kTrEpiWaitAcc], tr0);
             atomicAdd(&a.trace[kTrEpiWaitStash], tr1);
             atomicAdd(&a.trace[kTrEpiWork], tr2 - tr1);
         }
-    } else if (warp == 8) {
+    } else if (warp == kConvWarps + 4) {
         // ------------------------------------------------ producer
         int64_t it = 0;
         if (lane == 0) {
-            mbar_arrive_expect_tx(b_full, 2 * C::B_BYTES);
-            bulk_g2s(sB, a.bimage, 2 * C::B_BYTES, b_full);
+            mbar_arrive_expect_tx(b_full, C::B_BYTES);
+            bulk_g2s(sB, a.bimage, C::B_BYTES, b_full);
             const uint8_t* src = B == 0 ? reinterpret_cast<const uint8_t*>(a.seqs)
                                         : reinterpret_cast<const uint8_t*>(a.words);
             unsigned long long tr0 = 0, tr1 = 0;
@@ -480,14 +500,15 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_f16_f32(C::M, C::N);
-            const uint32_t aBase = smem_u32(sA);
-            const uint32_t bBase = smem_u32(sB);
+            // B descriptor of k-step 0; later steps add to the start-address
+            // field (bits 0-13, address >> 4)
+            const uint64_t bdesc0 = sdesc_noswizzle(smem_u32(sB), C::B_KSTRIDE, 128);
             bool ok = mbar_wait(b_full, 0, abort_flag, a.status, 5);
             int64_t it = 0;
             unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
             for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++it) {
-                const int as = (int)(it % C::A_STAGES);
-                const uint32_t aph = (uint32_t)((it / C::A_STAGES) & 1);
+                const int as = (int)(it % C::AS);
+                const uint32_t aph = (uint32_t)((it / C::AS) & 1);
                 const int b = (int)(it % C::NACC);
                 const uint32_t bph = (uint32_t)((it / C::NACC) & 1);
                 const long long c0 = clock64();
@@ -499,17 +520,11 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 tr1 += c2 - c1;
                 tc_fence_after();
                 const uint32_t d = tmem_base + (uint32_t)(b * C::N);
-                const uint32_t aS = aBase + (uint32_t)(as * C::A_BYTES);
+                const uint32_t a0 = tmem_base + (uint32_t)(C::A_COL0 + as * (K / 2));
 #pragma unroll
-                for (int pass = 0; pass < 2; ++pass) {
-#pragma unroll
-                    for (int ks = 0; ks < C::KSTEPS; ++ks) {
-                        const uint64_t ad = sdesc_noswizzle(aS + (uint32_t)(ks * 2 * C::A_KSTRIDE), C::A_KSTRIDE, 128);
-                        const uint64_t bd = sdesc_noswizzle(
-                            bBase + (uint32_t)(pass * C::B_BYTES + ks * 2 * C::B_KSTRIDE), C::B_KSTRIDE, 128);
-                        umma_f16(d, ad, bd, idesc, (pass | ks) != 0 ? 1u : 0u);
-                    }
-                }
+                for (int ks = 0; ks < C::KSTEPS; ++ks)
+                    umma_f16_ts(d, a0 + (uint32_t)(8 * ks), bdesc0 + (uint64_t)((ks * 2 * C::B_KSTRIDE) >> 4), idesc,
+                                ks != 0 ? 1u : 0u);
                 const long long c3 = clock64();
                 umma_commit(&a_empty[as]);
                 umma_commit(&acc_full[b]);
@@ -637,10 +652,11 @@ float tc_err_coef(int K) {
 }
 
 size_t build_twiddle_image(int L, int K, void* out) {
-    const int N = K;
-    const size_t tile = (size_t)N * K * 2;
-    if (!out) return 2 * tile;
-    std::vector<uint16_t> hi((size_t)N * K, 0), lo((size_t)N * K, 0);
+    // B operand: 2K rows (hi rows 0..K-1, lo rows K..2K-1) x K columns
+    const int N = K, NT = 2 * K;
+    const size_t bytes = (size_t)NT * K * 2;
+    if (!out) return bytes;
+    std::vector<uint16_t> img((size_t)NT * K, 0);
     const int H = L / 2;
     const double two_pi = 6.283185307179586476925286766559;
     for (int nrow = 0; nrow < N; ++nrow) {
@@ -653,15 +669,16 @@ size_t build_twiddle_image(int L, int K, void* out) {
             const uint16_t h = half_bits(w);
             const uint16_t l = half_bits(w - half_value(h));
             // canonical no-swizzle K-major layout: core matrix (n/8, j/8) at
-            // (j/8) * (N/8) * 128 + (n/8) * 128, row n%8 at +16, col j%8 at +2
-            const size_t byte = (size_t)(j / 8) * (N / 8) * 128 + (size_t)(nrow / 8) * 128 + (nrow % 8) * 16 + (j % 8) * 2;
-            hi[byte / 2] = h;
-            lo[byte / 2] = l;
+            // (j/8) * (NT/8) * 128 + (n/8) * 128, row n%8 at +16, col j%8 at +2
+            for (int part = 0; part < 2; ++part) {
+                const int n = nrow + part * K;
+                const size_t byte = (size_t)(j / 8) * (NT / 8) * 128 + (size_t)(n / 8) * 128 + (n % 8) * 16 + (j % 8) * 2;
+                img[byte / 2] = part ? l : h;
+            }
         }
     }
-    std::memcpy(out, hi.data(), tile);
-    std::memcpy(static_cast<uint8_t*>(out) + tile, lo.data(), tile);
-    return 2 * tile;
+    std::memcpy(out, img.data(), bytes);
+    return bytes;
 }
 
 cudaError_t launch_psd_tc(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
