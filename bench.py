@@ -357,6 +357,79 @@ def run_gpu(args):
     return 0
 
 
+def _windows():
+    """Seed-chosen 2^32-word rank windows of the uneven-batch configuration
+    (orders 34, 50, 58, 68 at compression 2 and 90 at compression 5); a
+    space smaller than the window is enumerated whole."""
+    import numpy as np
+    out = []
+    for order, comp in [(34, 2), (50, 2), (58, 2), (68, 2), (90, 5)]:
+        L = order // comp
+        k = len(range(-comp, comp + 1, 2)) if comp % 2 == 0 else comp + 1
+        space = k ** L
+        if space <= 2 ** 32:
+            lo, hi = 0, space
+        else:
+            lo = int(np.random.default_rng(order * 1000 + comp).integers(0, space - 2 ** 32))
+            hi = lo + 2 ** 32
+        out.append((order, comp, 0, lo, hi))
+    return out
+
+
+def run_pipeline(args):
+    """Times the search stages on the generation configurations (one JSON
+    line each): full generation of order 57 (paf -2, compression 3), its sort
+    and match, uncompression of its first pairs, and the 2^32-word windows."""
+    import ctypes
+    import tempfile
+
+    import golaypair_gb300 as gp
+    env = dict(os.environ, LC_ALL="C")
+    with gp.Context(0) as ctx, tempfile.TemporaryDirectory() as tmp:
+        def gen_window(order, comp, paf, lo, hi):
+            st = gp.GenStats()
+            t0 = time.perf_counter()
+            ctx.check(ctx._lib.gp_generate_window(ctx.handle, order, comp, paf, lo >> 64, lo & (2**64 - 1), hi >> 64,
+                                                  hi & (2**64 - 1), os.path.join(tmp, "a").encode(),
+                                                  os.path.join(tmp, "b").encode(), ctypes.byref(st)),
+                      "gp_generate_window")
+            return st, time.perf_counter() - t0
+        gen_window(16, 2, 0, 0, 3 ** 8)  # warm-up (module load, twiddles)
+        for order, comp, paf, lo, hi in _windows():
+            st, el = gen_window(order, comp, paf, lo, hi)
+            print(json.dumps({"pipeline": "window", "order": order, "compress": comp, "paf": paf,
+                              "rank_window": [lo, hi], "seconds": el, "necklaces": st.necklaces,
+                              "candidates": st.candidates, "psd_pass": st.psd_pass,
+                              "written": st.written_a + st.written_b, "unsure": st.unsure,
+                              "necklaces_per_s": st.necklaces / el, "candidates_per_s": st.candidates / el}))
+        cli = gp.CLI_PATH
+        d = os.path.join(tmp, "r57")
+        times = {}
+        for stage in ("gen", "sort", "match"):
+            t0 = time.perf_counter()
+            subprocess.run([cli, "57", "-c", "3", "1", "--paf", "-2", "--dir", d, stage], check=True, env=env,
+                           stdout=subprocess.DEVNULL)
+            times[stage] = time.perf_counter() - t0
+        wd = os.path.join(d, "order-57")
+        with open(os.path.join(wd, "57-pairs-3")) as f:
+            pairs = f.readlines()
+        head = pairs[:args.pipeline_pairs]
+        with open(os.path.join(wd, "57-head-3"), "w") as f:
+            f.writelines(head)
+        t0 = time.perf_counter()
+        subprocess.run([cli, "57", "-c", "3", "1", "--paf", "-2", "--dir", d, "uncompress", "-i", "head", "-o",
+                        "headout"], check=True, env=env, stdout=subprocess.DEVNULL)
+        times["uncompress"] = time.perf_counter() - t0
+        with open(os.path.join(wd, "57-headout-1")) as f:
+            found = sum(1 for _ in f)
+        lines = {fn: sum(1 for _ in open(os.path.join(wd, fn))) for fn in
+                 ("57-filtered-a#0", "57-filtered-b#0", "57-pairs-3")}
+        print(json.dumps({"pipeline": "order57", "order": 57, "compress": [3, 1], "paf": -2,
+                          "seconds": times, "lines": lines, "uncompressed_pairs_of_first": [len(head), found],
+                          "note": "process wall times of the golay driver, including context creation"}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -366,11 +439,15 @@ def main():
     ap.add_argument("--rows", type=int, default=1 << 28, help="batch rows (profiling runs only)")
     ap.add_argument("--profile", action="store_true", help="time the tensor-core filter only")
     ap.add_argument("--trace", action="store_true", help="with --profile: per-role cycle counters")
+    ap.add_argument("--pipeline", action="store_true", help="time the generation configurations instead")
+    ap.add_argument("--pipeline-pairs", type=int, default=200, help="compressed pairs to uncompress (--pipeline)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.pipeline:
+        return run_pipeline(args)
     return run_gpu(args)
 
 

@@ -131,6 +131,13 @@ int gp_ctx_create(gp_ctx** out, int device) {
         cudaEventCreateWithFlags(&c->ev_h2d[i], cudaEventDisableTiming);
         cudaEventCreateWithFlags(&c->ev_done[i], cudaEventDisableTiming);
     }
+    for (int i = 0; i < gp_ctx::kCopyStreams; ++i) {
+        if (cudaStreamCreateWithFlags(&c->s_copies[i], cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            return GP_ERR_CUDA;
+        }
+        cudaEventCreateWithFlags(&c->ev_part[i], cudaEventDisableTiming);
+    }
     if (!c->status.ensure(sizeof(int)) || !c->counts.ensure(64 * sizeof(unsigned long long)) ||
         !c->h_counts.ensure(64 * sizeof(unsigned long long))) {
         delete c;
@@ -163,6 +170,10 @@ int gp_ctx_destroy(gp_ctx* c) {
     for (auto& b : c->hscratch) b.release();
     if (c->s_comp) cudaStreamDestroy(c->s_comp);
     if (c->s_copy) cudaStreamDestroy(c->s_copy);
+    for (int i = 0; i < gp_ctx::kCopyStreams; ++i) {
+        if (c->s_copies[i]) cudaStreamDestroy(c->s_copies[i]);
+        if (c->ev_part[i]) cudaEventDestroy(c->ev_part[i]);
+    }
     delete c;
     return GP_OK;
 }
@@ -255,11 +266,21 @@ int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, in
         const int b = (int)(ci & 1);
         const int64_t r0 = ci * chunk;
         const int64_t rows = std::min(chunk, n - r0);
-        if (ci >= 2) GP_CUDA_TRY(c, cudaStreamWaitEvent(c->s_copy, c->ev_done[b], 0));
-        GP_CUDA_TRY(c, cudaMemcpyAsync(c->seq_buf[b].p, seqs + r0 * L, (size_t)rows * L, cudaMemcpyHostToDevice,
-                                       c->s_copy));
-        GP_CUDA_TRY(c, cudaEventRecord(c->ev_h2d[b], c->s_copy));
-        GP_CUDA_TRY(c, cudaStreamWaitEvent(c->s_comp, c->ev_h2d[b], 0));
+        // the chunk's host->device copy is split over several copy streams
+        // (several copy engines in flight); compute waits for all parts
+        const size_t bytes = (size_t)rows * L;
+        const size_t part = (bytes / gp_ctx::kCopyStreams + 4095) & ~size_t(4095);
+        for (int q = 0; q < gp_ctx::kCopyStreams; ++q) {
+            const size_t o = (size_t)q * part;
+            if (o >= bytes) break;
+            const size_t nb = std::min(part, bytes - o);
+            if (ci >= 2) GP_CUDA_TRY(c, cudaStreamWaitEvent(c->s_copies[q], c->ev_done[b], 0));
+            GP_CUDA_TRY(c, cudaMemcpyAsync(static_cast<uint8_t*>(c->seq_buf[b].p) + o,
+                                           reinterpret_cast<const uint8_t*>(seqs) + r0 * L + o, nb,
+                                           cudaMemcpyHostToDevice, c->s_copies[q]));
+            GP_CUDA_TRY(c, cudaEventRecord(c->ev_part[q], c->s_copies[q]));
+            GP_CUDA_TRY(c, cudaStreamWaitEvent(c->s_comp, c->ev_part[q], 0));
+        }
         rc = c->enqueue_filter(int8_src(c->seq_buf[b].as<int8_t>(), L), rows, order, paf, mode,
                                c->mask_buf[b].as<uint32_t>(), c->unsure_buf[b].as<uint32_t>(), d_counts + b, c->s_comp);
         if (rc) return rc;
@@ -275,7 +296,7 @@ int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, in
         }
     }
     GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_comp));
-    GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_copy));
+    for (int q = 0; q < gp_ctx::kCopyStreams; ++q) GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_copies[q]));
     if (mode == GP_PSD_TC_GUARDED)
         for (int64_t k = 0; k < nchunks % 62; ++k) unsure_total += (int64_t)h_counts[2 + k];
     rc = c->check_status("gp_psd_filter");

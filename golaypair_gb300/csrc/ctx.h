@@ -80,6 +80,9 @@ struct gp_ctx {
     int num_sms = 0;
     cudaStream_t s_comp = nullptr;
     cudaStream_t s_copy = nullptr;
+    static constexpr int kCopyStreams = 4;   // host->device copies of a chunk are split over these
+    cudaStream_t s_copies[kCopyStreams] = {};
+    cudaEvent_t ev_part[kCopyStreams] = {};
     cudaEvent_t ev_h2d[2] = {nullptr, nullptr};
     cudaEvent_t ev_done[2] = {nullptr, nullptr};
     std::string err;
