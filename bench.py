@@ -357,51 +357,56 @@ def run_gpu(args):
     return 0
 
 
-def _windows():
-    """Seed-chosen 2^32-word rank windows of the uneven-batch configuration
-    (orders 34, 50, 58, 68 at compression 2 and 90 at compression 5); a
-    space smaller than the window is enumerated whole."""
-    import numpy as np
-    out = []
-    for order, comp in [(34, 2), (50, 2), (58, 2), (68, 2), (90, 5)]:
-        L = order // comp
-        k = len(range(-comp, comp + 1, 2)) if comp % 2 == 0 else comp + 1
-        space = k ** L
-        if space <= 2 ** 32:
-            lo, hi = 0, space
-        else:
-            lo = int(np.random.default_rng(order * 1000 + comp).integers(0, space - 2 ** 32))
-            hi = lo + 2 ** 32
-        out.append((order, comp, 0, lo, hi))
-    return out
-
-
 def run_pipeline(args):
     """Times the search stages on the generation configurations (one JSON
-    line each): full generation of order 57 (paf -2, compression 3), its sort
-    and match, uncompression of its first pairs, and the 2^32-word windows."""
-    import ctypes
+    line each): the uneven batch (orders 34, 50, 58, 68 at compression 2 and
+    90 at compression 5, 2^32-word windows) in one engine run and one order
+    at a time, then full generation of order 57 (paf -2, compression 3), its
+    sort and match, and uncompression of its first pairs."""
     import tempfile
 
     import golaypair_gb300 as gp
+    from golaypair_gb300.workloads import batch_windows
     env = dict(os.environ, LC_ALL="C")
     with gp.Context(0) as ctx, tempfile.TemporaryDirectory() as tmp:
         def gen_window(order, comp, paf, lo, hi):
-            st = gp.GenStats()
             t0 = time.perf_counter()
-            ctx.check(ctx._lib.gp_generate_window(ctx.handle, order, comp, paf, lo >> 64, lo & (2**64 - 1), hi >> 64,
-                                                  hi & (2**64 - 1), os.path.join(tmp, "a").encode(),
-                                                  os.path.join(tmp, "b").encode(), ctypes.byref(st)),
-                      "gp_generate_window")
+            st = ctx.generate_window(order, comp, paf, lo, hi, os.path.join(tmp, "a"), os.path.join(tmp, "b"))
             return st, time.perf_counter() - t0
+
+        def stats_dict(st, el):
+            return {"seconds": el, "necklaces": st.necklaces, "candidates": st.candidates, "psd_pass": st.psd_pass,
+                    "written": st.written_a + st.written_b, "unsure": st.unsure,
+                    "necklaces_per_s": st.necklaces / el, "candidates_per_s": st.candidates / el}
+
         gen_window(16, 2, 0, 0, 3 ** 8)  # warm-up (module load, twiddles)
-        for order, comp, paf, lo, hi in _windows():
+        wins = batch_windows()
+        # the uneven batch in one engine run: tuner first (its result is
+        # cached in the context), then the timed run with the tuned settings
+        spec = [(o, c, p, lo, hi, os.path.join(tmp, f"{o}a"), os.path.join(tmp, f"{o}b"))
+                for (o, c, p, lo, hi) in wins]
+        t0 = time.perf_counter()
+        _, cfg = ctx.generate_batch(spec, autotune=True)
+        tune_el = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        stats, cfg = ctx.generate_batch(spec, autotune=True)
+        el = time.perf_counter() - t0
+        tot_n = sum(s.necklaces for s in stats)
+        tot_c = sum(s.candidates for s in stats)
+        print(json.dumps({"pipeline": "batch", "jobs": [list(w) for w in wins], "seconds": el,
+                          "necklaces_per_s": tot_n / el, "candidates_per_s": tot_c / el,
+                          "necklaces": tot_n, "candidates": tot_c, "iterations": cfg.iterations,
+                          "tuned": {k: getattr(cfg, k) for k in ("enum_variant", "windows_per_thread", "cand_cap",
+                                                                 "tc_ctas_per_sm")},
+                          "tune_run_seconds": tune_el, "tuner_seconds": cfg.tune_seconds,
+                          "per_job": [dict(order=w[0], compress=w[1], written=s.written_a + s.written_b,
+                                           necklaces=s.necklaces, candidates=s.candidates, psd_pass=s.psd_pass,
+                                           unsure=s.unsure) for w, s in zip(wins, stats)]}), flush=True)
+        # the same windows one order per call, for comparison
+        for order, comp, paf, lo, hi in wins:
             st, el = gen_window(order, comp, paf, lo, hi)
-            print(json.dumps({"pipeline": "window", "order": order, "compress": comp, "paf": paf,
-                              "rank_window": [lo, hi], "seconds": el, "necklaces": st.necklaces,
-                              "candidates": st.candidates, "psd_pass": st.psd_pass,
-                              "written": st.written_a + st.written_b, "unsure": st.unsure,
-                              "necklaces_per_s": st.necklaces / el, "candidates_per_s": st.candidates / el}))
+            print(json.dumps(dict({"pipeline": "window", "order": order, "compress": comp, "paf": paf,
+                                   "rank_window": [lo, hi]}, **stats_dict(st, el))), flush=True)
         cli = gp.CLI_PATH
         d = os.path.join(tmp, "r57")
         times = {}
@@ -426,6 +431,9 @@ def run_pipeline(args):
                  ("57-filtered-a#0", "57-filtered-b#0", "57-pairs-3")}
         print(json.dumps({"pipeline": "order57", "order": 57, "compress": [3, 1], "paf": -2,
                           "seconds": times, "lines": lines, "uncompressed_pairs_of_first": [len(head), found],
+                          "pairs_per_s_match": lines["57-pairs-3"] / times["match"],
+                          "candidates_written_per_s_gen": (lines["57-filtered-a#0"] + lines["57-filtered-b#0"])
+                          / times["gen"],
                           "note": "process wall times of the golay driver, including context creation"}))
     return 0
 

@@ -39,6 +39,22 @@ class GenStats(ctypes.Structure):
                 ("seconds", ctypes.c_double)]
 
 
+class GenJob(ctypes.Structure):
+    """One job of gp_generate_batch: a word-rank window of one order."""
+    _fields_ = [("order", ctypes.c_int), ("compress", ctypes.c_int), ("paf", ctypes.c_int),
+                ("begin_hi", ctypes.c_uint64), ("begin_lo", ctypes.c_uint64), ("end_hi", ctypes.c_uint64),
+                ("end_lo", ctypes.c_uint64), ("path_a", ctypes.c_char_p), ("path_b", ctypes.c_char_p)]
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("enum_variant", ctypes.c_int), ("windows_per_thread", ctypes.c_int), ("cand_cap", ctypes.c_int64),
+                ("tc_ctas_per_sm", ctypes.c_int), ("no_graph", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("tune_seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 def build():
     from . import native_build
     return native_build.build()
@@ -78,6 +94,7 @@ _P, _i32, _i64, _u64, _cp = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctype
 _STAGE_SIGS = {
     "gp_generate": [_P, _i32, _i32, _i32, _i32, _i32, _cp, _cp, _P],
     "gp_generate_window": [_P, _i32, _i32, _i32, _u64, _u64, _u64, _u64, _cp, _cp, _P],
+    "gp_generate_batch": [_P, _P, _i32, _i32, _P, _P],
     "gp_sort": [_P, _P, _i32, _cp],
     "gp_match": [_P, _i32, _i32, _i32, _cp, _cp, _cp, _i32, _P],
     "gp_uncompress": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp],
@@ -158,6 +175,33 @@ class Context:
         self.check(self._lib.gp_psd_filter(self._h, seqs_ptr, n, L, order, paf, mode, mask_ptr, ctypes.byref(st)),
                    "gp_psd_filter")
         return st
+
+    def generate_window(self, order, compress, paf, begin, end, path_a, path_b):
+        """gp_generate_window over word ranks [begin, end); returns GenStats."""
+        st = GenStats()
+        m = (1 << 64) - 1
+        self.check(self._lib.gp_generate_window(self._h, order, compress, paf, begin >> 64, begin & m, end >> 64,
+                                                end & m, str(path_a).encode(), str(path_b).encode(),
+                                                ctypes.byref(st)), "gp_generate_window")
+        return st
+
+    def generate_batch(self, jobs, autotune=False, config=None):
+        """gp_generate_batch.  jobs: (order, compress, paf, begin, end,
+        path_a, path_b) tuples.  Returns ([GenStats per job], BatchConfig)."""
+        n = len(jobs)
+        arr = (GenJob * n)()
+        keep = []
+        m = (1 << 64) - 1
+        for i, (order, comp, paf, lo, hi, pa, pb) in enumerate(jobs):
+            a, b = str(pa).encode(), str(pb).encode()
+            keep += [a, b]
+            arr[i] = GenJob(order, comp, paf, lo >> 64, lo & m, hi >> 64, hi & m, a, b)
+        cfg = config if config is not None else BatchConfig()
+        stats = (GenStats * n)()
+        self.check(self._lib.gp_generate_batch(self._h, ctypes.cast(arr, ctypes.c_void_p), n, 1 if autotune else 0,
+                                               ctypes.byref(cfg), ctypes.cast(stats, ctypes.c_void_p)),
+                   "gp_generate_batch")
+        return list(stats), cfg
 
     def kernel_timing(self, enable=True):
         self._lib.gp_kernel_timing(self._h, 1 if enable else 0)

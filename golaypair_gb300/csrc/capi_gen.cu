@@ -2,7 +2,7 @@
 // src/core/generate/generate_hybrid.cpp:107-163, and its job split,
 // src/utils/lyndon.cpp:87-121).
 //
-// Device pipeline per batch:
+// Device pipeline per iteration (the batch engine below):
 //   enumerate_kernel   rank windows -> row-sum-gated necklaces (packed words)
 //   psd_tc_kernel      guarded FP32 tensor-core PSD filter (+ FP64 recheck)
 //   mask_to_list       surviving rows
@@ -11,6 +11,7 @@
 // order) and writes the candidate files.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -83,181 +84,424 @@ int write_records(gp_ctx* c, const GenPlan& p, std::vector<Record>& recs, const 
     return ok ? GP_OK : c->fail(GP_ERR_IO, "write failed: %s", path);
 }
 
-// Runs the device pipeline over rank ranges [lo, hi) of the word space.
-int run_generation(gp_ctx* c, const GenPlan& p, const std::vector<std::pair<gp::u128, gp::u128>>& ranges,
-                   std::vector<Record>& rec_a, std::vector<Record>& rec_b, gp_gen_stats* st) {
-    const int L = p.L, b = p.b, k = p.k;
+// ------------------------------------------------------------ batch engine
+//
+// One engine serves gp_generate (one job) and gp_generate_batch (up to
+// kMaxEnumJobs jobs of different orders / compressions).  Per iteration:
+//
+//   memset   per-iteration counters
+//   enumerate_kernel          all jobs' rank windows, one launch
+//   per job, on its own stream branch:
+//     psd_tc_kernel           row count read on the device
+//     psd_recheck_kernel      FP64 recheck of the unsure rows
+//     mask_to_list_kernel     surviving rows
+//     finalize_kernel         FP64 PSD, canonical check, records (accumulate)
+//   copy     counters -> pinned host
+//
+// Nothing in that sequence depends on a host-side count, so it is captured
+// once as a CUDA graph and replayed until every window is finished.  The
+// host reads the counters after each replay, drains a job's records when
+// its record buffer could not take another iteration, and stops when no
+// window is left unfinished.
+
+constexpr int kIterSlots = 4;   // per job: [0] candidates, [1] unsure, [2] survivors
+constexpr int kCumSlots = 4;    // per job: [0] necklaces, [1] records, [2] psd passes
+constexpr int kIncomplete = kIterSlots * gp::kMaxEnumJobs;          // u64 slot of the flag
+constexpr int kIterWords = kIncomplete + 1;
+constexpr int kCumBase = 40;                                        // u64 offset of the cumulative block
+constexpr int kCounterWords = kCumBase + kCumSlots * gp::kMaxEnumJobs;
+
+struct BatchCfg {
+    int enum_variant = 0;        // enumerator kernel variant (see launch_enumerate)
+    int windows_per_thread = 1;  // rank windows per enumerator thread
+    int64_t cand_cap = int64_t(1) << 22;  // candidates per job per iteration (soft)
+    int tc_ctas_per_sm = 0;      // tensor-core filter CTAs per SM (0 = as many as fit)
+    int use_graph = 1;
+};
+
+struct JobRun {
+    GenPlan p;
+    std::vector<std::pair<gp::u128, gp::u128>> ranges;
+    int64_t soft = 0, hard = 0, rcap = 0, rec_bytes = 0;
+    size_t off_words = 0, off_roles = 0, off_mask = 0, off_unsure = 0, off_idx = 0, off_rec = 0, off_units = 0;
+    std::vector<int16_t> units;
+    std::vector<Record> ra, rb;
+    gp_gen_stats st{};
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+gp::u128 range_words(const JobRun& j) {
+    gp::u128 t = 0;
+    for (auto& r : j.ranges) t += r.second - r.first;
+    return t;
+}
+
+uint4 to_u4(gp::u128 w) {
+    return make_uint4((uint32_t)w, (uint32_t)(w >> 32), (uint32_t)(w >> 64), (uint32_t)(w >> 96));
+}
+
+// Copies job j's records to the host and appends them to its A/B lists.
+int drain_records(gp_ctx* c, JobRun& j, uint8_t* arena, int64_t nrec) {
+    if (nrec <= 0) return GP_OK;
+    const int L = j.p.L;
+    uint8_t* rb = arena + j.off_rec;
+    const int64_t rcap = j.rcap;
+    std::vector<uint4> w(nrec);
+    std::vector<uint8_t> ro(nrec);
+    std::vector<uint16_t> sg((size_t)nrec * (L - 1));
+    GP_CUDA_TRY(c, cudaMemcpy(w.data(), rb, nrec * 16, cudaMemcpyDeviceToHost));
+    GP_CUDA_TRY(c, cudaMemcpy(ro.data(), rb + (size_t)rcap * 16, nrec, cudaMemcpyDeviceToHost));
+    GP_CUDA_TRY(c, cudaMemcpy(sg.data(), rb + align_up((size_t)rcap * 17, 16), sg.size() * 2, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < nrec; ++i) {
+        Record r;
+        r.word = ((gp::u128)w[i].w << 96) | ((gp::u128)w[i].z << 64) | ((gp::u128)w[i].y << 32) | w[i].x;
+        r.sig.assign(sg.begin() + i * (L - 1), sg.begin() + (i + 1) * (L - 1));
+        (ro[i] == 1 ? j.ra : j.rb).push_back(std::move(r));
+    }
+    return GP_OK;
+}
+
+int64_t rec_region_bytes(int64_t rcap, int L) {
+    return (int64_t)align_up((size_t)rcap * 17, 16) + rcap * 2 * (int64_t)(L - 1);
+}
+
+// Runs the batch engine over the jobs' ranges; records land in the jobs'
+// A/B lists, counts in their stats.
+int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* iterations) {
+    const int nj = (int)jobs.size();
+    if (nj < 1 || nj > gp::kMaxEnumJobs) return c->fail(GP_ERR_ARG, "batch of %d jobs (1..%d)", nj, gp::kMaxEnumJobs);
     cudaStream_t s = c->s_comp;
-    // ---- windows
-    gp::u128 total = 0;
-    for (auto& r : ranges) total += r.second - r.first;
-    const int64_t target = (int64_t)c->num_sms * 256 * 8;
-    gp::u128 wsize = total / (gp::u128)target;
-    if (wsize < 1) wsize = 1;
-    const gp::u128 space = gp::upow(k, L);
-    const gp::u128 maxw = gp::rank_to_word(space - 1, k, b, L);
+    if (!c->ensure_job_streams()) return c->fail(GP_ERR_CUDA, "cannot create job streams");
+    // ---- rank windows, shared out over the jobs by words in range
+    const int64_t threads = (int64_t)c->num_sms * 8 * 256;
+    const int64_t target = threads * std::max(1, cfg.windows_per_thread);
+    double total_words = 0;
+    for (auto& j : jobs) total_words += (double)range_words(j);
     std::vector<uint4> cur, end;
-    auto to_u4 = [](gp::u128 w) {
-        return make_uint4((uint32_t)w, (uint32_t)(w >> 32), (uint32_t)(w >> 64), (uint32_t)(w >> 96));
-    };
-    for (auto& r : ranges) {
-        for (gp::u128 lo = r.first; lo < r.second; lo += wsize) {
-            gp::u128 hi = lo + wsize < r.second ? lo + wsize : r.second;
-            cur.push_back(to_u4(gp::rank_to_word(lo, k, b, L)));
-            end.push_back(to_u4(hi >= space ? maxw + 1 : gp::rank_to_word(hi, k, b, L)));
+    std::vector<uint8_t> wjob;
+    for (int ji = 0; ji < nj; ++ji) {
+        JobRun& j = jobs[ji];
+        const gp::u128 words = range_words(j);
+        if (words == 0) continue;
+        int64_t nw = (int64_t)((double)target * ((double)words / total_words));
+        if (nw < 256) nw = 256;
+        gp::u128 wsize = words / (gp::u128)nw;
+        if (wsize < 1) wsize = 1;
+        const gp::u128 space = gp::upow(j.p.k, j.p.L);
+        const gp::u128 maxw = gp::rank_to_word(space - 1, j.p.k, j.p.b, j.p.L);
+        for (auto& r : j.ranges) {
+            for (gp::u128 lo = r.first; lo < r.second; lo += wsize) {
+                const gp::u128 hi = lo + wsize < r.second ? lo + wsize : r.second;
+                cur.push_back(to_u4(gp::rank_to_word(lo, j.p.k, j.p.b, j.p.L)));
+                end.push_back(to_u4(hi >= space ? maxw + 1 : gp::rank_to_word(hi, j.p.k, j.p.b, j.p.L)));
+                wjob.push_back((uint8_t)ji);
+            }
         }
     }
     const int64_t nwin = (int64_t)cur.size();
-    // ---- roles by digit sum: rowsum = -c L + 2 * digitsum
-    std::vector<uint8_t> roles(gp::kMaxDigitSum + 1, 0);
-    for (int ds = 0; ds <= L * (k - 1) && ds <= gp::kMaxDigitSum; ++ds) {
-        const int rs = -p.compress * L + 2 * ds;
-        for (auto& d : p.dec) {
-            if (rs == d.first) roles[ds] |= 1;
-            if (rs == d.second) roles[ds] |= 2;
+    // ---- capacities and the device arena
+    const int64_t slack = threads * 8 + 4096;  // appends after a job met its soft cap
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes, 256);
+        return o;
+    };
+    const size_t off_ctr = take(kCounterWords * 8);
+    const size_t off_ejobs = take(sizeof(gp::EnumJob) * nj);
+    const size_t off_rtab = take((size_t)nj * (gp::kMaxDigitSum + 1));
+    const size_t off_cur = take((size_t)nwin * 16);
+    const size_t off_end = take((size_t)nwin * 16);
+    const size_t off_wjob = take((size_t)nwin);
+    for (auto& j : jobs) {
+        const gp::u128 words = range_words(j);
+        if (words < (gp::u128)cfg.cand_cap) {
+            j.soft = (int64_t)words + 1;  // never met: the job cannot park
+            j.hard = j.soft;
+        } else {
+            j.soft = cfg.cand_cap;
+            j.hard = cfg.cand_cap + slack;
         }
+        // one iteration adds at most 2 records per candidate (x == y: A and B)
+        j.rcap = 2 * j.hard + std::max<int64_t>(j.hard / 2, 4096);
+        j.units.clear();
+        for (int u = 1; u < j.p.L; ++u)
+            if (std::gcd(u, j.p.L) == 1) j.units.push_back((int16_t)u);
+        if (j.units.empty()) j.units.push_back(1);
+        j.off_words = take((size_t)j.hard * 16);
+        j.off_roles = take((size_t)j.hard);
+        j.off_mask = take((size_t)(j.hard + 31) / 32 * 4);
+        j.off_unsure = take((size_t)j.hard * 4);
+        j.off_idx = take((size_t)j.hard * 4);
+        j.off_rec = take((size_t)rec_region_bytes(j.rcap, j.p.L));
+        j.off_units = take(j.units.size() * 2);
     }
-    // ---- device buffers
-    const int64_t cap = std::min<int64_t>(int64_t(1) << 25, std::max<int64_t>(1 << 16, (int64_t)std::min<gp::u128>(total, (gp::u128)1 << 40)));
-    const int64_t slack = (int64_t)c->num_sms * 8 * 256 / 32 * 256 + 4096;
-    const int64_t hard = cap + slack;
-    DevBuf& d_cur = c->scratch[5];
-    DevBuf& d_end = c->scratch[6];
-    DevBuf& d_words = c->scratch[7];
-    DevBuf& d_roles = c->scratch[8];
-    DevBuf& d_mask = c->scratch[9];
-    DevBuf& d_unsure = c->scratch[10];
-    DevBuf& d_idx = c->scratch[11];
-    DevBuf& d_rtab = c->scratch[12];
-    DevBuf& d_misc = c->scratch[13];  // counters
-    DevBuf& d_rec = c->scratch[14];
-    DevBuf& d_units = c->scratch[15];
-    if (!d_cur.ensure(nwin * 16) || !d_end.ensure(nwin * 16) || !d_words.ensure(hard * 16) || !d_roles.ensure(hard) ||
-        !d_mask.ensure((hard + 31) / 32 * 4) || !d_unsure.ensure(hard * 4) || !d_idx.ensure(hard * 4) ||
-        !d_rtab.ensure(roles.size()) || !d_misc.ensure(64 * 8) || !d_units.ensure(2 * (L + 1)))
-        return c->fail(GP_ERR_NOMEM, "generate: device allocation failed");
-    GP_CUDA_TRY(c, cudaMemcpyAsync(d_cur.p, cur.data(), nwin * 16, cudaMemcpyHostToDevice, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(d_end.p, end.data(), nwin * 16, cudaMemcpyHostToDevice, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(d_rtab.p, roles.data(), roles.size(), cudaMemcpyHostToDevice, s));
-    std::vector<int16_t> units;
-    for (int u = 1; u < L; ++u)
-        if (std::gcd(u, L) == 1) units.push_back((int16_t)u);
-    if (units.empty()) units.push_back(1);
-    GP_CUDA_TRY(c, cudaMemcpyAsync(d_units.p, units.data(), units.size() * 2, cudaMemcpyHostToDevice, s));
-    unsigned long long* misc = d_misc.as<unsigned long long>();
-    // misc: [0] candidates, [1] necklaces, [2] incomplete(int), [3] unsure count,
-    //       [4] survivors, [5] records, [6] psd passes
-    gp::EnumArgs ea;
-    ea.L = L;
-    ea.b = b;
-    gp::u128 mp = 0;
-    for (int j = 0; j < L; ++j) mp |= (gp::u128)(k - 1) << (b * j);
-    ea.maxpat.lo = (uint64_t)mp;
-    ea.maxpat.hi = (uint64_t)(mp >> 64);
-    for (int t = 0; t < 4; ++t) {
-        gp::u128 pl = 0;
-        if (t < b)
-            for (int j = 0; j < L; ++j) pl |= (gp::u128)1 << (b * j + t);
-        ea.plane[t].lo = (uint64_t)pl;
-        ea.plane[t].hi = (uint64_t)(pl >> 64);
-    }
-    ea.roles = d_rtab.as<uint8_t>();
-    ea.cur = d_cur.as<uint4>();
-    ea.end = d_end.as<uint4>();
-    ea.nwin = nwin;
-    ea.words = d_words.as<uint4>();
-    ea.out_roles = d_roles.as<uint8_t>();
-    ea.count = misc + 0;
-    ea.cap = hard;
-    ea.soft_cap = cap;
-    ea.necklaces = misc + 1;
-    ea.incomplete = reinterpret_cast<int*>(misc + 2);
-    ea.status = c->status.as<int>();
-
-    gp::RowSrc src{nullptr, d_words.as<uint4>(), L, b, p.compress};
-    GP_CUDA_TRY(c, cudaMemsetAsync(misc, 0, 64 * 8, s));
-    for (int iter = 0;; ++iter) {
-        GP_CUDA_TRY(c, cudaMemsetAsync(misc + 0, 0, 8, s));
-        GP_CUDA_TRY(c, cudaMemsetAsync(misc + 2, 0, 8, s));
-        GP_CUDA_TRY(c, cudaMemsetAsync(misc + 4, 0, 8, s));
-        GP_CUDA_TRY(c, cudaMemsetAsync(misc + 5, 0, 8, s));
-        GP_CUDA_TRY(c, gp::launch_enumerate(ea, c->num_sms, s));
-        unsigned long long h[8];
-        GP_CUDA_TRY(c, cudaMemcpyAsync(h, misc, sizeof h, cudaMemcpyDeviceToHost, s));
-        GP_CUDA_TRY(c, cudaStreamSynchronize(s));
-        int rc = c->check_status("enumerate");
-        if (rc) return rc;
-        const int64_t n = (int64_t)h[0];
-        const bool incomplete = h[2] != 0;
-        if (n > 0) {
-            st->candidates += n;
-            rc = c->enqueue_filter(src, n, p.order, p.paf, GP_PSD_TC_GUARDED, d_mask.as<uint32_t>(),
-                                   d_unsure.as<uint32_t>(), misc + 3, s);
-            if (rc) return rc;
-            GP_CUDA_TRY(c, gp::launch_mask_to_list(d_mask.as<uint32_t>(), n, d_idx.as<uint32_t>(), misc + 4, hard,
-                                                   c->status.as<int>(), c->num_sms, s));
-            unsigned long long hs[2];
-            GP_CUDA_TRY(c, cudaMemcpyAsync(hs, misc + 3, 16, cudaMemcpyDeviceToHost, s));
-            GP_CUDA_TRY(c, cudaStreamSynchronize(s));
-            rc = c->check_status("psd filter");
-            if (rc) return rc;
-            st->unsure += (int64_t)hs[0];
-            const int64_t surv = (int64_t)hs[1];
-            if (surv > 0) {
-                const int64_t rcap = 2 * surv;
-                const size_t rec_bytes = (size_t)rcap * (16 + 1 + 2 * (L - 1)) + 64;
-                if (!d_rec.ensure(rec_bytes)) return c->fail(GP_ERR_NOMEM, "generate: record buffer");
-                uint8_t* rb = d_rec.as<uint8_t>();
-                gp::FinalizeArgs fa;
-                fa.src = src;
-                fa.roles = d_roles.as<uint8_t>();
-                fa.fixed_role = 0;
-                fa.idx = d_idx.as<uint32_t>();
-                fa.n_idx = misc + 4;
-                fa.idx_cap = hard;
-                fa.tw = c->twiddle64(L);
-                fa.thr = 2.0 * p.order - p.paf + 0.001;
-                fa.bound = 2 * p.order - p.paf;
-                fa.invert_roles = 2;  // B lines carry bound - rint(psd) (io.cpp:26-36)
-                fa.check_canonical = 1;
-                fa.units = d_units.as<int16_t>();
-                fa.n_units = (int)units.size();
-                fa.rec_words = reinterpret_cast<uint4*>(rb);
-                fa.rec_role = rb + (size_t)rcap * 16;
-                fa.rec_sig = reinterpret_cast<uint16_t*>(rb + (size_t)rcap * 17 + ((rcap * 17) & 1));
-                fa.rec_src = nullptr;
-                fa.rec_count = misc + 5;
-                fa.rec_cap = rcap;
-                fa.psd_pass = misc + 6;
-                fa.status = c->status.as<int>();
-                GP_CUDA_TRY(c, gp::launch_finalize(fa, surv, c->num_sms, s));
-                unsigned long long nrec = 0;
-                GP_CUDA_TRY(c, cudaMemcpyAsync(&nrec, misc + 5, 8, cudaMemcpyDeviceToHost, s));
-                GP_CUDA_TRY(c, cudaStreamSynchronize(s));
-                rc = c->check_status("finalize");
-                if (rc) return rc;
-                if (nrec) {
-                    std::vector<uint4> w(nrec);
-                    std::vector<uint8_t> ro(nrec);
-                    std::vector<uint16_t> sg(nrec * (L - 1));
-                    GP_CUDA_TRY(c, cudaMemcpy(w.data(), fa.rec_words, nrec * 16, cudaMemcpyDeviceToHost));
-                    GP_CUDA_TRY(c, cudaMemcpy(ro.data(), fa.rec_role, nrec, cudaMemcpyDeviceToHost));
-                    GP_CUDA_TRY(c, cudaMemcpy(sg.data(), fa.rec_sig, sg.size() * 2, cudaMemcpyDeviceToHost));
-                    for (size_t i = 0; i < nrec; ++i) {
-                        Record r;
-                        r.word = ((gp::u128)w[i].w << 96) | ((gp::u128)w[i].z << 64) | ((gp::u128)w[i].y << 32) | w[i].x;
-                        r.sig.assign(sg.begin() + i * (L - 1), sg.begin() + (i + 1) * (L - 1));
-                        (ro[i] == 1 ? rec_a : rec_b).push_back(std::move(r));
-                    }
-                }
+    DevBuf& arena = c->scratch[7];
+    HostPinned& hbuf = c->hscratch[3];
+    if (!arena.ensure(off) || !hbuf.ensure(kCounterWords * 8))
+        return c->fail(GP_ERR_NOMEM, "batch generation: cannot allocate %zu bytes of device memory", off);
+    uint8_t* A = arena.as<uint8_t>();
+    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(A + off_ctr);
+    unsigned long long* hctr = hbuf.as<unsigned long long>();
+    // ---- job tables
+    std::vector<gp::EnumJob> ej(nj);
+    std::vector<uint8_t> rtab((size_t)nj * (gp::kMaxDigitSum + 1), 0);
+    for (int ji = 0; ji < nj; ++ji) {
+        JobRun& j = jobs[ji];
+        const GenPlan& p = j.p;
+        gp::EnumJob& e = ej[ji];
+        e.L = p.L;
+        e.b = p.b;
+        gp::u128 mp = 0;
+        for (int q = 0; q < p.L; ++q) mp |= (gp::u128)(p.k - 1) << (p.b * q);
+        e.maxpat = {(uint64_t)mp, (uint64_t)(mp >> 64)};
+        for (int t = 0; t < 4; ++t) {
+            gp::u128 pl = 0;
+            if (t < p.b)
+                for (int q = 0; q < p.L; ++q) pl |= (gp::u128)1 << (p.b * q + t);
+            e.plane[t] = {(uint64_t)pl, (uint64_t)(pl >> 64)};
+        }
+        e.words = reinterpret_cast<uint4*>(A + j.off_words);
+        e.out_roles = A + j.off_roles;
+        e.count = ctr + ji * kIterSlots + 0;
+        e.cap = j.hard;
+        e.soft_cap = j.soft;
+        e.necklaces = ctr + kCumBase + ji * kCumSlots + 0;
+        // roles by digit sum: row sum = -c L + 2 * digit sum
+        for (int ds = 0; ds <= p.L * (p.k - 1) && ds <= gp::kMaxDigitSum; ++ds) {
+            const int rs = -p.compress * p.L + 2 * ds;
+            uint8_t& r = rtab[(size_t)ji * (gp::kMaxDigitSum + 1) + ds];
+            for (auto& d : p.dec) {
+                if (rs == d.first) r |= 1;
+                if (rs == d.second) r |= 2;
             }
         }
-        if (!incomplete) break;
+        if (!c->twiddle_image(p.L) || !c->twiddle64(p.L))
+            return c->fail(GP_ERR_NOMEM, "batch generation: twiddle tables for length %d", p.L);
+        GP_CUDA_TRY(c, cudaMemcpyAsync(A + j.off_units, j.units.data(), j.units.size() * 2, cudaMemcpyHostToDevice, s));
     }
-    unsigned long long h2[8];
-    GP_CUDA_TRY(c, cudaMemcpy(h2, misc, sizeof h2, cudaMemcpyDeviceToHost));
-    st->necklaces += (int64_t)h2[1];
-    st->psd_pass += (int64_t)h2[6];
+    GP_CUDA_TRY(c, cudaMemcpyAsync(A + off_ejobs, ej.data(), sizeof(gp::EnumJob) * nj, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(A + off_rtab, rtab.data(), rtab.size(), cudaMemcpyHostToDevice, s));
+    if (nwin) {
+        GP_CUDA_TRY(c, cudaMemcpyAsync(A + off_cur, cur.data(), (size_t)nwin * 16, cudaMemcpyHostToDevice, s));
+        GP_CUDA_TRY(c, cudaMemcpyAsync(A + off_end, end.data(), (size_t)nwin * 16, cudaMemcpyHostToDevice, s));
+        GP_CUDA_TRY(c, cudaMemcpyAsync(A + off_wjob, wjob.data(), (size_t)nwin, cudaMemcpyHostToDevice, s));
+    }
+    GP_CUDA_TRY(c, cudaMemsetAsync(ctr, 0, kCounterWords * 8, s));
+    gp::EnumArgs ea;
+    ea.jobs = reinterpret_cast<const gp::EnumJob*>(A + off_ejobs);
+    ea.njobs = nj;
+    ea.roles = A + off_rtab;
+    ea.cur = reinterpret_cast<uint4*>(A + off_cur);
+    ea.end = reinterpret_cast<const uint4*>(A + off_end);
+    ea.win_job = A + off_wjob;
+    ea.nwin = nwin;
+    ea.incomplete = reinterpret_cast<int*>(ctr + kIncomplete);
+    ea.status = c->status.as<int>();
+
+    // ---- one iteration of the pipeline on stream s (branches per job)
+    auto enqueue_iteration = [&]() -> int {
+        GP_CUDA_TRY(c, cudaMemsetAsync(ctr, 0, kIterWords * 8, s));
+        GP_CUDA_TRY(c, gp::launch_enumerate(ea, c->num_sms, s, cfg.enum_variant));
+        GP_CUDA_TRY(c, cudaEventRecord(c->ev_fork, s));
+        for (int ji = 0; ji < nj; ++ji) {
+            JobRun& j = jobs[ji];
+            const GenPlan& p = j.p;
+            cudaStream_t sj = c->s_jobs[ji];
+            GP_CUDA_TRY(c, cudaStreamWaitEvent(sj, c->ev_fork, 0));
+            unsigned long long* it = ctr + ji * kIterSlots;
+            const gp::RowSrc src{nullptr, reinterpret_cast<const uint4*>(A + j.off_words), p.L, p.b, p.compress};
+            uint32_t* mask = reinterpret_cast<uint32_t*>(A + j.off_mask);
+            uint32_t* idx = reinterpret_cast<uint32_t*>(A + j.off_idx);
+            int rc = c->enqueue_filter_dev(src, j.hard, it + 0, p.order, p.paf, mask,
+                                           reinterpret_cast<uint32_t*>(A + j.off_unsure), it + 1, cfg.tc_ctas_per_sm, sj);
+            if (rc) return rc;
+            GP_CUDA_TRY(c, gp::launch_mask_to_list(mask, j.hard, idx, it + 2, j.hard, c->status.as<int>(), c->num_sms,
+                                                   sj, it + 0));
+            uint8_t* rb = A + j.off_rec;
+            gp::FinalizeArgs fa;
+            fa.src = src;
+            fa.roles = A + j.off_roles;
+            fa.fixed_role = 0;
+            fa.idx = idx;
+            fa.n_idx = it + 2;
+            fa.idx_cap = j.hard;
+            fa.tw = c->twiddle64(p.L);
+            fa.thr = 2.0 * p.order - p.paf + 0.001;
+            fa.bound = 2 * p.order - p.paf;
+            fa.invert_roles = 2;  // B lines carry bound - rint(psd) (io.cpp:26-36)
+            fa.check_canonical = 1;
+            fa.units = reinterpret_cast<const int16_t*>(A + j.off_units);
+            fa.n_units = (int)j.units.size();
+            fa.rec_words = reinterpret_cast<uint4*>(rb);
+            fa.rec_role = rb + (size_t)j.rcap * 16;
+            fa.rec_sig = reinterpret_cast<uint16_t*>(rb + align_up((size_t)j.rcap * 17, 16));
+            fa.rec_src = nullptr;
+            fa.rec_count = ctr + kCumBase + ji * kCumSlots + 1;
+            fa.rec_cap = j.rcap;
+            fa.psd_pass = ctr + kCumBase + ji * kCumSlots + 2;
+            fa.status = c->status.as<int>();
+            GP_CUDA_TRY(c, gp::launch_finalize(fa, j.hard, c->num_sms, sj));
+            GP_CUDA_TRY(c, cudaEventRecord(c->ev_join[ji], sj));
+            GP_CUDA_TRY(c, cudaStreamWaitEvent(s, c->ev_join[ji], 0));
+        }
+        GP_CUDA_TRY(c, cudaMemcpyAsync(hctr, ctr, kCounterWords * 8, cudaMemcpyDeviceToHost, s));
+        return GP_OK;
+    };
+    // ---- capture it once
+    cudaGraphExec_t exec = nullptr;
+    if (cfg.use_graph) {
+        GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+        GP_CUDA_TRY(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+        const int rc = enqueue_iteration();
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return rc;
+        }
+        if (e != cudaSuccess) return c->cuda_fail(e, "batch generation: graph capture");
+        const cudaError_t e2 = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) return c->cuda_fail(e2, "batch generation: graph instantiation");
+    }
+    struct ExecGuard {
+        cudaGraphExec_t& x;
+        ~ExecGuard() {
+            if (x) cudaGraphExecDestroy(x);
+        }
+    } guard{exec};
+    // ---- iterate until no window is left unfinished
+    int iters = 0;
+    int stalled = 0;
+    for (;;) {
+        if (exec) {
+            GP_CUDA_TRY(c, cudaGraphLaunch(exec, s));
+        } else {
+            const int rc = enqueue_iteration();
+            if (rc) return rc;
+        }
+        GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+        int rc = c->check_status("batch generation");
+        if (rc) return rc;
+        ++iters;
+        int64_t added = 0;
+        for (int ji = 0; ji < nj; ++ji) {
+            JobRun& j = jobs[ji];
+            const int64_t cand = (int64_t)hctr[ji * kIterSlots + 0];
+            added += cand;
+            j.st.candidates += cand;
+            j.st.unsure += (int64_t)hctr[ji * kIterSlots + 1];
+            const int64_t nrec = (int64_t)hctr[kCumBase + ji * kCumSlots + 1];
+            if (nrec > j.rcap - 2 * j.hard) {
+                rc = drain_records(c, j, A, nrec);
+                if (rc) return rc;
+                GP_CUDA_TRY(c, cudaMemsetAsync(ctr + kCumBase + ji * kCumSlots + 1, 0, 8, s));
+                hctr[kCumBase + ji * kCumSlots + 1] = 0;
+            }
+        }
+        if (!hctr[kIncomplete]) break;
+        // a window is left only when its job met its soft cap, so every
+        // unfinished iteration appends candidates
+        stalled = added ? 0 : stalled + 1;
+        if (stalled > 2) return c->fail(GP_ERR_CUDA, "batch generation: no progress");
+    }
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    for (int ji = 0; ji < nj; ++ji) {
+        JobRun& j = jobs[ji];
+        const int rc = drain_records(c, j, A, (int64_t)hctr[kCumBase + ji * kCumSlots + 1]);
+        if (rc) return rc;
+        j.st.necklaces += (int64_t)hctr[kCumBase + ji * kCumSlots + 0];
+        j.st.psd_pass += (int64_t)hctr[kCumBase + ji * kCumSlots + 2];
+    }
+    if (iterations) *iterations = iters;
+    return GP_OK;
+}
+
+// One order per call (gp_generate, gp_generate_window): larger iterations.
+BatchCfg single_job_cfg() {
+    BatchCfg b;
+    b.cand_cap = int64_t(1) << 24;
+    return b;
+}
+
+std::string batch_key(const std::vector<JobRun>& jobs) {
+    std::string k;
+    for (auto& j : jobs) {
+        const double w = (double)range_words(j);
+        char buf[96];
+        snprintf(buf, sizeof buf, "%d/%d/%d/%d;", j.p.order, j.p.compress, j.p.paf, w > 0 ? (int)std::log2(w) : -1);
+        k += buf;
+    }
+    return k;
+}
+
+// The tuner: times a few settings of the engine on a sample of every job
+// (the first 1/32 of its words, at least 2^24 or all of them) and keeps the
+// fastest.  Results are cached in the context by the batch's shape.
+int tune_batch(gp_ctx* c, const std::vector<JobRun>& jobs, BatchCfg& best, double* seconds) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const std::string key = "batch:" + batch_key(jobs);
+    auto hit = c->tuned.find(key);
+    if (hit != c->tuned.end() && hit->second.size() == 5) {
+        const auto& v = hit->second;
+        best.enum_variant = (int)v[0];
+        best.windows_per_thread = (int)v[1];
+        best.cand_cap = v[2];
+        best.tc_ctas_per_sm = (int)v[3];
+        best.use_graph = (int)v[4];
+        *seconds = 0;
+        return GP_OK;
+    }
+    std::vector<JobRun> sample;
+    for (auto& j : jobs) {
+        JobRun s;
+        s.p = j.p;
+        const gp::u128 words = range_words(j);
+        gp::u128 want = words / 32;
+        if (want < ((gp::u128)1 << 24)) want = words < ((gp::u128)1 << 24) ? words : ((gp::u128)1 << 24);
+        for (auto& r : j.ranges) {
+            if (want == 0) break;
+            const gp::u128 n = r.second - r.first;
+            const gp::u128 t = n < want ? n : want;
+            s.ranges.emplace_back(r.first, r.first + t);
+            want -= t;
+        }
+        sample.push_back(std::move(s));
+    }
+    std::vector<BatchCfg> cands;
+    BatchCfg base;
+    cands.push_back(base);
+    BatchCfg v1 = base;
+    v1.enum_variant = 1;
+    cands.push_back(v1);
+    BatchCfg w4 = base;
+    w4.windows_per_thread = 4;
+    cands.push_back(w4);
+    BatchCfg big = base;
+    big.cand_cap = int64_t(1) << 24;
+    cands.push_back(big);
+    BatchCfg one = base;
+    one.tc_ctas_per_sm = 1;
+    cands.push_back(one);
+    double best_t = 1e300;
+    for (size_t ci = 0; ci <= cands.size(); ++ci) {
+        // candidate 0 runs twice; its first run (module loading) is not scored
+        const BatchCfg& cfg = cands[ci == 0 ? 0 : ci - 1];
+        std::vector<JobRun> run = sample;
+        const auto a = std::chrono::steady_clock::now();
+        const int rc = run_batch(c, run, cfg, nullptr);
+        if (rc) return rc;
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+        if (ci > 0 && el < best_t) {
+            best_t = el;
+            best = cfg;
+        }
+    }
+    c->tuned[key] = {best.enum_variant, best.windows_per_thread, best.cand_cap, best.tc_ctas_per_sm, best.use_graph};
+    *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return GP_OK;
 }
 
@@ -336,10 +580,13 @@ int gp_generate(gp_ctx* c, int order, int compress, int paf, int proc_id, int pr
     } else {
         ranges.emplace_back(0, gp::upow(k, L));
     }
-    std::vector<Record> ra, rb;
-    rc = run_generation(c, p, ranges, ra, rb, &st);
+    std::vector<JobRun> jobs(1);
+    jobs[0].p = p;
+    jobs[0].ranges = std::move(ranges);
+    rc = run_batch(c, jobs, single_job_cfg(), nullptr);
     if (rc) return rc;
-    rc = finish(c, p, ra, rb, path_a, path_b, &st);
+    st = jobs[0].st;
+    rc = finish(c, p, jobs[0].ra, jobs[0].rb, path_a, path_b, &st);
     if (rc) return rc;
     st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = st;
@@ -362,12 +609,13 @@ int gp_generate_window(gp_ctx* c, int order, int compress, int paf, uint64_t beg
     gp::u128 hi = ((gp::u128)end_hi << 64) | end_lo;
     const gp::u128 space = gp::upow(p.k, p.L);
     if (hi > space) hi = space;
-    std::vector<std::pair<gp::u128, gp::u128>> ranges;
-    if (lo < hi) ranges.emplace_back(lo, hi);
-    std::vector<Record> ra, rb;
-    rc = run_generation(c, p, ranges, ra, rb, &st);
+    std::vector<JobRun> jobs(1);
+    jobs[0].p = p;
+    if (lo < hi) jobs[0].ranges.emplace_back(lo, hi);
+    rc = run_batch(c, jobs, single_job_cfg(), nullptr);
     if (rc) return rc;
-    rc = finish(c, p, ra, rb, path_a, path_b, &st);
+    st = jobs[0].st;
+    rc = finish(c, p, jobs[0].ra, jobs[0].rb, path_a, path_b, &st);
     if (rc) return rc;
     st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = st;
@@ -375,3 +623,61 @@ int gp_generate_window(gp_ctx* c, int order, int compress, int paf, uint64_t beg
 }
 
 }  // extern "C"
+
+extern "C" int gp_generate_batch(gp_ctx* c, const gp_gen_job* jobs, int njobs, int autotune, gp_batch_config* cfg,
+                                 gp_gen_stats* stats) {
+    if (!c || !jobs) return GP_ERR_ARG;
+    if (njobs < 1 || njobs > gp::kMaxEnumJobs)
+        return c->fail(GP_ERR_ARG, "batch of %d jobs (1..%d)", njobs, gp::kMaxEnumJobs);
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaSetDevice(c->device);
+    std::vector<JobRun> run(njobs);
+    for (int i = 0; i < njobs; ++i) {
+        const gp_gen_job& q = jobs[i];
+        if (!q.path_a || !q.path_b) return c->fail(GP_ERR_ARG, "job %d: missing output path", i);
+        int rc = plan_for(c, q.order, q.compress, q.paf, run[i].p);
+        if (rc) return rc;
+        if (run[i].p.dec.empty())
+            return c->fail(GP_NO_DECOMPOSITION, "job %d: order %d cannot be decomposed", i, q.order);
+        gp::u128 lo = ((gp::u128)q.begin_hi << 64) | q.begin_lo;
+        gp::u128 hi = ((gp::u128)q.end_hi << 64) | q.end_lo;
+        const gp::u128 space = gp::upow(run[i].p.k, run[i].p.L);
+        if (hi > space) hi = space;
+        if (lo < hi) run[i].ranges.emplace_back(lo, hi);
+    }
+    BatchCfg bc;
+    double tune_s = 0;
+    if (autotune) {
+        int rc = tune_batch(c, run, bc, &tune_s);
+        if (rc) return rc;
+    } else if (cfg) {
+        if (cfg->enum_variant == 1) bc.enum_variant = 1;
+        if (cfg->windows_per_thread > 0) bc.windows_per_thread = cfg->windows_per_thread;
+        if (cfg->cand_cap > 0) bc.cand_cap = cfg->cand_cap;
+        if (cfg->tc_ctas_per_sm > 0) bc.tc_ctas_per_sm = cfg->tc_ctas_per_sm;
+        bc.use_graph = cfg->no_graph ? 0 : 1;
+    }
+    int iters = 0;
+    int rc = run_batch(c, run, bc, &iters);
+    if (rc) return rc;
+    for (int i = 0; i < njobs; ++i) {
+        rc = finish(c, run[i].p, run[i].ra, run[i].rb, jobs[i].path_a, jobs[i].path_b, &run[i].st);
+        if (rc) return rc;
+    }
+    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats)
+        for (int i = 0; i < njobs; ++i) {
+            stats[i] = run[i].st;
+            stats[i].seconds = el;
+        }
+    if (cfg) {
+        cfg->enum_variant = bc.enum_variant;
+        cfg->windows_per_thread = bc.windows_per_thread;
+        cfg->cand_cap = bc.cand_cap;
+        cfg->tc_ctas_per_sm = bc.tc_ctas_per_sm;
+        cfg->no_graph = bc.use_graph ? 0 : 1;
+        cfg->iterations = iters;
+        cfg->tune_seconds = tune_s;
+    }
+    return GP_OK;
+}

@@ -88,6 +88,50 @@ int gp_ctx::enqueue_filter(const gp::RowSrc& src, int64_t n, int order, int paf,
     return GP_OK;
 }
 
+int gp_ctx::enqueue_filter_dev(const gp::RowSrc& src, int64_t cap, const unsigned long long* n_dev, int order,
+                               int paf, uint32_t* d_mask, uint32_t* d_unsure, unsigned long long* d_ucount,
+                               int grid_per_sm, cudaStream_t st) {
+    const int L = src.L;
+    const double* tw = twiddle64(L);
+    const void* img = twiddle_image(L);
+    if (!tw || !img) return fail(GP_ERR_UNSUPPORTED, "tensor-core filter: unsupported length %d", L);
+    if (src.words && !gp::tc_packed_supported(L, src.pack_bits))
+        return fail(GP_ERR_UNSUPPORTED, "tensor-core filter: packed length %d x %d bits", L, src.pack_bits);
+    gp::PsdTcArgs a;
+    a.seqs = src.seqs;
+    a.words = src.words;
+    a.pack_bits = src.pack_bits;
+    a.alpha_c = src.alpha_c;
+    a.n = cap;
+    a.n_dev = n_dev;
+    a.grid_per_sm = grid_per_sm;
+    a.L = L;
+    a.bimage = img;
+    a.thr = (float)threshold(order, paf);
+    a.guard_cfg = guard_band(order);
+    a.err_coef = gp::tc_err_coef(gp::tc_k_for_len(L));
+    a.mask = d_mask;
+    a.mask_words = (cap + 31) / 32;
+    a.unsure = d_unsure;
+    a.unsure_count = d_ucount;
+    a.unsure_cap = cap;
+    a.psd_out = nullptr;
+    a.status = status.as<int>();
+    a.trace = nullptr;
+    GP_CUDA_TRY(this, gp::launch_psd_tc(a, num_sms, st));
+    GP_CUDA_TRY(this, gp::launch_psd_recheck(src, tw, threshold(order, paf), d_unsure, d_ucount, cap, d_mask, num_sms, st));
+    return GP_OK;
+}
+
+bool gp_ctx::ensure_job_streams() {
+    if (ev_fork) return true;
+    for (int i = 0; i < kJobStreams; ++i) {
+        if (cudaStreamCreateWithFlags(&s_jobs[i], cudaStreamNonBlocking) != cudaSuccess) return false;
+        if (cudaEventCreateWithFlags(&ev_join[i], cudaEventDisableTiming) != cudaSuccess) return false;
+    }
+    return cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) == cudaSuccess;
+}
+
 int gp_ctx::check_status(const char* what) {
     int st = 0;
     cudaError_t e = cudaMemcpy(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost);
@@ -174,6 +218,11 @@ int gp_ctx_destroy(gp_ctx* c) {
         if (c->s_copies[i]) cudaStreamDestroy(c->s_copies[i]);
         if (c->ev_part[i]) cudaEventDestroy(c->ev_part[i]);
     }
+    for (int i = 0; i < gp_ctx::kJobStreams; ++i) {
+        if (c->s_jobs[i]) cudaStreamDestroy(c->s_jobs[i]);
+        if (c->ev_join[i]) cudaEventDestroy(c->ev_join[i]);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     delete c;
     return GP_OK;
 }

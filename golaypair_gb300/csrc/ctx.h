@@ -116,6 +116,14 @@ struct gp_ctx {
     // generic scratch arenas used by the stage pipelines
     DevBuf scratch[16];
     HostPinned hscratch[4];
+    // batched generation: one stream per job branch, fork/join events
+    static constexpr int kJobStreams = 8;
+    cudaStream_t s_jobs[kJobStreams] = {};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kJobStreams] = {};
+    bool ensure_job_streams();
+    // tuned settings of batched generation and of the sort, by workload key
+    std::map<std::string, std::vector<int64_t>> tuned;
 
     int fail(int code, const char* fmt, ...) {
         char buf[1024];
@@ -137,6 +145,12 @@ struct gp_ctx {
     // on st: mask bit = pass; TC mode rechecks its unsure rows in FP64.
     int enqueue_filter(const gp::RowSrc& src, int64_t n, int order, int paf, int mode, uint32_t* d_mask,
                        uint32_t* d_unsure, unsigned long long* d_ucount, cudaStream_t st);
+    // TC-mode filter of a device batch whose row count is read on the device
+    // (*n_dev, at most cap rows): nothing here depends on the count, so the
+    // sequence can be captured in a CUDA graph.  *d_ucount must be zero.
+    int enqueue_filter_dev(const gp::RowSrc& src, int64_t cap, const unsigned long long* n_dev, int order, int paf,
+                           uint32_t* d_mask, uint32_t* d_unsure, unsigned long long* d_ucount, int grid_per_sm,
+                           cudaStream_t st);
     // reads the kernel status word; resets it; returns a GP code
     int check_status(const char* what);
 };

@@ -14,9 +14,12 @@
 // until it leaves the window.  Words are packed (see rows.cuh), so the
 // successor is a handful of 128-bit bit operations.  Necklaces whose digit
 // sum matches a decomposition's row sum are appended (warp-aggregated) to a
-// candidate buffer with their A/B role bits.  A thread that meets the
-// buffer's soft capacity saves its position; the host drains the buffer
-// and relaunches.
+// candidate buffer with their A/B role bits.
+//
+// One launch serves several jobs (orders / compressions, each with its own
+// length, alphabet, row-sum table and candidate buffer): every window names
+// its job.  A window whose job's buffer has met its soft capacity is left
+// with its position saved; the host drains the buffers and relaunches.
 #include "gp_device.cuh"
 #include "enumerate.h"
 
@@ -27,7 +30,7 @@ namespace {
 struct W128 {
     uint64_t lo, hi;
 };
-__device__ __forceinline__ W128 w128(const decltype(EnumArgs::maxpat)& v) { return {v.lo, v.hi}; }
+__device__ __forceinline__ W128 w128(const U128p& v) { return {v.lo, v.hi}; }
 
 __device__ __forceinline__ W128 shr(W128 a, int s) {
     if (s <= 0) return a;
@@ -81,13 +84,30 @@ __device__ __forceinline__ int first_prenecklace(W128& w, int b, int L) {
     return p;
 }
 
+// The layout of the job a thread is enumerating, held in registers.
+struct JobView {
+    int L, b;
+    W128 maxpat, full;        // full = low_mask(b * L)
+    W128 ones;                // bit 0 of every digit; bit t of every digit = ones << t
+};
+
+__device__ __forceinline__ JobView job_view(const EnumJob& j) {
+    JobView v;
+    v.L = j.L;
+    v.b = j.b;
+    v.maxpat = w128(j.maxpat);
+    v.full = low_mask(j.b * j.L);
+    v.ones = w128(j.plane[0]);
+    return v;
+}
+
 // FKM successor; returns the new period, or 0 when w was the last word.
-__device__ __forceinline__ int fkm_next(W128& w, const EnumArgs& a) {
-    const W128 x = band(bxor(w, w128(a.maxpat)), low_mask(a.b * a.L));
+__device__ __forceinline__ int fkm_next(W128& w, const JobView& a) {
+    const W128 x = band(bxor(w, a.maxpat), a.full);
     if (is_zero(x)) return 0;
     const int r = ctz128(x) / a.b;  // digits after the incremented one
     const int j = a.L - 1 - r;
-    w = bor(band(w, bxor(low_mask(a.b * a.L), low_mask(a.b * r))), {0, 0});
+    w = band(w, bxor(a.full, low_mask(a.b * r)));
     // increment digit j (it is below the maximum, so no carry)
     const W128 one = shl({1ull, 0ull}, a.b * r);
     w.lo += one.lo;
@@ -97,57 +117,88 @@ __device__ __forceinline__ int fkm_next(W128& w, const EnumArgs& a) {
     return p;
 }
 
-__device__ __forceinline__ int digit_sum(W128 w, const EnumArgs& a) {
+__device__ __forceinline__ int digit_sum(W128 w, const JobView& a) {
     int s = 0;
-    for (int t = 0; t < a.b; ++t) {
-        const W128 m = band(w, W128{a.plane[t].lo, a.plane[t].hi});
-        s += (__popcll(m.lo) + __popcll(m.hi)) << t;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        if (t < a.b) {
+            const W128 m = band(w, shl(a.ones, t));
+            s += (__popcll(m.lo) + __popcll(m.hi)) << t;
+        }
     }
     return s;
 }
 
-__global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs a) {
-    __shared__ uint8_t role_tab[kMaxDigitSum + 1];
-    for (int i = threadIdx.x; i <= kMaxDigitSum; i += blockDim.x) role_tab[i] = a.roles[i];
+__device__ __forceinline__ uint4 to_u4(W128 w) {
+    return make_uint4((uint32_t)w.lo, (uint32_t)(w.lo >> 32), (uint32_t)w.hi, (uint32_t)(w.hi >> 32));
+}
+__device__ __forceinline__ W128 from_u4(uint4 v) {
+    return {((uint64_t)v.y << 32) | v.x, ((uint64_t)v.w << 32) | v.z};
+}
+__device__ __forceinline__ bool job_full(const EnumJob& j) {
+    return (int64_t)*reinterpret_cast<volatile unsigned long long*>(j.count) >= j.soft_cap;
+}
+
+// Each thread walks the windows tid, tid + nthreads, ...  A window whose job
+// has reached its soft capacity is left (position saved) and the thread goes
+// on with its next window, so one full job does not idle the others.
+// MINB = 1: registers as needed (4 CTAs of 256 per SM); MINB = 8: capped
+// at 32 registers for full occupancy (some spills).  The tuner picks.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
+    __shared__ uint8_t role_tab[kMaxEnumJobs][kMaxDigitSum + 1];
+    __shared__ EnumJob jobs[kMaxEnumJobs];
+    for (int i = threadIdx.x; i < a.njobs * (kMaxDigitSum + 1); i += blockDim.x)
+        role_tab[i / (kMaxDigitSum + 1)][i % (kMaxDigitSum + 1)] = a.roles[i];
+    if (threadIdx.x < a.njobs) jobs[threadIdx.x] = a.jobs[threadIdx.x];
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-    int64_t win = tid;                   // this thread's current window
+    int64_t win = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // current window
     bool active = win < a.nwin;
     W128 w = {0, 0}, end = {0, 0};
+    JobView jv{};
+    int job = 0;
     int p = 0;
-    bool have = false;                   // w is a valid prenecklace to process
-    unsigned long long necklaces = 0;
-    bool stop = false;
-    int step = 0;
-    for (;;) {
-        // (re)load a window when idle
-        if (active && !have) {
-            const uint4 c = a.cur[win];
-            const uint4 e = a.end[win];
-            w = {((uint64_t)c.y << 32) | c.x, ((uint64_t)c.w << 32) | c.z};
-            end = {((uint64_t)e.y << 32) | e.x, ((uint64_t)e.w << 32) | e.z};
-            if (lt(w, end)) {
-                p = first_prenecklace(w, a.b, a.L);
-                have = lt(w, end);
+    bool have = false;  // w is a valid prenecklace to process
+    bool parked_any = false;
+    unsigned long long necklaces = 0;  // of job `job`, flushed when the job changes
+    for (int step = 1;; ++step) {
+        // (re)load a window when idle; skip windows whose job is full
+        while (active && !have) {
+            const int nj = a.win_job[win];
+            if (nj != job && necklaces) {
+                atomicAdd(jobs[job].necklaces, necklaces);
+                necklaces = 0;
+            }
+            job = nj;
+            if (job_full(jobs[job])) {
+                parked_any = true;  // window untouched: it keeps its position
+            } else {
+                w = from_u4(a.cur[win]);
+                end = from_u4(a.end[win]);
+                jv = job_view(jobs[job]);
+                if (lt(w, end)) {
+                    p = first_prenecklace(w, jv.b, jv.L);
+                    have = lt(w, end);
+                }
+                if (!have) a.cur[win] = a.end[win];  // window finished
             }
             if (!have) {
-                a.cur[win] = a.end[win];  // window finished
                 win += nthreads;
                 active = win < a.nwin;
             }
         }
-        const bool any = __any_sync(0xFFFFFFFFu, active);
-        if (!any) break;
+        if (!__any_sync(0xFFFFFFFFu, active)) break;
         uint8_t role = 0;
         W128 cand = w;
-        if (active && have) {
-            if (a.L % p == 0) {
+        if (active) {
+            if (jv.L % p == 0) {
                 ++necklaces;
-                role = role_tab[digit_sum(w, a)];
+                role = role_tab[job][digit_sum(w, jv)];
             }
-            const int np = fkm_next(w, a);
+            const int np = fkm_next(w, jv);
             if (np == 0 || !lt(w, end)) {
                 have = false;
                 a.cur[win] = a.end[win];
@@ -157,51 +208,48 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs a) {
                 p = np;
             }
         }
-        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, role != 0);
-        if (bal) {
+        // append: lanes grouped by job, one atomic per group
+        const uint32_t want = __ballot_sync(0xFFFFFFFFu, role != 0);
+        if (role) {
+            const uint32_t grp = __match_any_sync(want, job);
+            const int leader = __ffs(grp) - 1;
+            const EnumJob& J = jobs[job];
             unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(a.count, (unsigned long long)__popc(bal));
-            base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if (role) {
-                const unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
-                if ((int64_t)pos < a.cap) {
-                    a.words[pos] = make_uint4((uint32_t)cand.lo, (uint32_t)(cand.lo >> 32), (uint32_t)cand.hi,
-                                              (uint32_t)(cand.hi >> 32));
-                    a.out_roles[pos] = role;
-                } else {
-                    atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
-                }
+            if (lane == leader) base = atomicAdd(J.count, (unsigned long long)__popc(grp));
+            base = __shfl_sync(grp, base, leader);
+            const unsigned long long pos = base + __popc(grp & lt_mask);
+            if ((int64_t)pos < J.cap) {
+                J.words[pos] = to_u4(cand);
+                J.out_roles[pos] = role;
+            } else {
+                atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
             }
         }
-        if ((++step & 7) == 0) {
-            unsigned long long cnt = 0;
-            if (lane == 0) cnt = *reinterpret_cast<volatile unsigned long long*>(a.count);
-            cnt = __shfl_sync(0xFFFFFFFFu, cnt, 0);
-            if ((int64_t)cnt >= a.soft_cap) {
-                stop = true;
-                break;
-            }
+        // every 8 steps: leave a window whose job reached its soft capacity
+        if ((step & 7) == 0 && active && have && job_full(jobs[job])) {
+            a.cur[win] = to_u4(w);
+            have = false;
+            parked_any = true;
+            win += nthreads;
+            active = win < a.nwin;
         }
     }
-    if (stop) {
-        // save the position of the unfinished window; later windows of this
-        // thread are untouched and still hold their starting words
-        if (active && have) {
-            a.cur[win] = make_uint4((uint32_t)w.lo, (uint32_t)(w.lo >> 32), (uint32_t)w.hi, (uint32_t)(w.hi >> 32));
-        }
-        *a.incomplete = 1;
-    }
-    if (necklaces) atomicAdd(a.necklaces, necklaces);
+    if (parked_any) *a.incomplete = 1;
+    if (necklaces) atomicAdd(jobs[job].necklaces, necklaces);
 }
 
 }  // namespace
 
-cudaError_t launch_enumerate(const EnumArgs& a, int num_sms, cudaStream_t st) {
+cudaError_t launch_enumerate(const EnumArgs& a, int num_sms, cudaStream_t st, int variant) {
     if (a.nwin <= 0) return cudaSuccess;
+    if (a.njobs < 1 || a.njobs > kMaxEnumJobs) return cudaErrorInvalidValue;
     int64_t blocks = (a.nwin + 255) / 256;
     const int64_t maxb = (int64_t)num_sms * 8;
     if (blocks > maxb) blocks = maxb;
-    enumerate_kernel<<<(unsigned)blocks, 256, 0, st>>>(a);
+    if (variant == 1)
+        enumerate_kernel<8><<<(unsigned)blocks, 256, 0, st>>>(a);
+    else
+        enumerate_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -21,9 +21,10 @@ namespace {
 
 constexpr int kWarps = 8;
 
-__global__ void mask_to_list_kernel(const uint32_t* mask, int64_t n, uint32_t* out, unsigned long long* count,
-                                    int64_t cap, int* status) {
+__global__ void mask_to_list_kernel(const uint32_t* mask, int64_t n, const unsigned long long* n_dev, uint32_t* out,
+                                    unsigned long long* count, int64_t cap, int* status) {
     const int lane = threadIdx.x & 31;
+    if (n_dev && (int64_t)*n_dev < n) n = (int64_t)*n_dev;
     const int64_t nwords = (n + 31) / 32;
     for (int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < nwords;
          wi += ((int64_t)gridDim.x * blockDim.x) >> 5) {
@@ -133,11 +134,12 @@ __global__ void __launch_bounds__(kWarps * 32) finalize_kernel(FinalizeArgs a) {
 }  // namespace
 
 cudaError_t launch_mask_to_list(const uint32_t* mask, int64_t n, uint32_t* out, unsigned long long* count,
-                                int64_t cap, int* status, int num_sms, cudaStream_t st) {
+                                int64_t cap, int* status, int num_sms, cudaStream_t st,
+                                const unsigned long long* n_dev) {
     if (n <= 0) return cudaSuccess;
     int64_t blocks = ((n + 31) / 32 + 7) / 8;
     if (blocks > (int64_t)num_sms * 16) blocks = (int64_t)num_sms * 16;
-    mask_to_list_kernel<<<(unsigned)blocks, 256, 0, st>>>(mask, n, out, count, cap, status);
+    mask_to_list_kernel<<<(unsigned)blocks, 256, 0, st>>>(mask, n, n_dev, out, count, cap, status);
     return cudaGetLastError();
 }
 

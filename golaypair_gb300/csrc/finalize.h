@@ -33,8 +33,10 @@ struct FinalizeArgs {
     int* status;
 };
 
+// Lists the set bits of mask[0 .. n) (n = min(n, *n_dev) when n_dev is set).
 cudaError_t launch_mask_to_list(const uint32_t* mask, int64_t n, uint32_t* out, unsigned long long* count,
-                                int64_t cap, int* status, int num_sms, cudaStream_t st);
+                                int64_t cap, int* status, int num_sms, cudaStream_t st,
+                                const unsigned long long* n_dev = nullptr);
 cudaError_t launch_finalize(const FinalizeArgs& a, int64_t max_rows, int num_sms, cudaStream_t st);
 
 }  // namespace gp

@@ -22,7 +22,9 @@ struct PsdTcArgs {
     const uint4* words;      // n packed words (packed input), or nullptr
     int pack_bits;           // packed: bits per digit (1..4)
     int alpha_c;             // packed: value = 2*digit - alpha_c (also bounds |value|)
-    int64_t n;
+    int64_t n;               // rows (or the capacity when n_dev is set)
+    const unsigned long long* n_dev = nullptr;  // optional: row count read on the device, min(n, *n_dev)
+    int grid_per_sm = 0;     // CTAs per SM (0 = as many as fit)
     int L;
     const void* bimage;      // twiddles: hi tile then lo tile, UMMA smem image
     float thr;               // T = 2n - paf + 0.001

@@ -205,7 +205,11 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int L = a.L;
-    const int64_t n = a.n;
+    int64_t n = a.n;
+    if (a.n_dev) {
+        const int64_t nd = (int64_t)*reinterpret_cast<const volatile unsigned long long*>(a.n_dev);
+        if (nd < n) n = nd;
+    }
     const int64_t ntiles = (n + kTileM - 1) / kTileM;
     const int RS = (int)lay.raw_stages;
     const int row_bytes = B == 0 ? L : 16;
@@ -565,7 +569,8 @@ cudaError_t launch_kb(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
     auto kern = psd_tc_kernel<K, B, WP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
     if (e != cudaSuccess) return e;
-    int64_t grid = (int64_t)num_sms * TcCfg<K>::MIN_BLOCKS;
+    const int per_sm = a.grid_per_sm > 0 && a.grid_per_sm < TcCfg<K>::MIN_BLOCKS ? a.grid_per_sm : TcCfg<K>::MIN_BLOCKS;
+    int64_t grid = (int64_t)num_sms * per_sm;
     if (grid > ntiles) grid = ntiles;
     kern<<<(unsigned)grid, kThreads, lay.total, st>>>(a, lay);
     return cudaGetLastError();

@@ -141,6 +141,40 @@ int gp_generate_window(gp_ctx* ctx, int order, int compress, int paf, uint64_t b
                        uint64_t end_hi, uint64_t end_lo, const char* path_a, const char* path_b,
                        gp_gen_stats* stats);
 
+/* One job of a batched generation: the words of one order / compression
+ * whose rank lies in [begin, end) (end clipped to the word space), written
+ * to its own A and B files. */
+typedef struct gp_gen_job {
+    int order, compress, paf;
+    uint64_t begin_hi, begin_lo, end_hi, end_lo;
+    const char* path_a;
+    const char* path_b;
+} gp_gen_job;
+
+/* Settings of the batched generation engine; zero fields take defaults. */
+typedef struct gp_batch_config {
+    int enum_variant;        /* enumerator kernel: 0 = registers as needed, 1 = full occupancy */
+    int windows_per_thread;  /* rank windows per enumerator thread (0: 1) */
+    int64_t cand_cap;        /* candidates per job per pipeline iteration (0: 2^22) */
+    int tc_ctas_per_sm;      /* tensor-core filter CTAs per SM (0: as many as fit) */
+    int no_graph;            /* 1: launch each iteration's kernels directly instead of replaying a CUDA graph */
+    int iterations;          /* out: pipeline iterations run */
+    double tune_seconds;     /* out: time spent by the tuner (0 when its result was cached) */
+} gp_batch_config;
+
+/* Generation of up to 8 jobs of different orders / compressions at once:
+ * one enumerator launch covers every job's rank windows, and each job's
+ * filter / finalize kernels run on their own branch of a per-iteration CUDA
+ * graph that is captured once and replayed until all windows are done.
+ * With autotune != 0 the engine first times its settings on a sample of
+ * the jobs and uses (and writes to *cfg) the fastest; otherwise it uses
+ * *cfg (or defaults when cfg is NULL).  stats, when not NULL, receives one
+ * entry per job.  Per job the files equal those of gp_generate_window over
+ * the same window.  No counterpart in the reference, which runs one order
+ * per process. */
+int gp_generate_batch(gp_ctx* ctx, const gp_gen_job* jobs, int njobs, int autotune, gp_batch_config* cfg,
+                      gp_gen_stats* stats);
+
 /*
  * Replaces GNU_sort(const std::vector<std::string>& in, const std::string& out,
  * const std::string& tmpdir) (src/core/sort/sort.cpp:7-22), which runs

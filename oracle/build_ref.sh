@@ -1,7 +1,9 @@
 #!/usr/bin/env bash
 # Compiles the reference's OWN C++ sources, unchanged, where they lie under
 # /root/reference, against the stand-in headers in oracle/shim/ (FFTW and
-# Boost are not installed here).  Output goes only to oracle/_ref/.
+# Boost are not installed here), into the reference CLI (golay_ref) and the
+# window driver of oracle/ref_window_driver.cpp (golay_ref_window).  Output
+# goes only to oracle/_ref/.
 #
 # Test infrastructure: the resulting binary cross-checks the oracle
 # restatement and generates golden files.  It is never shipped and never run
@@ -38,4 +40,8 @@ for s in "${SRCS[@]}"; do
 done
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -O2 -o "$OUT/golay_ref" "${OBJS[@]}" -lm
-echo "build_ref: built $OUT/golay_ref"
+# the window driver (oracle/ref_window_driver.cpp) over the same objects, minus main
+DRV="$OUT/obj/ref_window_driver.o"
+g++ -std=c++20 -O2 -w "${INC[@]}" -c "$HERE/ref_window_driver.cpp" -o "$DRV"
+g++ -O2 -o "$OUT/golay_ref_window" "$DRV" "${OBJS[@]:1}" -lm
+echo "build_ref: built $OUT/golay_ref and $OUT/golay_ref_window"
