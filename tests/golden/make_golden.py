@@ -7,10 +7,14 @@ Boost headers) into oracle/_ref/golay_ref, runs it under LC_ALL=C, and stores:
 * n16/, n26/   -- every stage file of `main N -c 2 1 all` (small, verbatim);
 * manifest.json -- line counts and SHA-256 of those files, plus of the larger
   outputs that are not stored verbatim (n=34 gen, the n=57 lambda=-2 c=3
-  shard 7 of 1000).
+  shard 7 of 1000);
+* manifest.json "windows" -- the same for the uneven batch's windows
+  (golaypair_gb300/workloads.py) at 2^32 and 2^24 words, produced by the
+  reference's own generation functions through oracle/ref_window_driver.cpp.
 
 Needs the reference sources; run in the build container only:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # everything
+    python tests/golden/make_golden.py --windows  # only the window goldens
 """
 import hashlib
 import json
@@ -19,10 +23,12 @@ import shutil
 import subprocess
 import sys
 import tempfile
+from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 REF_BIN = os.path.join(REPO, "oracle", "_ref", "golay_ref")
+REF_WINDOW_BIN = os.path.join(REPO, "oracle", "_ref", "golay_ref_window")
 
 # (name, argv after the binary, files to record, keep verbatim)
 RUNS = [
@@ -45,10 +51,43 @@ def sha256(path):
     return h.hexdigest()
 
 
+def window_key(job):
+    return "%d/%d/%d/%d-%d" % tuple(job)
+
+
+def run_window(job, tmp):
+    o, c, p, lo, hi = job
+    fa, fb = os.path.join(tmp, window_key(job).replace("/", "_") + "a"), os.path.join(tmp, window_key(job).replace("/", "_") + "b")
+    out = subprocess.run([REF_WINDOW_BIN, str(o), str(c), str(p), str(lo), str(hi), fa, fb], check=True,
+                         capture_output=True, text=True, env=dict(os.environ, LC_ALL="C")).stdout
+    rec = {"job": list(job), "necklaces": int(out.split()[-1])}
+    for side, path in (("a", fa), ("b", fb)):
+        with open(path, "rb") as f:
+            rec[side] = {"lines": f.read().count(b"\n"), "sha256": sha256(path)}
+    return rec
+
+
+def make_windows(manifest):
+    sys.path.insert(0, REPO)
+    from golaypair_gb300.workloads import batch_windows
+    jobs = batch_windows() + batch_windows(1 << 24)
+    with tempfile.TemporaryDirectory() as tmp, ThreadPoolExecutor(len(jobs)) as ex:
+        recs = list(ex.map(lambda j: run_window(j, tmp), jobs))
+    manifest["windows"] = {window_key(r["job"]): r for r in recs}
+
+
 def main():
     subprocess.run(["bash", os.path.join(REPO, "oracle", "build_ref.sh")], check=True)
     if not os.path.exists(REF_BIN):
         sys.exit("reference binary missing (no reference sources here)")
+    if "--windows" in sys.argv[1:]:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest = json.load(f)
+        make_windows(manifest)
+        with open(os.path.join(HERE, "manifest.json"), "w") as f:
+            json.dump(manifest, f, indent=1, sort_keys=True)
+        print("window goldens written")
+        return
     env = dict(os.environ, LC_ALL="C")
     manifest = {"generator": "reference sources built by oracle/build_ref.sh, LC_ALL=C", "runs": {}}
     with tempfile.TemporaryDirectory() as tmp:
@@ -68,6 +107,7 @@ def main():
                     os.makedirs(os.path.join(HERE, name), exist_ok=True)
                     shutil.copy(p, os.path.join(HERE, name, fn.replace("#", "_")))
             manifest["runs"][name] = rec
+    make_windows(manifest)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
     print("golden fixtures written")

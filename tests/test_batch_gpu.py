@@ -118,3 +118,22 @@ def test_batch_rejects_bad_jobs(tmp_path):
             ctx.generate_batch([(15, 2, 0, 0, 10, tmp_path / "a", tmp_path / "b")])  # 15 not divisible by 2
         with pytest.raises(gp.GPError):
             ctx.generate_batch([(16, 2, 0, 0, 10, tmp_path / "a", tmp_path / "b")] * 9)  # more than 8 jobs
+
+
+@pytest.mark.parametrize("size", [1 << 24, 1 << 32])
+def test_uneven_batch_windows_match_reference(golden_manifest, tmp_path, size):
+    """The uneven batch (orders 34, 50, 58, 68 at compression 2, 90 at
+    compression 5) over its seed-chosen windows, against the reference's own
+    generation functions run over the same windows (the bench's workload at
+    2^32 words)."""
+    from golaypair_gb300.workloads import batch_windows
+    wins = batch_windows(size)
+    recs = golden_manifest["windows"]
+    with gp.Context(0) as ctx:
+        files, stats, _ = run_batch(ctx, tmp_path, "w", jobs=wins, autotune=size > (1 << 24))
+    for w, (a, b), st in zip(wins, files, stats):
+        rec = recs["%d/%d/%d/%d-%d" % tuple(w)]
+        assert st.necklaces == rec["necklaces"], w
+        assert a.count(b"\n") == rec["a"]["lines"] and b.count(b"\n") == rec["b"]["lines"], w
+        assert hashlib.sha256(a).hexdigest() == rec["a"]["sha256"], w
+        assert hashlib.sha256(b).hexdigest() == rec["b"]["sha256"], w
