@@ -95,6 +95,7 @@ _STAGE_SIGS = {
     "gp_generate": [_P, _i32, _i32, _i32, _i32, _i32, _cp, _cp, _P],
     "gp_generate_window": [_P, _i32, _i32, _i32, _u64, _u64, _u64, _u64, _cp, _cp, _P],
     "gp_generate_batch": [_P, _P, _i32, _i32, _P, _P],
+    "gp_tuned_settings": [_P, _P, _i32],
     "gp_sort": [_P, _P, _i32, _cp],
     "gp_match": [_P, _i32, _i32, _i32, _cp, _cp, _cp, _i32, _P],
     "gp_uncompress": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp],
@@ -202,6 +203,17 @@ class Context:
                                                ctypes.byref(cfg), ctypes.cast(stats, ctypes.c_void_p)),
                    "gp_generate_batch")
         return list(stats), cfg
+
+    def tuned_settings(self):
+        """{workload key: [values]} chosen by the context's tuners."""
+        need = self._lib.gp_tuned_settings(self._h, None, 0)
+        buf = ctypes.create_string_buffer(max(need, 1))
+        self._lib.gp_tuned_settings(self._h, buf, len(buf))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            k, *v = line.split()
+            out[k] = [int(x) for x in v]
+        return out
 
     def kernel_timing(self, enable=True):
         self._lib.gp_kernel_timing(self._h, 1 if enable else 0)

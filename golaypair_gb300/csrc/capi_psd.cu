@@ -291,7 +291,7 @@ static int check_args(gp_ctx* c, int64_t n, int L, int mode) {
     if (n < 0 || L < 1 || L > gp::kMaxLen) return c->fail(GP_ERR_ARG, "bad n=%lld or L=%d", (long long)n, L);
     if (mode != GP_PSD_FP64 && mode != GP_PSD_TC_GUARDED) return c->fail(GP_ERR_ARG, "bad mode %d", mode);
     if (mode == GP_PSD_TC_GUARDED && !gp::tc_k_for_len(L))
-        return c->fail(GP_ERR_UNSUPPORTED, "tensor-core filter supports 2 <= L <= %d", gp::kMaxTcK);
+        return c->fail(GP_ERR_UNSUPPORTED, "tensor-core filter supports 2 <= L <= %d", gp::kMaxTcK - 1);
     return GP_OK;
 }
 

@@ -15,6 +15,7 @@
 // vectors.  Pairs are written in the reference's order: token order, then A
 // line order, then B line order.
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -261,6 +262,38 @@ int gp_match_texts(gp_ctx* c, int L, int compress, int paf, const std::string& t
     return GP_OK;
 }
 
+// The sort's tuner: per key width, times whole sorts with 8- and 4-bit
+// passes on (up to) the first 2^18 keys, twice each (the first round warms
+// up), and keeps the faster; cached in the context.  Leaves di scrambled.
+int sort_radix_bits(gp_ctx* c, const uint32_t* dk, int Wk, int64_t n, uint32_t* di, void* tmp, cudaStream_t s,
+                    int* bits) {
+    const std::string key = "sort:W" + std::to_string(Wk);
+    auto it = c->tuned.find(key);
+    if (it != c->tuned.end()) {
+        *bits = (int)it->second[0];
+        return GP_OK;
+    }
+    *bits = 8;
+    if (n < (1 << 14)) return GP_OK;  // too small to time: default, not cached
+    const int64_t m = std::min<int64_t>(n, 1 << 18);
+    double best = 1e300;
+    const int order[4] = {8, 4, 8, 4};
+    for (int r = 0; r < 4; ++r) {
+        GP_CUDA_TRY(c, gp::iota_u32(di, m, s));
+        GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+        const auto t0 = std::chrono::steady_clock::now();
+        GP_CUDA_TRY(c, gp::radix_sort_keys(dk, Wk, Wk, di, m, tmp, s, order[r]));
+        GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (r >= 2 && el < best) {
+            best = el;
+            *bits = order[r];
+        }
+    }
+    c->tuned[key] = {*bits, (int64_t)(best * 1e6)};
+    return GP_OK;
+}
+
 // Sorted, de-duplicated lines of `text` (byte order).
 int gp_sort_text(gp_ctx* c, const std::string& text, std::string& out) {
     std::vector<uint64_t> start;
@@ -302,8 +335,11 @@ int gp_sort_text(gp_ctx* c, const std::string& text, std::string& out) {
     build_keys_kernel<<<grid_for(n), 256, 0, s>>>(dt.as<char>(), ds.as<uint64_t>(), dl.as<uint32_t>(), n, Wk,
                                                   nibble ? 1 : 0, dk.as<uint32_t>());
     GP_CUDA_TRY(c, cudaGetLastError());
+    int bits = 8;
+    int rc = sort_radix_bits(c, dk.as<uint32_t>(), Wk, n, di.as<uint32_t>(), dtmp.p, s, &bits);
+    if (rc) return rc;
     GP_CUDA_TRY(c, gp::iota_u32(di.as<uint32_t>(), n, s));
-    GP_CUDA_TRY(c, gp::radix_sort_keys(dk.as<uint32_t>(), Wk, Wk, di.as<uint32_t>(), n, dtmp.p, s));
+    GP_CUDA_TRY(c, gp::radix_sort_keys(dk.as<uint32_t>(), Wk, Wk, di.as<uint32_t>(), n, dtmp.p, s, bits));
     GP_CUDA_TRY(c, gp::mark_unique(dk.as<uint32_t>(), Wk, di.as<uint32_t>(), n, Wk, dflag.as<uint32_t>(), s));
     uint32_t* d_cnt = dout.as<uint32_t>() + n;
     GP_CUDA_TRY(c, gp::compact_flags(dflag.as<uint32_t>(), di.as<uint32_t>(), dout.as<uint32_t>(), n, dpos.as<uint32_t>(),
@@ -322,6 +358,22 @@ int gp_sort_text(gp_ctx* c, const std::string& text, std::string& out) {
 }
 
 extern "C" {
+
+int gp_tuned_settings(const gp_ctx* c, char* buf, int cap) {
+    if (!c) return GP_ERR_ARG;
+    std::string t;
+    for (const auto& kv : c->tuned) {
+        t += kv.first;
+        for (int64_t v : kv.second) t += " " + std::to_string(v);
+        t += "\n";
+    }
+    if (buf && cap > 0) {
+        const size_t k = std::min(t.size(), (size_t)cap - 1);
+        std::memcpy(buf, t.data(), k);
+        buf[k] = 0;
+    }
+    return (int)t.size() + 1;
+}
 
 int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
     if (!c || (!in_paths && n_in > 0) || !out_path) return GP_ERR_ARG;

@@ -13,7 +13,7 @@
 namespace gp {
 
 constexpr int kTileM = 128;     // candidates per tensor-core tile (TMEM lanes)
-constexpr int kMaxTcK = 128;    // longest sequence the tensor-core filter takes
+constexpr int kMaxTcK = 128;    // largest padded K of the tensor-core filter (L <= 127)
 constexpr int kMaxLen = 512;    // longest sequence any kernel takes
 
 // ------------------------------------------------------------ PSD filter
@@ -49,10 +49,32 @@ enum TcTrace {
     kTrProdWait, kTrProdIssue, kTrTiles, kTrConvFence, kTrMmaCommit, kTrCount
 };
 
-// Builds the B-operand image (hi tile, lo tile) for length L, K = padded L.
+// Builds the B-operand image (hi and lo twiddles) for length L, K = padded L.
 // Returns its size in bytes; writes it to out when out != nullptr.
 size_t build_twiddle_image(int L, int K, void* out);
-int tc_k_for_len(int L);               // padded K (multiple of 16), or 0 if unsupported
+int tc_k_for_len(int L);               // padded K (multiple of 16, > L), or 0 if unsupported
+
+// Where twiddle row `nrow` (0..K-1), column j (0..K-1), part (0 hi, 1 lo)
+// sits in the B image, as an index of fp16 elements.  The image is a K x 2K
+// fp16 matrix (hi part at column j, lo part at column K + j) in the
+// canonical no-swizzle K-major layout of 8 x 8 core matrices: core matrix
+// (n/8, col/8) at byte (col/8) * (K/8) * 128 + (n/8) * 128, row n%8 at +16,
+// column col%8 at +2.
+__host__ __device__ inline size_t tc_image_index(int nrow, int j, int part, int K) {
+    const int col = j + part * K;
+    return ((size_t)(col / 8) * (K / 8) * 128 + (size_t)(nrow / 8) * 128 + (size_t)(nrow % 8) * 16 + (col % 8) * 2) / 2;
+}
+
+// Bin of twiddle row nrow: cosine rows 0..K/2-1 are bins 1..K/2, sine rows
+// K/2..K-1 bins 1..K/2.  Bins above L/2 are zero rows, except the last
+// cosine row (bin K/2 > L/2 since K > L): all ones, the row sum X_0.
+// Returns 0 (zero row), 1 (cosine of *bin), 2 (sine of *bin) or 3 (ones).
+__host__ __device__ inline int tc_row_kind(int nrow, int L, int K, int* bin) {
+    const bool is_sin = nrow >= K / 2;
+    *bin = (is_sin ? nrow - K / 2 : nrow) + 1;
+    if (*bin <= L / 2) return is_sin ? 2 : 1;
+    return (!is_sin && nrow == K / 2 - 1) ? 3 : 0;
+}
 bool tc_packed_supported(int L, int b);  // packed-word input with b bits per digit
 float tc_err_coef(int K);              // |X| error per unit of sum|x|
 

@@ -51,28 +51,23 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 // Twiddles built on the device: the tensor-core image in the same canonical
 // layout as build_twiddle_image, and the FP64 (cos, sin) table.
 __global__ void noalloc_twiddles_kernel(unsigned char* scratch, int L, int K) {
-    // B operand image: 2K rows (hi rows 0..K-1, lo rows K..2K-1) x K columns
     uint16_t* img = reinterpret_cast<uint16_t*>(scratch + kOffImage);
     double* tw = reinterpret_cast<double*>(scratch + kOffTw64);
-    const int N = K, NT = 2 * K, H = L / 2;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N * K; e += gridDim.x * blockDim.x) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < K * K; e += gridDim.x * blockDim.x) {
         const int nrow = e / K, j = e % K;
-        const bool is_sin = nrow >= N / 2;
-        const int bin = (is_sin ? nrow - N / 2 : nrow) + 1;
+        int bin = 0;
+        const int kind = tc_row_kind(nrow, L, K, &bin);
         double w = 0.0;
-        if (bin <= H && j < L) {
+        if (kind != 0 && j < L) {
             const int m = (int)(((long long)j * bin) % L);
             double s, c;
             sincospi(2.0 * (double)m / (double)L, &s, &c);
-            w = is_sin ? s : c;
+            w = kind == 3 ? 1.0 : kind == 2 ? s : c;
         }
         const __half h = __double2half(w);
         const __half l = __double2half(w - (double)__half2float(h));
-        for (int part = 0; part < 2; ++part) {
-            const int nn = nrow + part * K;
-            const size_t byte = (size_t)(j / 8) * (NT / 8) * 128 + (size_t)(nn / 8) * 128 + (nn % 8) * 16 + (j % 8) * 2;
-            img[byte / 2] = __half_as_ushort(part ? l : h);
-        }
+        img[tc_image_index(nrow, j, 0, K)] = __half_as_ushort(h);
+        img[tc_image_index(nrow, j, 1, K)] = __half_as_ushort(l);
     }
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < L; m += gridDim.x * blockDim.x) {
         double s, c;

@@ -3,8 +3,9 @@
 //
 // Keys are rows of W 32-bit words, word 0 most significant.  The sort
 // permutes a uint32 index array (keys stay in place and are gathered per
-// pass), 8 bits per pass; a pass whose digit is the same for every key is
-// skipped (its histogram has a single non-empty bucket).
+// pass), 4 or 8 bits per pass (the sort's tuner picks); a pass whose digit
+// is the same for every key is skipped (its histogram has a single non-empty
+// bucket).
 #include <cstdio>
 #include <vector>
 
@@ -67,50 +68,59 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
 
+template <int RB>
 __device__ __forceinline__ uint32_t key_digit(const uint32_t* keys, int W, uint32_t idx, int word, int shift) {
-    return (keys[(int64_t)idx * W + word] >> shift) & 0xFFu;
+    return (keys[(int64_t)idx * W + word] >> shift) & ((1u << RB) - 1u);
 }
 
+// RB bits per pass: 2^RB buckets (RB <= 8, so one thread per bucket).
+template <int RB>
 __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint32_t* keys, int W, const uint32_t* idx,
                                                                    int64_t n, int word, int shift, uint32_t* counts,
                                                                    int64_t nblocks, uint32_t* total) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
+    constexpr int NB = 1 << RB;
+    __shared__ uint32_t h[NB];
+    if (threadIdx.x < NB) h[threadIdx.x] = 0;
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * kSortTile;
     for (int k = 0; k < kSortItems; ++k) {
         const int64_t i = base + (int64_t)k * kSortThreads + threadIdx.x;
-        if (i < n) atomicAdd(&h[key_digit(keys, W, idx[i], word, shift)], 1u);
+        if (i < n) atomicAdd(&h[key_digit<RB>(keys, W, idx[i], word, shift)], 1u);
     }
     __syncthreads();
-    const uint32_t c = h[threadIdx.x];
-    counts[(int64_t)threadIdx.x * nblocks + blockIdx.x] = c;
-    if (c) atomicAdd(&total[threadIdx.x], c);
+    if (threadIdx.x < NB) {
+        const uint32_t c = h[threadIdx.x];
+        counts[(int64_t)threadIdx.x * nblocks + blockIdx.x] = c;
+        if (c) atomicAdd(&total[threadIdx.x], c);
+    }
 }
 
+template <int RB>
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(const uint32_t* keys, int W, const uint32_t* idx_in,
                                                                       uint32_t* idx_out, int64_t n, int word, int shift,
                                                                       const uint32_t* offsets, int64_t nblocks) {
-    __shared__ uint32_t base[256];
-    __shared__ uint32_t wh[kSortThreads / 32][256];
+    constexpr int NB = 1 << RB;
+    __shared__ uint32_t base[NB];
+    __shared__ uint32_t wh[kSortThreads / 32][NB];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    base[threadIdx.x] = offsets[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+    if (threadIdx.x < NB) base[threadIdx.x] = offsets[(int64_t)threadIdx.x * nblocks + blockIdx.x];
     const int64_t tile0 = (int64_t)blockIdx.x * kSortTile;
     for (int k = 0; k < kSortItems; ++k) {
-        for (int w = 0; w < kSortThreads / 32; ++w) wh[w][threadIdx.x] = 0;
+        if (threadIdx.x < NB)
+            for (int w = 0; w < kSortThreads / 32; ++w) wh[w][threadIdx.x] = 0;
         __syncthreads();
         const int64_t i = tile0 + (int64_t)k * kSortThreads + threadIdx.x;
         const bool valid = i < n;
         uint32_t my_idx = 0, d = 0x100u + (uint32_t)lane;  // invalid lanes: unique sentinel
         if (valid) {
             my_idx = idx_in[i];
-            d = key_digit(keys, W, my_idx, word, shift);
+            d = key_digit<RB>(keys, W, my_idx, word, shift);
         }
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
         const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
         if (valid && rank == 0) wh[warp][d] = __popc(peers);
         __syncthreads();
-        {
+        if (threadIdx.x < NB) {
             uint32_t run = base[threadIdx.x];
             for (int w = 0; w < kSortThreads / 32; ++w) {
                 const uint32_t c = wh[w][threadIdx.x];
@@ -212,9 +222,13 @@ size_t radix_sort_tmp_bytes(int64_t n) {
 
 // Sorts idx (a permutation of row numbers) by the keys' first `sort_words`
 // words (of W).  Stable.  tmp: radix_sort_tmp_bytes(n) bytes of device memory.
+// radix_bits: 4 or 8 bits per pass.
 cudaError_t radix_sort_keys(const uint32_t* keys, int W, int sort_words, uint32_t* idx, int64_t n, void* tmp,
-                            cudaStream_t st) {
+                            cudaStream_t st, int radix_bits) {
     if (n <= 1) return cudaSuccess;
+    if (radix_bits != 4 && radix_bits != 8) return cudaErrorInvalidValue;
+    const int NB = 1 << radix_bits;
+    const int per_word = 32 / radix_bits;
     const int64_t nb = (n + kSortTile - 1) / kSortTile;
     uint8_t* t = static_cast<uint8_t*>(tmp);
     uint32_t* alt = reinterpret_cast<uint32_t*>(t);
@@ -229,23 +243,29 @@ cudaError_t radix_sort_keys(const uint32_t* keys, int W, int sort_words, uint32_
     uint32_t* stmp = reinterpret_cast<uint32_t*>(t);
     uint32_t* cur = idx;
     uint32_t* nxt = alt;
-    std::vector<uint32_t> htotal(256);
-    for (int bi = 0; bi < 4 * sort_words; ++bi) {
-        const int word = sort_words - 1 - bi / 4;
-        const int shift = 8 * (bi % 4);
-        cudaError_t e = cudaMemsetAsync(total, 0, 256 * 4, st);
+    std::vector<uint32_t> htotal(NB);
+    for (int bi = 0; bi < per_word * sort_words; ++bi) {
+        const int word = sort_words - 1 - bi / per_word;
+        const int shift = radix_bits * (bi % per_word);
+        cudaError_t e = cudaMemsetAsync(total, 0, NB * 4, st);
         if (e != cudaSuccess) return e;
-        radix_hist_kernel<<<(unsigned)nb, kSortThreads, 0, st>>>(keys, W, cur, n, word, shift, counts, nb, total);
-        e = cudaMemcpyAsync(htotal.data(), total, 256 * 4, cudaMemcpyDeviceToHost, st);
+        if (radix_bits == 8)
+            radix_hist_kernel<8><<<(unsigned)nb, kSortThreads, 0, st>>>(keys, W, cur, n, word, shift, counts, nb, total);
+        else
+            radix_hist_kernel<4><<<(unsigned)nb, kSortThreads, 0, st>>>(keys, W, cur, n, word, shift, counts, nb, total);
+        e = cudaMemcpyAsync(htotal.data(), total, NB * 4, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return e;
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return e;
         int nonempty = 0;
         for (uint32_t c : htotal) nonempty += c != 0;
         if (nonempty <= 1) continue;  // every key has the same digit here
-        e = exclusive_scan_u32(counts, offs, nb * 256, stmp, st);
+        e = exclusive_scan_u32(counts, offs, nb * NB, stmp, st);
         if (e != cudaSuccess) return e;
-        radix_scatter_kernel<<<(unsigned)nb, kSortThreads, 0, st>>>(keys, W, cur, nxt, n, word, shift, offs, nb);
+        if (radix_bits == 8)
+            radix_scatter_kernel<8><<<(unsigned)nb, kSortThreads, 0, st>>>(keys, W, cur, nxt, n, word, shift, offs, nb);
+        else
+            radix_scatter_kernel<4><<<(unsigned)nb, kSortThreads, 0, st>>>(keys, W, cur, nxt, n, word, shift, offs, nb);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         uint32_t* sw = cur;

@@ -20,6 +20,6 @@ cudaError_t mark_unique(const uint32_t* keys, int W, const uint32_t* idx, int64_
 cudaError_t iota_u32(uint32_t* p, int64_t n, cudaStream_t st);
 size_t radix_sort_tmp_bytes(int64_t n);
 cudaError_t radix_sort_keys(const uint32_t* keys, int W, int sort_words, uint32_t* idx, int64_t n, void* tmp,
-                            cudaStream_t st);
+                            cudaStream_t st, int radix_bits = 8);
 
 }  // namespace gp

@@ -4,14 +4,21 @@
 // psd[k] > 2n - paf + 0.001 for k = 1..L/2) as a batched dense contraction:
 //
 //   X[M=128 candidates x K] (fp16, exact small integers)
-//     * [W_hi | W_lo][K x 2K] (cos/sin twiddles split into hi + lo fp16)
-//     -> D[128 x 2K] fp32 in TMEM;  re_k = D_hi + D_lo, p_k = re^2 + im^2.
+//     * W[K x N] (cos/sin twiddles, each split into hi + lo fp16)
+//     -> D[128 x N] fp32 in TMEM, p_k = re_k^2 + im_k^2.
 //
-// One UMMA of N = 2K per 16-wide K step (hi and lo side by side) instead of
-// two passes of N = K: half the MMA instructions.  Within each half, row
-// n < K/2 of W is the cosine of bin n+1, row K/2 + n the sine of bin n+1;
-// bins above L/2 and columns j >= L are zero, so the padding columns of X
-// never contribute.  K = L rounded up to 16.
+// Row n < K/2 of W is the cosine of bin n+1, row K/2 + n the sine of bin
+// n+1; bins above L/2 and columns j >= L are zero, so the padding columns of
+// X never contribute.  K = L + 1 rounded up to 16, so the last cosine row
+// (bin K/2) is always beyond L/2: it holds ones instead, and that column of
+// D is the row sum X_0 (exact).  By Parseval, sum x^2 = (X_0^2 + 2 sum_k p_k)
+// / L (bin L/2 of an even L counted twice: an upper bound), which gives the
+// per-row error bound without reading the row twice.
+//
+// The hi and lo twiddles are stacked along K: the B image is K x 2K, and
+// the UMMA runs K/16 steps against the hi columns, then K/16 against the lo
+// columns, all reading the same A columns and accumulating into ONE fp32
+// accumulator of N = K columns (re and im come straight out of TMEM).
 //
 // Each candidate is classified against T = 2n - paf + 0.001 with a guard g
 // (the configured band, widened per row to a rigorous bound on the fp32
@@ -31,8 +38,7 @@
 // the bulk-copy engine, read once by the converters) and the constant B.
 //
 // Persistent kernel, one 128-candidate tile per step, warp roles:
-//   warps 0-3  convert: staged tile -> fp16 row in TMEM (+ sum x^2 for the
-//              int8 error bound)
+//   warps 0-3  convert: staged tile -> fp16 row in TMEM
 //   warps 4-7  epilogue: TMEM -> registers -> PSD max -> mask / unsure list
 //   warp 8     producer: cp.async.bulk of each tile into a deep ring
 //   warp 9     MMA issuer (one lane) and TMEM owner
@@ -54,30 +60,29 @@ constexpr uint32_t kSmemBudget2Cta = 112 * 1024;  // two CTAs per SM
 constexpr uint32_t kSmemBudget1Cta = 220 * 1024;
 constexpr int kLutBytes = 4096;
 
-// accumulator buffers and TMEM A stages per K (columns: NACC*2K + AS*K/2)
-constexpr int tc_nacc(int K) { return K == 16 ? 4 : K == 32 ? 3 : K == 48 ? 2 : K == 64 ? 3 : K <= 96 ? 2 : K == 112 ? 2 : 1; }
-constexpr int tc_as(int K) { return K == 16 ? 4 : K == 32 ? 3 : K == 48 ? 2 : K <= 80 ? 4 : K == 96 ? 2 : K == 112 ? 1 : 4; }
+// accumulator buffers and TMEM A stages per K (columns: NACC*N + AS*K/2)
+constexpr int tc_nacc(int K) { return K <= 32 ? 4 : K == 48 ? 3 : K <= 80 ? 4 : K <= 112 ? 3 : 2; }
+constexpr int tc_as(int K) { return K == 112 ? 3 : 4; }
 
 template <int K>
 struct TcCfg {
     static constexpr int M = kTileM;
-    static constexpr int N = 2 * K;                    // UMMA N: hi half then lo half
+    static constexpr int N = K;                        // UMMA N: K/2 cosine + K/2 sine bins
     static constexpr int KCH = K / 8;                  // 8-element chunks along K
     static constexpr int KW = K / 4 + 1;               // 32-bit words covering a row's K bytes + misalignment
-    static constexpr int KSTEPS = K / 16;              // UMMA instructions per tile
-    static constexpr int B_BYTES = N * K * 2;          // whole B image (hi and lo)
-    static constexpr int B_KSTRIDE = (N / 8) * 128;
+    static constexpr int KSTEPS = K / 16;              // UMMA K steps per hi or lo pass
+    static constexpr int B_BYTES = 2 * K * K * 2;      // whole B image (hi and lo)
+    static constexpr int B_KSTRIDE = (N / 8) * 128;    // bytes between core matrices adjacent in K
     static constexpr int MIN_BLOCKS = K <= 48 ? 2 : 1;
     static constexpr int TMEM_COLS = MIN_BLOCKS == 2 ? 256 : 512;
     static constexpr int NACC = tc_nacc(K);
     static constexpr int AS = tc_as(K);                // A stages in TMEM
     static constexpr int A_COL0 = NACC * N;            // first TMEM column of the A stages
-    static constexpr int RING = AS + NACC;             // sum x^2 stash slots
     static_assert(NACC * N + AS * K / 2 <= TMEM_COLS, "TMEM budget");
 };
 
 struct SmemLayout {
-    uint32_t b_off, a_off, lut_off, raw_off, raw_stride, raw_stages, stash_off, bar_off, misc_off, total;
+    uint32_t b_off, lut_off, raw_off, raw_stride, raw_stages, bar_off, misc_off, total;
 };
 
 template <int K>
@@ -88,13 +93,10 @@ SmemLayout smem_layout(int row_bytes) {
     s.b_off = off;
     off += C::B_BYTES;
     off = (off + 1023) & ~1023u;
-    s.a_off = off;
     s.lut_off = off;
     off += kLutBytes;
-    s.stash_off = off;
-    off += C::RING * kTileM * 4;
     s.bar_off = off;
-    off += (2 * kMaxRawStages + 2 * C::AS + 2 * C::NACC + C::RING + 2) * 8;
+    off += (2 * kMaxRawStages + 2 * C::AS + 2 * C::NACC + 2) * 8;
     s.misc_off = off;
     off += 16;
     off = (off + 127) & ~127u;
@@ -188,7 +190,6 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     uint8_t* sB = smem + lay.b_off;
     uint8_t* sLut = smem + lay.lut_off;
     uint8_t* sRaw = smem + lay.raw_off;
-    float* stash = reinterpret_cast<float*>(smem + lay.stash_off);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bar_off);
     uint64_t* raw_full = bars;
     uint64_t* raw_empty = bars + kMaxRawStages;
@@ -198,7 +199,6 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     uint64_t* acc_empty = acc_full + C::NACC;
     uint64_t* b_full = acc_empty + C::NACC;
     uint64_t* final_bar = b_full + 1;
-    uint64_t* stash_full = final_bar + 1;  // RING barriers: sum x^2 of a tile is written
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + lay.misc_off);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + lay.misc_off + 4);
 
@@ -231,7 +231,6 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         }
         mbar_init(b_full, 1);
         mbar_init(final_bar, 1);
-        for (int i = 0; i < C::RING; ++i) mbar_init(&stash_full[i], kConvWarps);
         *abort_flag = 0;
         mbar_fence_init();
     }
@@ -246,14 +245,10 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
 
     if (warp < kConvWarps) {
         // ------------------------------------------------ converters
+        // Row r's bytes L..K-1 in a full tile are the next row's first
+        // bytes: they land in A columns whose B rows are all zero, so they
+        // add nothing and are not masked.
         const int r = threadIdx.x;  // row of the tile = TMEM lane
-        uint32_t mlo[C::KCH], mhi[C::KCH];
-#pragma unroll
-        for (int c = 0; c < C::KCH; ++c) {
-            const int v = L - 8 * c;
-            mlo[c] = v >= 4 ? 0xFFFFFFFFu : (v <= 0 ? 0u : ((1u << (8 * v)) - 1u));
-            mhi[c] = v >= 8 ? 0xFFFFFFFFu : (v <= 4 ? 0u : ((1u << (8 * (v - 4))) - 1u));
-        }
         const int norm = 128 - B * L;  // packed: left shift that puts digit 0 at bit 127
         const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16) + (uint32_t)C::A_COL0;
         int64_t it = 0;
@@ -273,7 +268,6 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             tc_fence_after();
             const int64_t row = t * kTileM + r;
             const bool full_tile = aligned && (t + 1) * kTileM <= n;
-            int sumsq = 0;
             uint32_t h[K / 2];  // the row as fp16 pairs
             if constexpr (B == 0) {
                 if (full_tile) {
@@ -286,10 +280,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                     for (int i = 0; i < C::KW; ++i) wv[i] = wp[i];
 #pragma unroll
                     for (int c = 0; c < C::KCH; ++c) {
-                        const uint32_t lo = __funnelshift_r(wv[2 * c], wv[2 * c + 1], sh) & mlo[c];
-                        const uint32_t hi = __funnelshift_r(wv[2 * c + 1], wv[2 * c + 2], sh) & mhi[c];
-                        sumsq = __dp4a((int)lo, (int)lo, sumsq);
-                        sumsq = __dp4a((int)hi, (int)hi, sumsq);
+                        const uint32_t lo = __funnelshift_r(wv[2 * c], wv[2 * c + 1], sh);
+                        const uint32_t hi = __funnelshift_r(wv[2 * c + 1], wv[2 * c + 2], sh);
                         i8x4_to_h2x2(lo, h[4 * c], h[4 * c + 1]);
                         i8x4_to_h2x2(hi, h[4 * c + 2], h[4 * c + 3]);
                     }
@@ -305,8 +297,6 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                             const uint32_t v = (valid && j < L) ? (uint32_t)(uint8_t)src[j] : 0u;
                             w[bb >> 2] |= v << (8 * (bb & 3));
                         }
-                        sumsq = __dp4a((int)w[0], (int)w[0], sumsq);
-                        sumsq = __dp4a((int)w[1], (int)w[1], sumsq);
                         i8x4_to_h2x2(w[0], h[4 * c], h[4 * c + 1]);
                         i8x4_to_h2x2(w[1], h[4 * c + 2], h[4 * c + 3]);
                     }
@@ -338,14 +328,12 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const uint32_t aaddr = lane_base + (uint32_t)(as * (K / 2));
 #pragma unroll
             for (int g = 0; g < K / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
-            if constexpr (B == 0) stash[(int)(it % C::RING) * kTileM + r] = (float)sumsq;
             const long long c3t = clock64();
             tr3 += c3t - c2t;
             tmem_wait_st();
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
-                if constexpr (B == 0) mbar_arrive(&stash_full[(int)(it % C::RING)]);
                 mbar_arrive(&a_full[as]);
                 mbar_arrive(&raw_empty[rs]);
             }
@@ -381,21 +369,28 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const int64_t row = t * kTileM + r;
             const bool valid = row < n;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * C::N);
-            float pmax = 0.f;
+            // column HB - 1 of the cosine block holds the row sum X_0
+            float pmax = 0.f, x0 = 0.f;
+            float2 psum = make_float2(0.f, 0.f);
 #pragma unroll
             for (int ch = 0; ch < HB / 8; ++ch) {
-                float chi[8], shi[8], clo[8], slo[8];
-                tmem_ld8(taddr + 8 * ch, chi);
-                tmem_ld8(taddr + HB + 8 * ch, shi);
-                tmem_ld8(taddr + K + 8 * ch, clo);
-                tmem_ld8(taddr + K + HB + 8 * ch, slo);
+                float cr[8], ci[8];
+                tmem_ld8(taddr + 8 * ch, cr);
+                tmem_ld8(taddr + HB + 8 * ch, ci);
                 tmem_wait_ld();
 #pragma unroll
                 for (int k = 0; k < 8; k += 2) {
-                    const float2 re = __fadd2_rn(make_float2(chi[k], chi[k + 1]), make_float2(clo[k], clo[k + 1]));
-                    const float2 im = __fadd2_rn(make_float2(shi[k], shi[k + 1]), make_float2(slo[k], slo[k + 1]));
+                    const float2 re = make_float2(cr[k], cr[k + 1]);
+                    const float2 im = make_float2(ci[k], ci[k + 1]);
                     const float2 p = __ffma2_rn(re, re, __fmul2_rn(im, im));
-                    pmax = fmaxf(pmax, fmaxf(p.x, p.y));
+                    if (ch == HB / 8 - 1 && k == 6) {
+                        pmax = fmaxf(pmax, p.x);
+                        psum.x += p.x;
+                        x0 = re.y;
+                    } else {
+                        pmax = fmaxf(pmax, fmaxf(p.x, p.y));
+                        psum = __fadd2_rn(psum, p);
+                    }
                     if constexpr (WRITE_PSD) {
                         if (valid) {
                             a.psd_out[row * HB + 8 * ch + k] = p.x;
@@ -406,17 +401,11 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             }
             float g = g_const;
             if constexpr (B == 0) {
-                // The converters wrote sum x^2 for this tile before the A tile
-                // was released to the MMA, and cannot lap the RING slots: the
-                // MMA of a later use waits for this epilogue to free its
-                // accumulator.
-                const int slot = (int)(it % C::RING);
-                const long long c3t = clock64();
-                if (!mbar_wait(&stash_full[slot], (uint32_t)((it / C::RING) & 1), abort_flag, a.status, 11)) break;
-                tr1 += clock64() - c3t;
-                // sum|x| <= sqrt(L * sum x^2)
-                const float ssq = stash[slot * kTileM + r];
-                const float d = a.err_coef * sqrtf((float)L * ssq);
+                // Parseval: L sum x^2 = X_0^2 + 2 sum_k p_k (an upper bound
+                // for even L), inflated by 1% and L for the fp32 error of the
+                // p_k; sum|x| <= sqrt(L sum x^2).
+                const float l_sumsq = fmaf(x0, x0, 2.f * (psum.x + psum.y)) * 1.01f + (float)L;
+                const float d = a.err_coef * sqrtf(l_sumsq);
                 g = fmaxf(a.guard_cfg, 2.f * sq * d + 3.f * d * d + 1e-4f);
             }
             tc_fence_before();
@@ -525,10 +514,15 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 tc_fence_after();
                 const uint32_t d = tmem_base + (uint32_t)(b * C::N);
                 const uint32_t a0 = tmem_base + (uint32_t)(C::A_COL0 + as * (K / 2));
+                // the hi pass, then the lo pass (B columns K..2K-1) into the
+                // same accumulator, both reading the same A columns
 #pragma unroll
-                for (int ks = 0; ks < C::KSTEPS; ++ks)
-                    umma_f16_ts(d, a0 + (uint32_t)(8 * ks), bdesc0 + (uint64_t)((ks * 2 * C::B_KSTRIDE) >> 4), idesc,
-                                ks != 0 ? 1u : 0u);
+                for (int pass = 0; pass < 2; ++pass)
+#pragma unroll
+                    for (int ks = 0; ks < C::KSTEPS; ++ks)
+                        umma_f16_ts(d, a0 + (uint32_t)(8 * ks),
+                                    bdesc0 + (uint64_t)(((pass * (K / 8) + 2 * ks) * C::B_KSTRIDE) >> 4), idesc,
+                                    (pass | ks) != 0 ? 1u : 0u);
                 const long long c3 = clock64();
                 umma_commit(&a_empty[as]);
                 umma_commit(&acc_full[b]);
@@ -563,13 +557,14 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
 
 template <int K, int B, bool WP>
 cudaError_t launch_kb(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
+    using C = TcCfg<K>;
     const SmemLayout lay = smem_layout<K>(B == 0 ? a.L : 16);
     const int64_t ntiles = (a.n + kTileM - 1) / kTileM;
     if (ntiles == 0) return cudaSuccess;
     auto kern = psd_tc_kernel<K, B, WP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
     if (e != cudaSuccess) return e;
-    const int per_sm = a.grid_per_sm > 0 && a.grid_per_sm < TcCfg<K>::MIN_BLOCKS ? a.grid_per_sm : TcCfg<K>::MIN_BLOCKS;
+    const int per_sm = a.grid_per_sm > 0 && a.grid_per_sm < C::MIN_BLOCKS ? a.grid_per_sm : C::MIN_BLOCKS;
     int64_t grid = (int64_t)num_sms * per_sm;
     if (grid > ntiles) grid = ntiles;
     kern<<<(unsigned)grid, kThreads, lay.total, st>>>(a, lay);
@@ -586,13 +581,13 @@ cudaError_t launch_k(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
     switch (a.pack_bits) {
         case 1: return launch_kb<K, 1, false>(a, num_sms, st);
         case 2:
-            if constexpr (K <= 64) return launch_kb<K, 2, false>(a, num_sms, st);
+            if constexpr (K <= 80) return launch_kb<K, 2, false>(a, num_sms, st);
             break;
         case 3:
             if constexpr (K <= 48) return launch_kb<K, 3, false>(a, num_sms, st);
             break;
         case 4:
-            if constexpr (K <= 32) return launch_kb<K, 4, false>(a, num_sms, st);
+            if constexpr (K <= 48) return launch_kb<K, 4, false>(a, num_sms, st);
             break;
         default: break;
     }
@@ -633,17 +628,19 @@ double half_value(uint16_t h) {
 
 }  // namespace
 
+// K: L + 1 rounded up to 16, so that the last cosine row is free for the
+// row sum (bin K/2 > L/2).
 int tc_k_for_len(int L) {
-    if (L < 2 || L > kMaxTcK) return 0;
-    return (L + 15) / 16 * 16;
+    if (L < 2) return 0;
+    const int K = (L + 16) / 16 * 16;
+    return K <= kMaxTcK ? K : 0;
 }
 
 bool tc_packed_supported(int L, int b) {
     const int K = tc_k_for_len(L);
     if (!K || b < 1 || b > 4 || b * L > 128) return false;
-    if (b == 2) return K <= 64;
-    if (b == 3) return K <= 48;
-    if (b == 4) return K <= 32;
+    if (b == 2) return K <= 80;
+    if (b == 3 || b == 4) return K <= 48;
     return true;
 }
 
@@ -657,29 +654,21 @@ float tc_err_coef(int K) {
 }
 
 size_t build_twiddle_image(int L, int K, void* out) {
-    // B operand: 2K rows (hi rows 0..K-1, lo rows K..2K-1) x K columns
-    const int N = K, NT = 2 * K;
-    const size_t bytes = (size_t)NT * K * 2;
+    const size_t bytes = (size_t)2 * K * K * 2;
     if (!out) return bytes;
-    std::vector<uint16_t> img((size_t)NT * K, 0);
-    const int H = L / 2;
+    std::vector<uint16_t> img((size_t)2 * K * K, 0);
     const double two_pi = 6.283185307179586476925286766559;
-    for (int nrow = 0; nrow < N; ++nrow) {
-        const bool is_sin = nrow >= N / 2;
-        const int bin = (is_sin ? nrow - N / 2 : nrow) + 1;
-        if (bin > H) continue;
+    for (int nrow = 0; nrow < K; ++nrow) {
+        int bin = 0;
+        const int kind = tc_row_kind(nrow, L, K, &bin);
+        if (kind == 0) continue;
         for (int j = 0; j < L; ++j) {
             const int m = (int)(((long long)j * bin) % L);
-            const double w = is_sin ? std::sin(two_pi * m / L) : std::cos(two_pi * m / L);
+            const double w = kind == 3 ? 1.0 : kind == 2 ? std::sin(two_pi * m / L) : std::cos(two_pi * m / L);
             const uint16_t h = half_bits(w);
             const uint16_t l = half_bits(w - half_value(h));
-            // canonical no-swizzle K-major layout: core matrix (n/8, j/8) at
-            // (j/8) * (NT/8) * 128 + (n/8) * 128, row n%8 at +16, col j%8 at +2
-            for (int part = 0; part < 2; ++part) {
-                const int n = nrow + part * K;
-                const size_t byte = (size_t)(j / 8) * (NT / 8) * 128 + (size_t)(n / 8) * 128 + (n % 8) * 16 + (j % 8) * 2;
-                img[byte / 2] = part ? l : h;
-            }
+            img[tc_image_index(nrow, j, 0, K)] = h;
+            img[tc_image_index(nrow, j, 1, K)] = l;
         }
     }
     std::memcpy(out, img.data(), bytes);

@@ -92,7 +92,7 @@ int gp_debug_tc_trace(gp_ctx* ctx, int enable, uint64_t* out, int nout);
  * array (about 4.3 MB, held by every GPU that loads the library until the
  * process exits).  Limits and rules:
  *   - n <= 2^20 rows (GP_ERR_ARG beyond, with a message on stderr);
- *     2 <= L <= 128 (GP_ERR_UNSUPPORTED otherwise);
+ *     2 <= L <= 127 (GP_ERR_UNSUPPORTED otherwise);
  *   - the first call on a device looks up the array's device address there
  *     (with that device current); make it before any stream capture;
  *   - all calls share the array: calls that overlap on the GPU race;
@@ -174,6 +174,14 @@ typedef struct gp_batch_config {
  * per process. */
 int gp_generate_batch(gp_ctx* ctx, const gp_gen_job* jobs, int njobs, int autotune, gp_batch_config* cfg,
                       gp_gen_stats* stats);
+
+/* The settings the tuners chose so far on this context, one line per tuned
+ * workload: "batch:<jobs> enum_variant windows_per_thread cand_cap
+ * tc_ctas_per_sm use_graph" for gp_generate_batch, "sort:W<words> radix_bits
+ * microseconds" for gp_sort (which tunes its radix width per key width on
+ * first use).  Writes at most cap bytes (NUL-terminated) to buf; returns the
+ * length needed including the NUL.  No counterpart in the reference. */
+int gp_tuned_settings(const gp_ctx* ctx, char* buf, int cap);
 
 /*
  * Replaces GNU_sort(const std::vector<std::string>& in, const std::string& out,
