@@ -280,11 +280,16 @@ static gp::RowSrc int8_src(const int8_t* d, int L) {
     return r;
 }
 
-static int64_t popcount_words(const uint32_t* w, int64_t nwords) {
-    int64_t s = 0;
-    for (int64_t i = 0; i < nwords; ++i) s += __builtin_popcount(w[i]);
-    return s;
+// *out += number of set bits in w[0 .. nwords)
+__global__ void popcount_add_kernel(const uint32_t* w, int64_t nwords, unsigned long long* out) {
+    unsigned long long s = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += (int64_t)gridDim.x * blockDim.x)
+        s += (unsigned long long)__popc(w[i]);
+    for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
 }
+
+constexpr int kPassCountSlot = 40;  // counts[]: passes of the current gp_psd_filter call
 
 static int check_args(gp_ctx* c, int64_t n, int L, int mode) {
     if (!c) return GP_ERR_ARG;
@@ -310,6 +315,7 @@ int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, in
     auto* d_counts = c->counts.as<unsigned long long>();
     auto* h_counts = c->h_counts.as<unsigned long long>();
     const int64_t nchunks = (n + chunk - 1) / chunk;
+    if (stats) GP_CUDA_TRY(c, cudaMemsetAsync(d_counts + kPassCountSlot, 0, sizeof(unsigned long long), c->s_comp));
     int64_t unsure_total = 0;
     for (int64_t ci = 0; ci < nchunks; ++ci) {
         const int b = (int)(ci & 1);
@@ -335,6 +341,13 @@ int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, in
         if (rc) return rc;
         GP_CUDA_TRY(c, cudaMemcpyAsync(pass_mask + r0 / 32, c->mask_buf[b].p, (size_t)(rows + 31) / 32 * 4,
                                        cudaMemcpyDeviceToHost, c->s_comp));
+        if (stats) {
+            const int64_t words = (rows + 31) / 32;
+            const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((words + 255) / 256, (int64_t)c->num_sms * 4));
+            popcount_add_kernel<<<(unsigned)blocks, 256, 0, c->s_comp>>>(c->mask_buf[b].as<uint32_t>(), words,
+                                                                         d_counts + kPassCountSlot);
+            GP_CUDA_TRY(c, cudaGetLastError());
+        }
         if (mode == GP_PSD_TC_GUARDED)
             GP_CUDA_TRY(c, cudaMemcpyAsync(h_counts + 2 + ci % 62, d_counts + b, sizeof(unsigned long long),
                                            cudaMemcpyDeviceToHost, c->s_comp));
@@ -351,8 +364,10 @@ int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, in
     rc = c->check_status("gp_psd_filter");
     if (rc) return rc;
     if (stats) {
+        unsigned long long passes = 0;
+        GP_CUDA_TRY(c, cudaMemcpy(&passes, d_counts + kPassCountSlot, sizeof passes, cudaMemcpyDeviceToHost));
         stats->n = n;
-        stats->n_pass = popcount_words(pass_mask, (n + 31) / 32);
+        stats->n_pass = (int64_t)passes;
         stats->n_unsure = unsure_total;
         stats->guard = guard_band(order);
         stats->err_coef = mode == GP_PSD_TC_GUARDED ? gp::tc_err_coef(gp::tc_k_for_len(L)) : 0.f;
@@ -376,12 +391,18 @@ int gp_psd_filter_device(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int 
         GP_CUDA_TRY(c, cudaStreamSynchronize(st));
         rc = c->check_status("gp_psd_filter_device");
         if (rc) return rc;
-        std::vector<uint32_t> m((size_t)(n + 31) / 32);
-        GP_CUDA_TRY(c, cudaMemcpy(m.data(), d_mask, m.size() * 4, cudaMemcpyDeviceToHost));
-        unsigned long long u = 0;
+        unsigned long long* pc = c->counts.as<unsigned long long>() + kPassCountSlot;
+        GP_CUDA_TRY(c, cudaMemsetAsync(pc, 0, sizeof(unsigned long long), st));
+        const int64_t words = (n + 31) / 32;
+        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((words + 255) / 256, (int64_t)c->num_sms * 4));
+        popcount_add_kernel<<<(unsigned)blocks, 256, 0, st>>>(d_mask, words, pc);
+        GP_CUDA_TRY(c, cudaGetLastError());
+        unsigned long long u = 0, passes = 0;
+        GP_CUDA_TRY(c, cudaMemcpyAsync(&passes, pc, sizeof passes, cudaMemcpyDeviceToHost, st));
+        GP_CUDA_TRY(c, cudaStreamSynchronize(st));
         GP_CUDA_TRY(c, cudaMemcpy(&u, c->counts.p, sizeof u, cudaMemcpyDeviceToHost));
         stats->n = n;
-        stats->n_pass = popcount_words(m.data(), (int64_t)m.size());
+        stats->n_pass = (int64_t)passes;
         stats->n_unsure = mode == GP_PSD_TC_GUARDED ? (int64_t)u : 0;
         stats->guard = guard_band(order);
         stats->err_coef = mode == GP_PSD_TC_GUARDED ? gp::tc_err_coef(gp::tc_k_for_len(L)) : 0.f;

@@ -181,7 +181,27 @@ __device__ __forceinline__ void packed_row(const uint32_t (&w)[4], const uint8_t
 }
 
 // B = 0: int8 rows; B = 1..4: packed words with B bits per digit.
-template <int K, int B, bool WRITE_PSD>
+// Cycle counter for the per-role diagnostics; compiled out when TR is false.
+template <bool TR>
+__device__ __forceinline__ long long tclock() {
+    if constexpr (TR) return clock64();
+    return 0;
+}
+
+// Stage index and phase parity of a ring of S stages, advanced once per tile.
+struct Ring {
+    int slot = 0;
+    uint32_t phase = 0;
+    __device__ __forceinline__ void next(int S) {
+        if (++slot == S) {
+            slot = 0;
+            phase ^= 1u;
+        }
+    }
+};
+
+// TR: per-role cycle counters (diagnostics build of the kernel).
+template <int K, int B, bool WRITE_PSD, bool TR>
 __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(PsdTcArgs a, SmemLayout lay) {
     using C = TcCfg<K>;
     extern __shared__ uint8_t smem_raw_base[];
@@ -251,18 +271,19 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         const int r = threadIdx.x;  // row of the tile = TMEM lane
         const int norm = 128 - B * L;  // packed: left shift that puts digit 0 at bit 127
         const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16) + (uint32_t)C::A_COL0;
-        int64_t it = 0;
+        int it = 0;
+        Ring raw, ast;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
-        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
-            const int rs = (int)(it % RS);
-            const uint32_t rph = (uint32_t)((it / RS) & 1);
-            const int as = (int)(it % C::AS);
-            const uint32_t aph = (uint32_t)((it / C::AS) & 1);
-            const long long c0t = clock64();
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it, raw.next(RS), ast.next(C::AS)) {
+            const int rs = raw.slot;
+            const uint32_t rph = raw.phase;
+            const int as = ast.slot;
+            const uint32_t aph = ast.phase;
+            const long long c0t = tclock<TR>();
             if (!mbar_wait(&raw_full[rs], rph, abort_flag, a.status, 1)) break;
-            const long long c1t = clock64();
+            const long long c1t = tclock<TR>();
             if (!mbar_wait(&a_empty[as], aph ^ 1u, abort_flag, a.status, 2)) break;
-            const long long c2t = clock64();
+            const long long c2t = tclock<TR>();
             tr0 += c1t - c0t;
             tr1 += c2t - c1t;
             tc_fence_after();
@@ -328,7 +349,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const uint32_t aaddr = lane_base + (uint32_t)(as * (K / 2));
 #pragma unroll
             for (int g = 0; g < K / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
-            const long long c3t = clock64();
+            const long long c3t = tclock<TR>();
             tr3 += c3t - c2t;
             tmem_wait_st();
             tc_fence_before();
@@ -337,7 +358,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 mbar_arrive(&a_full[as]);
                 mbar_arrive(&raw_empty[rs]);
             }
-            tr2 += clock64() - c2t;
+            tr2 += tclock<TR>() - c2t;
         }
         if (a.trace && lane == 0) {
             atomicAdd(&a.trace[kTrConvWaitRaw], tr0);
@@ -355,14 +376,14 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         const float d_const = a.err_coef * (float)L * (float)a.alpha_c;
         const float g_const = fmaxf(a.guard_cfg, 2.f * sq * d_const + 3.f * d_const * d_const + 1e-4f);
         constexpr int HB = K / 2;  // bins per half (cos block then sin block)
-        int64_t it = 0;
+        Ring acc;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0;
-        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
-            const int b = (int)(it % C::NACC);
-            const uint32_t ph = (uint32_t)((it / C::NACC) & 1);
-            const long long c0t = clock64();
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
+            const int b = acc.slot;
+            const uint32_t ph = acc.phase;
+            const long long c0t = tclock<TR>();
             if (!mbar_wait(&acc_full[b], ph, abort_flag, a.status, 3)) break;
-            const long long c1t = clock64();
+            const long long c1t = tclock<TR>();
             tr0 += c1t - c0t;
             tc_fence_after();
             const int r = q * 32 + lane;
@@ -429,7 +450,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
                 }
             }
-            tr2 += clock64() - c1t;
+            tr2 += tclock<TR>() - c1t;
         }
         if (a.trace && lane == 0) {
             atomicAdd(&a.trace[kTrEpiWaitAcc], tr0);
@@ -445,12 +466,13 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const uint8_t* src = B == 0 ? reinterpret_cast<const uint8_t*>(a.seqs)
                                         : reinterpret_cast<const uint8_t*>(a.words);
             unsigned long long tr0 = 0, tr1 = 0;
-            for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
-                const int rs = (int)(it % RS);
-                const uint32_t ph = (uint32_t)((it / RS) & 1);
-                const long long c0 = clock64();
+            Ring raw;
+            for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it, raw.next(RS)) {
+                const int rs = raw.slot;
+                const uint32_t ph = raw.phase;
+                const long long c0 = tclock<TR>();
                 if (!mbar_wait(&raw_empty[rs], ph ^ 1u, abort_flag, a.status, 4)) break;
-                const long long c1 = clock64();
+                const long long c1 = tclock<TR>();
                 tr0 += c1 - c0;
                 const bool full_tile = aligned && (t + 1) * kTileM <= n;
                 if (full_tile) {
@@ -460,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 } else {
                     mbar_arrive(&raw_full[rs]);
                 }
-                tr1 += clock64() - c1;
+                tr1 += tclock<TR>() - c1;
             }
             if (a.trace) {
                 atomicAdd(&a.trace[kTrProdWait], tr0);
@@ -497,18 +519,18 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             // field (bits 0-13, address >> 4)
             const uint64_t bdesc0 = sdesc_noswizzle(smem_u32(sB), C::B_KSTRIDE, 128);
             bool ok = mbar_wait(b_full, 0, abort_flag, a.status, 5);
-            int64_t it = 0;
+            Ring ast, acc;
             unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
-            for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++it) {
-                const int as = (int)(it % C::AS);
-                const uint32_t aph = (uint32_t)((it / C::AS) & 1);
-                const int b = (int)(it % C::NACC);
-                const uint32_t bph = (uint32_t)((it / C::NACC) & 1);
-                const long long c0 = clock64();
+            for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ast.next(C::AS), acc.next(C::NACC)) {
+                const int as = ast.slot;
+                const uint32_t aph = ast.phase;
+                const int b = acc.slot;
+                const uint32_t bph = acc.phase;
+                const long long c0 = tclock<TR>();
                 if (!mbar_wait(&a_full[as], aph, abort_flag, a.status, 6)) break;
-                const long long c1 = clock64();
+                const long long c1 = tclock<TR>();
                 if (!mbar_wait(&acc_empty[b], bph ^ 1u, abort_flag, a.status, 9)) break;
-                const long long c2 = clock64();
+                const long long c2 = tclock<TR>();
                 tr0 += c1 - c0;
                 tr1 += c2 - c1;
                 tc_fence_after();
@@ -523,10 +545,10 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         umma_f16_ts(d, a0 + (uint32_t)(8 * ks),
                                     bdesc0 + (uint64_t)(((pass * (K / 8) + 2 * ks) * C::B_KSTRIDE) >> 4), idesc,
                                     (pass | ks) != 0 ? 1u : 0u);
-                const long long c3 = clock64();
+                const long long c3 = tclock<TR>();
                 umma_commit(&a_empty[as]);
                 umma_commit(&acc_full[b]);
-                const long long c4 = clock64();
+                const long long c4 = tclock<TR>();
                 tr2 += c3 - c2;
                 tr3 += c4 - c3;
             }
@@ -561,7 +583,10 @@ cudaError_t launch_kb(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
     const SmemLayout lay = smem_layout<K>(B == 0 ? a.L : 16);
     const int64_t ntiles = (a.n + kTileM - 1) / kTileM;
     if (ntiles == 0) return cudaSuccess;
-    auto kern = psd_tc_kernel<K, B, WP>;
+    // the counting variant exists for the int8 input only (diagnostics)
+    auto kern = psd_tc_kernel<K, B, WP, false>;
+    if constexpr (B == 0 && !WP)
+        if (a.trace) kern = psd_tc_kernel<K, B, WP, true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
     if (e != cudaSuccess) return e;
     const int per_sm = a.grid_per_sm > 0 && a.grid_per_sm < C::MIN_BLOCKS ? a.grid_per_sm : C::MIN_BLOCKS;
