@@ -15,6 +15,7 @@ Boost headers) into oracle/_ref/golay_ref, runs it under LC_ALL=C, and stores:
 Needs the reference sources; run in the build container only:
     python tests/golden/make_golden.py            # everything
     python tests/golden/make_golden.py --windows  # only the window goldens
+    python tests/golden/make_golden.py --run=NAME # only the named run (merged)
 """
 import hashlib
 import json
@@ -41,7 +42,20 @@ RUNS = [
     ("n34", ["34", "-c", "2", "gen"], ["34-filtered-a#0", "34-filtered-b#0"], False),
     ("n57_shard7of1000", ["57", "-c", "3", "1", "--paf", "-2", "-n", "1000", "-j", "7", "gen"],
      ["57-filtered-a#7", "57-filtered-b#7"], False),
+    # a three-level chain: generation at compression 4, uncompression 4 -> 2 -> 1
+    ("n32_c421", ["32", "-c", "4", "2", "1", "gen", "sort", "match", "uncompress"],
+     ["32-filtered-a#0", "32-filtered-b#0", "32-filtered_sorted-a", "32-filtered_sorted-b", "32-pairs-4",
+      "32-pairs-2", "32-pairs-1"], False),
 ]
+SUBCOMMANDS = {"gen", "sort", "match", "uncompress", "filter", "all"}
+
+
+def split_argv(args):
+    """(options and positionals, subcommands): --dir goes between them."""
+    i = len(args)
+    while i > 0 and args[i - 1] in SUBCOMMANDS:
+        i -= 1
+    return args[:i], args[i:]
 
 
 def sha256(path):
@@ -89,11 +103,19 @@ def main():
         print("window goldens written")
         return
     env = dict(os.environ, LC_ALL="C")
-    manifest = {"generator": "reference sources built by oracle/build_ref.sh, LC_ALL=C", "runs": {}}
+    only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--run=")]
+    if only:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest = json.load(f)
+    else:
+        manifest = {"generator": "reference sources built by oracle/build_ref.sh, LC_ALL=C", "runs": {}}
     with tempfile.TemporaryDirectory() as tmp:
         for name, args, files, keep in RUNS:
+            if only and name not in only:
+                continue
             d = os.path.join(tmp, name)
-            subprocess.run([REF_BIN] + args[:-1] + ["--dir", d, args[-1]], check=True, env=env,
+            opts, subs = split_argv(args)
+            subprocess.run([REF_BIN] + opts + ["--dir", d] + subs, check=True, env=env,
                            stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
             order = args[0]
             wd = os.path.join(d, f"order-{order}")
@@ -107,7 +129,8 @@ def main():
                     os.makedirs(os.path.join(HERE, name), exist_ok=True)
                     shutil.copy(p, os.path.join(HERE, name, fn.replace("#", "_")))
             manifest["runs"][name] = rec
-    make_windows(manifest)
+    if not only:
+        make_windows(manifest)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
     print("golden fixtures written")

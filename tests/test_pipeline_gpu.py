@@ -20,9 +20,17 @@ pytestmark = pytest.mark.gpu
 ENV = dict(os.environ, LC_ALL="C")
 
 
+SUBCOMMANDS = {"gen", "sort", "match", "uncompress", "filter", "all"}
+
+
 def golay(args, tmp, check=True):
+    """Runs the golay driver with --dir between the options and the trailing
+    subcommands (global options precede subcommands)."""
     d = str(tmp)
-    argv = [gp.CLI_PATH] + args[:-1] + ["--dir", d, args[-1]]
+    i = len(args)
+    while i > 0 and args[i - 1] in SUBCOMMANDS:
+        i -= 1
+    argv = [gp.CLI_PATH] + args[:i] + ["--dir", d] + args[i:]
     r = subprocess.run(argv, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=ENV)
     if check:
         assert r.returncode == 0, r.stderr + r.stdout
@@ -39,8 +47,10 @@ def test_all_matches_reference(tmp_path, golden_manifest, name):
         assert got == want, fn
 
 
-@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000"])
+@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000", "n32_c421"])
 def test_gen_matches_reference_hash(tmp_path, golden_manifest, name):
+    """Hashes of the reference's own outputs; n32_c421 runs generation at
+    compression 4 and uncompresses 4 -> 2 -> 1 (90,320 pairs at length 32)."""
     rec = golden_manifest["runs"][name]
     r, wd = golay(rec["argv"], tmp_path)
     for fn, meta in rec["files"].items():
