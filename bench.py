@@ -402,6 +402,8 @@ def run_pipeline(args):
                           "per_job": [dict(order=w[0], compress=w[1], written=s.written_a + s.written_b,
                                            necklaces=s.necklaces, candidates=s.candidates, psd_pass=s.psd_pass,
                                            unsure=s.unsure) for w, s in zip(wins, stats)]}), flush=True)
+        if args.pipeline_only == "batch":
+            return 0
         # the same windows one order per call, for comparison
         for order, comp, paf, lo, hi in wins:
             st, el = gen_window(order, comp, paf, lo, hi)
@@ -449,6 +451,8 @@ def main():
     ap.add_argument("--trace", action="store_true", help="with --profile: per-role cycle counters")
     ap.add_argument("--pipeline", action="store_true", help="time the generation configurations instead")
     ap.add_argument("--pipeline-pairs", type=int, default=200, help="compressed pairs to uncompress (--pipeline)")
+    ap.add_argument("--pipeline-only", choices=["all", "batch"], default="all",
+                    help="--pipeline: everything, or only the uneven batch in one engine run")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

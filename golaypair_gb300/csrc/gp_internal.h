@@ -55,14 +55,14 @@ size_t build_twiddle_image(int L, int K, void* out);
 int tc_k_for_len(int L);               // padded K (multiple of 16, > L), or 0 if unsupported
 
 // Where twiddle row `nrow` (0..K-1), column j (0..K-1), part (0 hi, 1 lo)
-// sits in the B image, as an index of fp16 elements.  The image is a K x 2K
-// fp16 matrix (hi part at column j, lo part at column K + j) in the
+// sits in the B image, as an index of fp16 elements.  The image is a 2K x K
+// fp16 matrix (hi part at row nrow, lo part at row K + nrow) in the
 // canonical no-swizzle K-major layout of 8 x 8 core matrices: core matrix
-// (n/8, col/8) at byte (col/8) * (K/8) * 128 + (n/8) * 128, row n%8 at +16,
-// column col%8 at +2.
+// (n/8, j/8) at byte (j/8) * (2K/8) * 128 + (n/8) * 128, row n%8 at +16,
+// column j%8 at +2.
 __host__ __device__ inline size_t tc_image_index(int nrow, int j, int part, int K) {
-    const int col = j + part * K;
-    return ((size_t)(col / 8) * (K / 8) * 128 + (size_t)(nrow / 8) * 128 + (size_t)(nrow % 8) * 16 + (col % 8) * 2) / 2;
+    const int n = nrow + part * K;
+    return ((size_t)(j / 8) * (2 * K / 8) * 128 + (size_t)(n / 8) * 128 + (size_t)(n % 8) * 16 + (j % 8) * 2) / 2;
 }
 
 // Bin of twiddle row nrow: cosine rows 0..K/2-1 are bins 1..K/2, sine rows
