@@ -385,11 +385,16 @@ def run_pipeline(args):
         # cached in the context), then the timed run with the tuned settings
         spec = [(o, c, p, lo, hi, os.path.join(tmp, f"{o}a"), os.path.join(tmp, f"{o}b"))
                 for (o, c, p, lo, hi) in wins]
+        # --pipeline-no-graph: default settings with direct launches (for
+        # per-kernel profiling, which does not follow graph replays)
+        direct = gp.BatchConfig()
+        direct.no_graph = 1
+        tune = not args.pipeline_no_graph
         t0 = time.perf_counter()
-        _, cfg = ctx.generate_batch(spec, autotune=True)
+        _, cfg = ctx.generate_batch(spec, autotune=tune, config=None if tune else direct)
         tune_el = time.perf_counter() - t0
         t0 = time.perf_counter()
-        stats, cfg = ctx.generate_batch(spec, autotune=True)
+        stats, cfg = ctx.generate_batch(spec, autotune=tune, config=None if tune else direct)
         el = time.perf_counter() - t0
         tot_n = sum(s.necklaces for s in stats)
         tot_c = sum(s.candidates for s in stats)
@@ -453,6 +458,8 @@ def main():
     ap.add_argument("--pipeline-pairs", type=int, default=200, help="compressed pairs to uncompress (--pipeline)")
     ap.add_argument("--pipeline-only", choices=["all", "batch"], default="all",
                     help="--pipeline: everything, or only the uneven batch in one engine run")
+    ap.add_argument("--pipeline-no-graph", action="store_true",
+                    help="--pipeline: run the batch engine with direct launches and default settings")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ctx.h"
@@ -24,9 +25,12 @@
 
 namespace {
 
-struct Record {
-    gp::u128 word;
-    std::vector<uint16_t> sig;
+// Survivor records of one role: packed words and their (L-1) signature
+// values, in flat arrays.
+struct RecordSet {
+    std::vector<gp::u128> words;
+    std::vector<uint16_t> sigs;
+    size_t size() const { return words.size(); }
 };
 
 struct GenPlan {
@@ -66,21 +70,44 @@ void format_line(std::string& out, const GenPlan& p, gp::u128 word, const uint16
     out.push_back('\n');
 }
 
-int write_records(gp_ctx* c, const GenPlan& p, std::vector<Record>& recs, const char* path) {
-    std::sort(recs.begin(), recs.end(), [](const Record& x, const Record& y) { return x.word < y.word; });
+// Writes the records in word order (the reference's FKM order).  Lines
+// are formatted by several host threads into per-thread buffers, then
+// written in order.
+int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, const char* path) {
+    const size_t n = recs.size();
+    const int S = p.L - 1;
+    std::vector<uint32_t> order(n);
+    for (size_t i = 0; i < n; ++i) order[i] = (uint32_t)i;
+    std::sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return recs.words[x] < recs.words[y]; });
     FILE* f = fopen(path, "w");
     if (!f) return c->fail(GP_ERR_IO, "cannot open %s for writing", path);
-    std::string buf;
-    buf.reserve(1 << 20);
-    for (const Record& r : recs) {
-        format_line(buf, p, r.word, r.sig.data());
-        if (buf.size() > (1u << 20)) {
-            fwrite(buf.data(), 1, buf.size(), f);
-            buf.clear();
+    const size_t per_block = 1 << 16;  // lines per formatting task
+    const size_t nblocks = (n + per_block - 1) / per_block;
+    unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (nblocks < nthreads) nthreads = (unsigned)std::max<size_t>(1, nblocks);
+    bool ok = true;
+    // rounds of nthreads blocks: format in parallel, write in order
+    std::vector<std::string> bufs(nthreads);
+    for (size_t b0 = 0; b0 < nblocks && ok; b0 += nthreads) {
+        const unsigned m = (unsigned)std::min<size_t>(nthreads, nblocks - b0);
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < m; ++t) {
+            th.emplace_back([&, t] {
+                std::string& out = bufs[t];
+                out.clear();
+                const size_t lo = (b0 + t) * per_block, hi = std::min(n, lo + per_block);
+                out.reserve((hi - lo) * (size_t)(4 * p.L + 8));
+                for (size_t i = lo; i < hi; ++i) {
+                    const uint32_t r = order[i];
+                    format_line(out, p, recs.words[r], recs.sigs.data() + (size_t)r * S);
+                }
+            });
         }
+        for (auto& x : th) x.join();
+        for (unsigned t = 0; t < m; ++t)
+            if (fwrite(bufs[t].data(), 1, bufs[t].size(), f) != bufs[t].size()) ok = false;
     }
-    fwrite(buf.data(), 1, buf.size(), f);
-    const bool ok = fclose(f) == 0;
+    ok = (fclose(f) == 0) && ok;
     return ok ? GP_OK : c->fail(GP_ERR_IO, "write failed: %s", path);
 }
 
@@ -125,7 +152,7 @@ struct JobRun {
     int64_t soft = 0, hard = 0, rcap = 0, rec_bytes = 0;
     size_t off_words = 0, off_roles = 0, off_mask = 0, off_unsure = 0, off_idx = 0, off_rec = 0, off_units = 0;
     std::vector<int16_t> units;
-    std::vector<Record> ra, rb;
+    RecordSet ra, rb;
     gp_gen_stats st{};
 };
 
@@ -154,10 +181,9 @@ int drain_records(gp_ctx* c, JobRun& j, uint8_t* arena, int64_t nrec) {
     GP_CUDA_TRY(c, cudaMemcpy(ro.data(), rb + (size_t)rcap * 16, nrec, cudaMemcpyDeviceToHost));
     GP_CUDA_TRY(c, cudaMemcpy(sg.data(), rb + align_up((size_t)rcap * 17, 16), sg.size() * 2, cudaMemcpyDeviceToHost));
     for (int64_t i = 0; i < nrec; ++i) {
-        Record r;
-        r.word = ((gp::u128)w[i].w << 96) | ((gp::u128)w[i].z << 64) | ((gp::u128)w[i].y << 32) | w[i].x;
-        r.sig.assign(sg.begin() + i * (L - 1), sg.begin() + (i + 1) * (L - 1));
-        (ro[i] == 1 ? j.ra : j.rb).push_back(std::move(r));
+        RecordSet& rs = ro[i] == 1 ? j.ra : j.rb;
+        rs.words.push_back(((gp::u128)w[i].w << 96) | ((gp::u128)w[i].z << 64) | ((gp::u128)w[i].y << 32) | w[i].x);
+        rs.sigs.insert(rs.sigs.end(), sg.begin() + i * (L - 1), sg.begin() + (i + 1) * (L - 1));
     }
     return GP_OK;
 }
@@ -523,7 +549,7 @@ int plan_for(gp_ctx* c, int order, int compress, int paf, GenPlan& p) {
     return GP_OK;
 }
 
-int finish(gp_ctx* c, const GenPlan& p, std::vector<Record>& ra, std::vector<Record>& rb, const char* path_a,
+int finish(gp_ctx* c, const GenPlan& p, const RecordSet& ra, const RecordSet& rb, const char* path_a,
            const char* path_b, gp_gen_stats* st) {
     int rc = write_records(c, p, ra, path_a);
     if (rc) return rc;
