@@ -95,6 +95,9 @@ _STAGE_SIGS = {
     "gp_generate": [_P, _i32, _i32, _i32, _i32, _i32, _cp, _cp, _P],
     "gp_generate_window": [_P, _i32, _i32, _i32, _u64, _u64, _u64, _u64, _cp, _cp, _P],
     "gp_generate_batch": [_P, _P, _i32, _i32, _P, _P],
+    "gp_generate_resumable": [_P, _i32, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _i32, ctypes.c_double, _P, _P],
+    "gp_generate_window_resumable": [_P, _i32, _i32, _i32, _u64, _u64, _u64, _u64, _cp, _cp, _cp, _i32,
+                                     ctypes.c_double, _P, _P],
     "gp_tuned_settings": [_P, _P, _i32],
     "gp_sort": [_P, _P, _i32, _cp],
     "gp_match": [_P, _i32, _i32, _i32, _cp, _cp, _cp, _i32, _P],
@@ -185,6 +188,18 @@ class Context:
                                                 end & m, str(path_a).encode(), str(path_b).encode(),
                                                 ctypes.byref(st)), "gp_generate_window")
         return st
+
+    def generate_window_resumable(self, order, compress, paf, begin, end, path_a, path_b, checkpoint,
+                                  max_iterations=0, max_seconds=0.0):
+        """gp_generate_window_resumable; returns (done, GenStats)."""
+        st = GenStats()
+        done = ctypes.c_int(0)
+        m = (1 << 64) - 1
+        self.check(self._lib.gp_generate_window_resumable(
+            self._h, order, compress, paf, begin >> 64, begin & m, end >> 64, end & m, str(path_a).encode(),
+            str(path_b).encode(), str(checkpoint).encode(), max_iterations, float(max_seconds), ctypes.byref(done),
+            ctypes.byref(st)), "gp_generate_window_resumable")
+        return bool(done.value), st
 
     def generate_batch(self, jobs, autotune=False, config=None):
         """gp_generate_batch.  jobs: (order, compress, paf, begin, end,

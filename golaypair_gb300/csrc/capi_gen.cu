@@ -154,6 +154,19 @@ struct JobRun {
     std::vector<int16_t> units;
     RecordSet ra, rb;
     gp_gen_stats st{};
+    // set when the engine stopped early: the word ranks still to search
+    std::vector<std::pair<gp::u128, gp::u128>> remaining;
+};
+
+// Early stop of the engine (checkpointed searches): after an iteration that
+// reaches max_iterations (> 0) or max_seconds (> 0) with windows left, the
+// engine drains its records, stores each job's unfinished rank ranges in
+// JobRun::remaining and returns with stopped = true.
+struct StopCtl {
+    int max_iterations = 0;
+    double max_seconds = 0;
+    std::chrono::steady_clock::time_point start = std::chrono::steady_clock::now();
+    bool stopped = false;
 };
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -194,7 +207,7 @@ int64_t rec_region_bytes(int64_t rcap, int L) {
 
 // Runs the batch engine over the jobs' ranges; records land in the jobs'
 // A/B lists, counts in their stats.
-int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* iterations) {
+int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* iterations, StopCtl* stop = nullptr) {
     const int nj = (int)jobs.size();
     if (nj < 1 || nj > gp::kMaxEnumJobs) return c->fail(GP_ERR_ARG, "batch of %d jobs (1..%d)", nj, gp::kMaxEnumJobs);
     cudaStream_t s = c->s_comp;
@@ -433,6 +446,28 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
         // unfinished iteration appends candidates
         stalled = added ? 0 : stalled + 1;
         if (stalled > 2) return c->fail(GP_ERR_CUDA, "batch generation: no progress");
+        if (stop && ((stop->max_iterations > 0 && iters >= stop->max_iterations) ||
+                     (stop->max_seconds > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() -
+                                                                             stop->start).count() >= stop->max_seconds))) {
+            // unfinished windows hold the next word to visit (a finished
+            // window holds its end): [rank(cur), rank(end)) is still to do
+            std::vector<uint4> hcur(nwin);
+            GP_CUDA_TRY(c, cudaMemcpy(hcur.data(), A + off_cur, (size_t)nwin * 16, cudaMemcpyDeviceToHost));
+            auto from_u4 = [](uint4 v) {
+                return ((gp::u128)v.w << 96) | ((gp::u128)v.z << 64) | ((gp::u128)v.y << 32) | v.x;
+            };
+            for (auto& j : jobs) j.remaining.clear();
+            for (int64_t w = 0; w < nwin; ++w) {
+                const gp::u128 cw = from_u4(hcur[w]), ew = from_u4(end[w]);
+                if (cw == ew) continue;
+                JobRun& j = jobs[wjob[w]];
+                const gp::u128 lo = gp::word_to_rank(cw, j.p.k, j.p.b, j.p.L);
+                const gp::u128 hi = gp::word_to_rank(ew, j.p.k, j.p.b, j.p.L);
+                if (lo < hi) j.remaining.emplace_back(lo, hi);
+            }
+            stop->stopped = true;
+            break;
+        }
     }
     GP_CUDA_TRY(c, cudaStreamSynchronize(s));
     for (int ji = 0; ji < nj; ++ji) {
@@ -560,6 +595,169 @@ int finish(gp_ctx* c, const GenPlan& p, const RecordSet& ra, const RecordSet& rb
     return GP_OK;
 }
 
+// Job split of src/utils/lyndon.cpp:93-106: prenecklace prefixes of the
+// first length i with at least proc_num * 10000 necklaces, dealt out round
+// robin (1-based count), each covering the words that extend it.
+std::vector<std::pair<gp::u128, gp::u128>> shard_ranges(const GenPlan& p, int proc_id, int proc_num) {
+    const int L = p.L, k = p.k;
+    std::vector<std::pair<gp::u128, gp::u128>> ranges;
+    int i = 1;
+    for (; i <= L; ++i)
+        if (gp::necklace_count(i, k) >= (gp::u128)proc_num * 10000) break;
+    if (proc_num > 1 && i < L) {
+        const gp::u128 span = gp::upow(k, L - i);
+        int64_t count = 0;
+        gp::prenecklaces(i, k, [&](const std::vector<int>& pre, int) {
+            ++count;
+            if (count % proc_num != proc_id) return;
+            gp::u128 r = 0;
+            for (int d : pre) r = r * (gp::u128)k + (gp::u128)d;
+            ranges.emplace_back(r * span, (r + 1) * span);
+        });
+    } else {
+        ranges.emplace_back(0, gp::upow(k, L));
+    }
+    return ranges;
+}
+
+// ------------------------------------------------------------ checkpoints
+//
+// A checkpoint holds a generation stopped part way: the job, its counts so
+// far, the word-rank ranges still to search and the survivor records found
+// so far.  Binary, host byte order:
+//   "GPCK0001"
+//   int32 order, compress, paf, L; uint32 n; n bytes: the job ("shard i n"
+//   or "window lo hi")
+//   int64 necklaces, candidates, psd_pass, unsure
+//   uint64 ranges; per range: lo, hi as (low, high) uint64 pairs
+//   A then B: uint64 records; the words as (low, high) uint64 pairs; then
+//   (L - 1) uint16 signature values per record
+// It is written to "<path>.tmp" and renamed over <path>, so a crash leaves
+// the previous checkpoint intact.
+const char kCkptMagic[8] = {'G', 'P', 'C', 'K', '0', '0', '0', '1'};
+
+std::string u128_dec(gp::u128 v) {
+    std::string s;
+    do {
+        s.push_back((char)('0' + (int)(v % 10)));
+        v /= 10;
+    } while (v);
+    return std::string(s.rbegin(), s.rend());
+}
+
+template <typename T>
+bool put(FILE* f, const T& v) { return fwrite(&v, sizeof v, 1, f) == 1; }
+template <typename T>
+bool get(FILE* f, T& v) { return fread(&v, sizeof v, 1, f) == 1; }
+
+bool put_u128(FILE* f, gp::u128 v) { return put(f, (uint64_t)v) && put(f, (uint64_t)(v >> 64)); }
+bool get_u128(FILE* f, gp::u128& v) {
+    uint64_t lo = 0, hi = 0;
+    if (!get(f, lo) || !get(f, hi)) return false;
+    v = ((gp::u128)hi << 64) | lo;
+    return true;
+}
+
+int save_checkpoint(gp_ctx* c, const char* path, const GenPlan& p, const std::string& spec, const JobRun& j) {
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE* f = fopen(tmp.c_str(), "wb");
+    if (!f) return c->fail(GP_ERR_IO, "cannot write checkpoint %s", tmp.c_str());
+    bool ok = fwrite(kCkptMagic, 1, 8, f) == 8;
+    ok = ok && put(f, (int32_t)p.order) && put(f, (int32_t)p.compress) && put(f, (int32_t)p.paf) &&
+         put(f, (int32_t)p.L) && put(f, (uint32_t)spec.size()) && fwrite(spec.data(), 1, spec.size(), f) == spec.size();
+    ok = ok && put(f, j.st.necklaces) && put(f, j.st.candidates) && put(f, j.st.psd_pass) && put(f, j.st.unsure);
+    ok = ok && put(f, (uint64_t)j.remaining.size());
+    for (auto& r : j.remaining) ok = ok && put_u128(f, r.first) && put_u128(f, r.second);
+    for (const RecordSet* rs : {&j.ra, &j.rb}) {
+        ok = ok && put(f, (uint64_t)rs->size());
+        for (gp::u128 w : rs->words) ok = ok && put_u128(f, w);
+        ok = ok && fwrite(rs->sigs.data(), 2, rs->sigs.size(), f) == rs->sigs.size();
+    }
+    ok = (fclose(f) == 0) && ok;
+    if (!ok || rename(tmp.c_str(), path) != 0) return c->fail(GP_ERR_IO, "cannot write checkpoint %s", path);
+    return GP_OK;
+}
+
+// Loads a checkpoint into j (ranges, records, counts).  GP_ERR_FORMAT when
+// the file is damaged or belongs to another job.
+int load_checkpoint(gp_ctx* c, const char* path, const GenPlan& p, const std::string& spec, JobRun& j) {
+    FILE* f = fopen(path, "rb");
+    if (!f) return c->fail(GP_ERR_IO, "cannot read checkpoint %s", path);
+    char magic[8];
+    int32_t order = 0, compress = 0, paf = 0, L = 0;
+    uint32_t n = 0;
+    bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, kCkptMagic, 8) == 0;
+    ok = ok && get(f, order) && get(f, compress) && get(f, paf) && get(f, L) && get(f, n) && n < 4096;
+    std::string got(ok ? n : 0, '\0');
+    ok = ok && fread(&got[0], 1, n, f) == n;
+    if (ok && (order != p.order || compress != p.compress || paf != p.paf || L != p.L || got != spec)) {
+        fclose(f);
+        return c->fail(GP_ERR_FORMAT, "checkpoint %s belongs to another job (%s)", path, got.c_str());
+    }
+    ok = ok && get(f, j.st.necklaces) && get(f, j.st.candidates) && get(f, j.st.psd_pass) && get(f, j.st.unsure);
+    uint64_t nr = 0;
+    ok = ok && get(f, nr);
+    j.ranges.clear();
+    for (uint64_t i = 0; ok && i < nr; ++i) {
+        gp::u128 lo = 0, hi = 0;
+        ok = get_u128(f, lo) && get_u128(f, hi) && lo < hi;
+        if (ok) j.ranges.emplace_back(lo, hi);
+    }
+    for (RecordSet* rs : {&j.ra, &j.rb}) {
+        uint64_t m = 0;
+        ok = ok && get(f, m);
+        if (!ok) break;
+        rs->words.resize(m);
+        for (uint64_t i = 0; ok && i < m; ++i) ok = get_u128(f, rs->words[i]);
+        rs->sigs.resize((size_t)m * (p.L - 1));
+        ok = ok && fread(rs->sigs.data(), 2, rs->sigs.size(), f) == rs->sigs.size();
+    }
+    fclose(f);
+    return ok ? GP_OK : c->fail(GP_ERR_FORMAT, "checkpoint %s is damaged", path);
+}
+
+// Generation that can stop after max_iterations pipeline iterations or
+// max_seconds (either <= 0: no limit) and resume from a checkpoint file.
+int generate_resumable(gp_ctx* c, const GenPlan& p, const std::string& spec,
+                       std::vector<std::pair<gp::u128, gp::u128>> ranges, const char* path_a, const char* path_b,
+                       const char* ckpt, int max_iterations, double max_seconds, int* done, gp_gen_stats* stats) {
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<JobRun> jobs(1);
+    JobRun& j = jobs[0];
+    j.p = p;
+    FILE* probe = fopen(ckpt, "rb");
+    if (probe) {
+        fclose(probe);
+        const int rc = load_checkpoint(c, ckpt, p, spec, j);
+        if (rc) return rc;
+    } else {
+        j.ranges = std::move(ranges);
+    }
+    StopCtl stop;
+    stop.max_iterations = max_iterations;
+    stop.max_seconds = max_seconds;
+    int rc = GP_OK;
+    if (!j.ranges.empty()) {
+        BatchCfg cfg;  // 2^22 candidates per iteration: iterations stay short
+        rc = run_batch(c, jobs, cfg, nullptr, &stop);
+        if (rc) return rc;
+    }
+    gp_gen_stats st = j.st;
+    if (stop.stopped) {
+        rc = save_checkpoint(c, ckpt, p, spec, j);
+        if (rc) return rc;
+        if (done) *done = 0;
+    } else {
+        rc = finish(c, p, j.ra, j.rb, path_a, path_b, &st);
+        if (rc) return rc;
+        remove(ckpt);
+        if (done) *done = 1;
+    }
+    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = st;
+    return GP_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -585,27 +783,7 @@ int gp_generate(gp_ctx* c, int order, int compress, int paf, int proc_id, int pr
         if (fb) fclose(fb);
         return GP_NO_DECOMPOSITION;
     }
-    const int L = p.L, k = p.k;
-    // job split of src/utils/lyndon.cpp:93-106: prenecklace prefixes of the
-    // first length i with at least proc_num * 10000 necklaces, dealt out
-    // round robin (1-based count), each covering the words that extend it
-    std::vector<std::pair<gp::u128, gp::u128>> ranges;
-    int i = 1;
-    for (; i <= L; ++i)
-        if (gp::necklace_count(i, k) >= (gp::u128)proc_num * 10000) break;
-    if (proc_num > 1 && i < L) {
-        const gp::u128 span = gp::upow(k, L - i);
-        int64_t count = 0;
-        gp::prenecklaces(i, k, [&](const std::vector<int>& pre, int) {
-            ++count;
-            if (count % proc_num != proc_id) return;
-            gp::u128 r = 0;
-            for (int d : pre) r = r * (gp::u128)k + (gp::u128)d;
-            ranges.emplace_back(r * span, (r + 1) * span);
-        });
-    } else {
-        ranges.emplace_back(0, gp::upow(k, L));
-    }
+    std::vector<std::pair<gp::u128, gp::u128>> ranges = shard_ranges(p, proc_id, proc_num);
     std::vector<JobRun> jobs(1);
     jobs[0].p = p;
     jobs[0].ranges = std::move(ranges);
@@ -706,4 +884,41 @@ extern "C" int gp_generate_batch(gp_ctx* c, const gp_gen_job* jobs, int njobs, i
         cfg->tune_seconds = tune_s;
     }
     return GP_OK;
+}
+
+extern "C" int gp_generate_resumable(gp_ctx* c, int order, int compress, int paf, int proc_id, int proc_num,
+                                     const char* path_a, const char* path_b, const char* checkpoint_path,
+                                     int max_iterations, double max_seconds, int* done, gp_gen_stats* stats) {
+    if (!c || !path_a || !path_b || !checkpoint_path) return GP_ERR_ARG;
+    if (proc_num < 1 || proc_id < 0 || proc_id >= proc_num)
+        return c->fail(GP_ERR_ARG, "bad job split %d of %d", proc_id, proc_num);
+    cudaSetDevice(c->device);
+    GenPlan p;
+    int rc = plan_for(c, order, compress, paf, p);
+    if (rc) return rc;
+    if (p.dec.empty()) return c->fail(GP_NO_DECOMPOSITION, "Order %d cannot be decomposed", order);
+    const std::string spec = "shard " + std::to_string(proc_id) + " " + std::to_string(proc_num);
+    return generate_resumable(c, p, spec, shard_ranges(p, proc_id, proc_num), path_a, path_b, checkpoint_path,
+                              max_iterations, max_seconds, done, stats);
+}
+
+extern "C" int gp_generate_window_resumable(gp_ctx* c, int order, int compress, int paf, uint64_t begin_hi,
+                                            uint64_t begin_lo, uint64_t end_hi, uint64_t end_lo, const char* path_a,
+                                            const char* path_b, const char* checkpoint_path, int max_iterations,
+                                            double max_seconds, int* done, gp_gen_stats* stats) {
+    if (!c || !path_a || !path_b || !checkpoint_path) return GP_ERR_ARG;
+    cudaSetDevice(c->device);
+    GenPlan p;
+    int rc = plan_for(c, order, compress, paf, p);
+    if (rc) return rc;
+    if (p.dec.empty()) return c->fail(GP_NO_DECOMPOSITION, "Order %d cannot be decomposed", order);
+    gp::u128 lo = ((gp::u128)begin_hi << 64) | begin_lo;
+    gp::u128 hi = ((gp::u128)end_hi << 64) | end_lo;
+    const gp::u128 space = gp::upow(p.k, p.L);
+    if (hi > space) hi = space;
+    std::vector<std::pair<gp::u128, gp::u128>> ranges;
+    if (lo < hi) ranges.emplace_back(lo, hi);
+    const std::string spec = "window " + u128_dec(lo) + " " + u128_dec(hi);
+    return generate_resumable(c, p, spec, ranges, path_a, path_b, checkpoint_path, max_iterations, max_seconds, done,
+                              stats);
 }

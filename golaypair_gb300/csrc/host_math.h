@@ -76,6 +76,19 @@ inline u128 rank_to_word(u128 r, int k, int b, int L) {
 
 inline int word_digit_h(u128 w, int b, int L, int j) { return (int)((w >> (b * (L - 1 - j))) & (((u128)1 << b) - 1)); }
 
+// Rank of a word (inverse of rank_to_word).  A bound past the last word
+// (a digit >= k, or bits above digit 0's field) maps to k^L.
+inline u128 word_to_rank(u128 w, int k, int b, int L) {
+    if (b * L < 128 && (w >> (b * L)) != 0) return upow(k, L);
+    u128 r = 0;
+    for (int j = 0; j < L; ++j) {
+        const int d = word_digit_h(w, b, L, j);
+        if (d >= k) return upow(k, L);
+        r = r * (u128)k + (u128)d;
+    }
+    return r;
+}
+
 // Every prenecklace of length n over digits 0..k-1 in lexicographic order
 // with its period (the FKM recursion of src/utils/lyndon.cpp:47-85).
 inline void prenecklaces(int n, int k, const std::function<void(const std::vector<int>&, int)>& cb) {

@@ -8,7 +8,9 @@
 //     -n,--numjob INT       number of jobs (default 1)
 //     -d,--dir PATH         work directory (default "results")
 //   subcommands (any number, run in pipeline order): all gen sort match
-//   uncompress filter, with the reference's per-subcommand options.
+//   uncompress filter, with the reference's per-subcommand options; gen
+//   also takes --checkpoint FILE [--max-seconds S] [--max-iterations N]
+//   (not in the reference) for searches that stop and resume.
 //
 // Files and their names are the reference's (src/main.cpp:32-44,62-67,
 // 88-90,147-149).  Every stage runs on the GPU through the C ABI in
@@ -35,7 +37,12 @@ struct Options {
     std::string work_dir() const { return temp_dir + "/order-" + std::to_string(order); }
 };
 
-struct GenOpts { std::string file_prefix = "filtered"; };
+struct GenOpts {
+    std::string file_prefix = "filtered";
+    std::string checkpoint;  // not in the reference: resumable generation
+    double max_seconds = 0;
+    int max_iterations = 0;
+};
 struct SortOpts { std::string input_prefix = "filtered", output_prefix = "filtered_sorted"; };
 struct MatchOpts {
     std::string input_prefix = "filtered_sorted", output_prefix = "pairs";
@@ -48,6 +55,8 @@ struct UncompressOpts {
 struct FilterOpts { std::string input_prefix = "pairs", output_prefix = "unique"; };
 
 gp_ctx* g_ctx = nullptr;
+// gen with --checkpoint stopped early: the checkpoint is written, run again
+constexpr int kExitCheckpointed = 75;
 
 int die(const char* what, int rc) {
     fprintf(stderr, "%s failed (%d): %s\n", what, rc, g_ctx ? gp_last_error(g_ctx) : "");
@@ -69,14 +78,24 @@ int stage_generate(const Options& o, const GenOpts& g) {
     gp_gen_stats st;
     const std::string fa = cand_file(o, g.file_prefix, 'a', o.job_id);
     const std::string fb = cand_file(o, g.file_prefix, 'b', o.job_id);
-    const int rc = gp_generate(g_ctx, o.order, o.compress[0], o.paf_constant, o.job_id, o.job_count, fa.c_str(),
-                               fb.c_str(), &st);
+    int done = 1;
+    const int rc = g.checkpoint.empty()
+                       ? gp_generate(g_ctx, o.order, o.compress[0], o.paf_constant, o.job_id, o.job_count, fa.c_str(),
+                                     fb.c_str(), &st)
+                       : gp_generate_resumable(g_ctx, o.order, o.compress[0], o.paf_constant, o.job_id, o.job_count,
+                                               fa.c_str(), fb.c_str(), g.checkpoint.c_str(), g.max_iterations,
+                                               g.max_seconds, &done, &st);
     if (rc == GP_NO_DECOMPOSITION) {
         fprintf(stderr, "Order %d cannot be decomposed into a sum of squares\n%d*2\nHence there are no solutions.\n",
                 o.order, o.order);
         return 1;
     }
     if (rc) return die("gen", rc);
+    if (!done) {
+        printf("[gpu] stopped after %.3f s: %lld necklaces so far; checkpoint %s; run gen again to continue\n",
+               st.seconds, (long long)st.necklaces, g.checkpoint.c_str());
+        return kExitCheckpointed;
+    }
     printf("Orderly Count: %lld\nPassed PSD filter: %lld\n", (long long)st.necklaces,
            (long long)(st.written_a + st.written_b));
     printf("[gpu] candidates %lld, exact PSD passes %lld, tensor-core unsure %lld, %.3f s\n",
@@ -172,6 +191,8 @@ void usage() {
         "Subcommands:\n"
         "  all                         Run all steps in the pipeline\n"
         "  gen                         Candidate generation step (-o,--output)\n"
+        "                              --checkpoint FILE [--max-seconds S] [--max-iterations N]:\n"
+        "                              stop early and resume from FILE (exit code 75 = stopped)\n"
         "  sort                        File sorting step (-i,--input -o,--output)\n"
         "  match                       Candidate matching step (-i,--input -o,--output -a,--append BOOL)\n"
         "  uncompress                  Pair uncompression step (-i -o --internal --sorted -l -b -e -s -p,--prefix\n"
@@ -232,6 +253,9 @@ int main(int argc, char** argv) {
             if (is_int(a.c_str()) && opts.order < 0) { opts.order = atoi(a.c_str()); continue; }
         } else if (ctx == "gen") {
             if (a == "-o" || a == "--output") { gen.file_prefix = next("--output"); continue; }
+            if (a == "--checkpoint") { gen.checkpoint = next("--checkpoint"); continue; }
+            if (a == "--max-seconds") { gen.max_seconds = atof(next("--max-seconds").c_str()); continue; }
+            if (a == "--max-iterations") { gen.max_iterations = atoi(next("--max-iterations").c_str()); continue; }
         } else if (ctx == "sort") {
             if (a == "-i" || a == "--input") { srt.input_prefix = next("--input"); continue; }
             if (a == "-o" || a == "--output") { srt.output_prefix = next("--output"); continue; }

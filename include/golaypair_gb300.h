@@ -141,6 +141,30 @@ int gp_generate_window(gp_ctx* ctx, int order, int compress, int paf, uint64_t b
                        uint64_t end_hi, uint64_t end_lo, const char* path_a, const char* path_b,
                        gp_gen_stats* stats);
 
+/*
+ * Checkpointed generation for searches that run for days: the same job as
+ * gp_generate (job split proc_id of proc_num) or gp_generate_window (word
+ * ranks [begin, end)), but the call stops after max_iterations pipeline
+ * iterations or max_seconds of searching (either <= 0: no limit).  When it
+ * stops early it writes checkpoint_path (the counts so far, the word ranges
+ * still to search and the records found so far; written to a temporary file
+ * and renamed, so an interrupted write keeps the previous checkpoint) and
+ * sets *done = 0; the output files are not written yet.  The next call with
+ * the same job and checkpoint_path resumes from it.  When the search
+ * finishes, the call writes the A and B files -- identical to those of the
+ * uninterrupted call -- removes the checkpoint and sets *done = 1.  stats
+ * counts the whole search so far; its seconds field is this call's time.
+ * A checkpoint of another job gives GP_ERR_FORMAT.  No counterpart in the
+ * reference, whose only restart unit is a whole stage output file.
+ */
+int gp_generate_resumable(gp_ctx* ctx, int order, int compress, int paf, int proc_id, int proc_num,
+                          const char* path_a, const char* path_b, const char* checkpoint_path, int max_iterations,
+                          double max_seconds, int* done, gp_gen_stats* stats);
+int gp_generate_window_resumable(gp_ctx* ctx, int order, int compress, int paf, uint64_t begin_hi, uint64_t begin_lo,
+                                 uint64_t end_hi, uint64_t end_lo, const char* path_a, const char* path_b,
+                                 const char* checkpoint_path, int max_iterations, double max_seconds, int* done,
+                                 gp_gen_stats* stats);
+
 /* One job of a batched generation: the words of one order / compression
  * whose rank lies in [begin, end) (end clipped to the word space), written
  * to its own A and B files. */
