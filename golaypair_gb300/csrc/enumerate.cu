@@ -87,8 +87,10 @@ __device__ __forceinline__ int first_prenecklace(W128& w, int b, int L) {
 // The layout of the job a thread is enumerating, held in registers.
 struct JobView {
     int L, b;
+    uint32_t inv_b;           // floor(x / b) = (x * inv_b) >> 8 for 0 <= x < 128
     W128 maxpat, full;        // full = low_mask(b * L)
     W128 ones;                // bit 0 of every digit; bit t of every digit = ones << t
+    W128 divisors;            // bit p set iff p divides L (the necklace test, no division)
 };
 
 __device__ __forceinline__ JobView job_view(const EnumJob& j) {
@@ -98,14 +100,22 @@ __device__ __forceinline__ JobView job_view(const EnumJob& j) {
     v.maxpat = w128(j.maxpat);
     v.full = low_mask(j.b * j.L);
     v.ones = w128(j.plane[0]);
+    v.inv_b = (256u + (uint32_t)j.b - 1u) / (uint32_t)j.b;
+    v.divisors = {0, 0};
+    for (int p = 1; p <= j.L; ++p)
+        if (j.L % p == 0) v.divisors = bor(v.divisors, shl({1ull, 0ull}, p));
     return v;
+}
+
+__device__ __forceinline__ bool divides_L(const JobView& a, int p) {
+    return ((p < 64 ? (a.divisors.lo >> p) : (a.divisors.hi >> (p - 64))) & 1ull) != 0;
 }
 
 // FKM successor; returns the new period, or 0 when w was the last word.
 __device__ __forceinline__ int fkm_next(W128& w, const JobView& a) {
     const W128 x = band(bxor(w, a.maxpat), a.full);
     if (is_zero(x)) return 0;
-    const int r = ctz128(x) / a.b;  // digits after the incremented one
+    const int r = (int)(((uint32_t)ctz128(x) * a.inv_b) >> 8);  // digits after the incremented one
     const int j = a.L - 1 - r;
     w = band(w, bxor(a.full, low_mask(a.b * r)));
     // increment digit j (it is below the maximum, so no carry)
@@ -194,7 +204,7 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
         uint8_t role = 0;
         W128 cand = w;
         if (active) {
-            if (jv.L % p == 0) {
+            if (divides_L(jv, p)) {
                 ++necklaces;
                 role = role_tab[job][digit_sum(w, jv)];
             }
