@@ -87,6 +87,7 @@ __device__ __forceinline__ int first_prenecklace(W128& w, int b, int L) {
 // The layout of the job a thread is enumerating, held in registers.
 struct JobView {
     int L, b;
+    bool narrow;              // b * L <= 64: the word fits its low 64 bits
     uint32_t inv_b;           // floor(x / b) = (x * inv_b) >> 8 for 0 <= x < 128
     W128 maxpat, full;        // full = low_mask(b * L)
     W128 ones;                // bit 0 of every digit; bit t of every digit = ones << t
@@ -101,6 +102,7 @@ __device__ __forceinline__ JobView job_view(const EnumJob& j) {
     v.full = low_mask(j.b * j.L);
     v.ones = w128(j.plane[0]);
     v.inv_b = (256u + (uint32_t)j.b - 1u) / (uint32_t)j.b;
+    v.narrow = j.b * j.L <= 64;
     v.divisors = {0, 0};
     for (int p = 1; p <= j.L; ++p)
         if (j.L % p == 0) v.divisors = bor(v.divisors, shl({1ull, 0ull}, p));
@@ -125,6 +127,30 @@ __device__ __forceinline__ int fkm_next(W128& w, const JobView& a) {
     const int p = j + 1;
     w = periodic_fill(w, a.b, a.L, p);
     return p;
+}
+
+// The same successor on words of at most 64 bits (native 64-bit shifts; no
+// shift below reaches 64: b * len, b * r < b * L <= 64).
+__device__ __forceinline__ uint64_t mask64(int bits) { return bits >= 64 ? ~0ull : ((1ull << bits) - 1ull); }
+
+__device__ __forceinline__ int fkm_next64(uint64_t& w, const JobView& a) {
+    const uint64_t x = (w ^ a.maxpat.lo) & a.full.lo;
+    if (!x) return 0;
+    const int r = (int)(((uint32_t)(__ffsll((long long)x) - 1) * a.inv_b) >> 8);
+    const int p = a.L - r;  // the incremented digit is L - 1 - r; the new period is its index + 1
+    w = (w & (a.full.lo ^ mask64(a.b * r))) + (1ull << (a.b * r));
+    uint64_t y = w & (a.full.lo ^ mask64(a.b * r));
+    for (int len = p; len < a.L; len <<= 1) y |= y >> (a.b * len);
+    w = y & a.full.lo;
+    return p;
+}
+
+__device__ __forceinline__ int digit_sum64(uint64_t w, const JobView& a) {
+    int s = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+        if (t < a.b) s += __popcll(w & (a.ones.lo << t)) << t;
+    return s;
 }
 
 __device__ __forceinline__ int digit_sum(W128 w, const JobView& a) {
@@ -206,9 +232,16 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
         if (active) {
             if (divides_L(jv, p)) {
                 ++necklaces;
-                role = role_tab[job][digit_sum(w, jv)];
+                role = role_tab[job][jv.narrow ? digit_sum64(w.lo, jv) : digit_sum(w, jv)];
             }
-            const int np = fkm_next(w, jv);
+            int np;
+            if (jv.narrow) {
+                uint64_t wl = w.lo;
+                np = fkm_next64(wl, jv);
+                w.lo = wl;
+            } else {
+                np = fkm_next(w, jv);
+            }
             if (np == 0 || !lt(w, end)) {
                 have = false;
                 a.cur[win] = a.end[win];
