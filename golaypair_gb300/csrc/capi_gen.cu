@@ -13,6 +13,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -207,7 +208,16 @@ int64_t rec_region_bytes(int64_t rcap, int L) {
 
 // Runs the batch engine over the jobs' ranges; records land in the jobs'
 // A/B lists, counts in their stats.
+// GP_GEN_TIMING=1 in the environment prints the engine's phase times to
+// stderr (diagnostics).
+double since(std::chrono::steady_clock::time_point t) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t).count();
+}
+
 int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* iterations, StopCtl* stop = nullptr) {
+    static const bool timing = getenv("GP_GEN_TIMING") != nullptr;
+    const auto tb = std::chrono::steady_clock::now();
+    double t_win = 0, t_setup = 0, t_capture = 0, t_iter = 0, t_drain = 0;
     const int nj = (int)jobs.size();
     if (nj < 1 || nj > gp::kMaxEnumJobs) return c->fail(GP_ERR_ARG, "batch of %d jobs (1..%d)", nj, gp::kMaxEnumJobs);
     cudaStream_t s = c->s_comp;
@@ -239,6 +249,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
         }
     }
     const int64_t nwin = (int64_t)cur.size();
+    t_win = since(tb);
     // ---- capacities and the device arena
     const int64_t slack = threads * 8 + 4096;  // appends after a job met its soft cap
     size_t off = 0;
@@ -388,6 +399,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
         GP_CUDA_TRY(c, cudaMemcpyAsync(hctr, ctr, kCounterWords * 8, cudaMemcpyDeviceToHost, s));
         return GP_OK;
     };
+    t_setup = since(tb) - t_win;
     // ---- capture it once
     cudaGraphExec_t exec = nullptr;
     if (cfg.use_graph) {
@@ -412,6 +424,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
             if (x) cudaGraphExecDestroy(x);
         }
     } guard{exec};
+    t_capture = since(tb) - t_win - t_setup;
     // ---- iterate until no window is left unfinished
     int iters = 0;
     int stalled = 0;
@@ -477,7 +490,12 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
         j.st.necklaces += (int64_t)hctr[kCumBase + ji * kCumSlots + 0];
         j.st.psd_pass += (int64_t)hctr[kCumBase + ji * kCumSlots + 2];
     }
+    t_iter = since(tb) - t_win - t_setup - t_capture;
     if (iterations) *iterations = iters;
+    if (timing)
+        fprintf(stderr, "[gen] windows %.4f s, setup %.4f s, capture %.4f s, %d iterations + drains %.4f s\n", t_win,
+                t_setup, t_capture, iters, t_iter);
+    (void)t_drain;
     return GP_OK;
 }
 
@@ -864,10 +882,12 @@ extern "C" int gp_generate_batch(gp_ctx* c, const gp_gen_job* jobs, int njobs, i
     int iters = 0;
     int rc = run_batch(c, run, bc, &iters);
     if (rc) return rc;
+    const auto tf = std::chrono::steady_clock::now();
     for (int i = 0; i < njobs; ++i) {
         rc = finish(c, run[i].p, run[i].ra, run[i].rb, jobs[i].path_a, jobs[i].path_b, &run[i].st);
         if (rc) return rc;
     }
+    if (getenv("GP_GEN_TIMING")) fprintf(stderr, "[gen] files %.4f s\n", since(tf));
     const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats)
         for (int i = 0; i < njobs; ++i) {
