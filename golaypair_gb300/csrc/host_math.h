@@ -66,9 +66,18 @@ inline u128 upow(int k, int e) {
 // most significant, b bits per digit).
 inline u128 rank_to_word(u128 r, int k, int b, int L) {
     u128 w = 0;
-    for (int j = L - 1; j >= 0; --j) {
+    int j = L - 1;
+    // 128-bit division is a library call: divide in 128 bits only while the
+    // rank does not fit 64 bits
+    for (; j >= 0 && (r >> 64) != 0; --j) {
         const int d = (int)(r % (u128)k);
         r /= (u128)k;
+        w |= (u128)d << (b * (L - 1 - j));
+    }
+    uint64_t q = (uint64_t)r;
+    for (; j >= 0; --j) {
+        const int d = (int)(q % (uint64_t)k);
+        q /= (uint64_t)k;
         w |= (u128)d << (b * (L - 1 - j));
     }
     return w;
