@@ -135,7 +135,8 @@ int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, const char
 constexpr int kIterSlots = 4;   // per job: [0] candidates, [1] unsure, [2] survivors
 constexpr int kCumSlots = 4;    // per job: [0] necklaces, [1] records, [2] psd passes
 constexpr int kIncomplete = kIterSlots * gp::kMaxEnumJobs;          // u64 slot of the flag
-constexpr int kIterWords = kIncomplete + 1;
+constexpr int kNextWin = kIncomplete + 1;                          // window handout counter
+constexpr int kIterWords = kIncomplete + 2;
 constexpr int kCumBase = 40;                                        // u64 offset of the cumulative block
 constexpr int kCounterWords = kCumBase + kCumSlots * gp::kMaxEnumJobs;
 
@@ -240,10 +241,19 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
         const gp::u128 space = gp::upow(j.p.k, j.p.L);
         const gp::u128 maxw = gp::rank_to_word(space - 1, j.p.k, j.p.b, j.p.L);
         for (auto& r : j.ranges) {
+            if (r.first >= r.second) continue;
+            gp::RankStepper step(r.first, wsize < space ? wsize : space, j.p.k, j.p.b, j.p.L);
             for (gp::u128 lo = r.first; lo < r.second; lo += wsize) {
-                const gp::u128 hi = lo + wsize < r.second ? lo + wsize : r.second;
-                cur.push_back(to_u4(gp::rank_to_word(lo, j.p.k, j.p.b, j.p.L)));
-                end.push_back(to_u4(hi >= space ? maxw + 1 : gp::rank_to_word(hi, j.p.k, j.p.b, j.p.L)));
+                const bool whole = lo + wsize <= r.second;  // the window ends wsize words on
+                const gp::u128 hi = whole ? lo + wsize : r.second;
+                cur.push_back(to_u4(step.word()));
+                step.advance();
+                if (hi >= space)
+                    end.push_back(to_u4(maxw + 1));
+                else if (whole)
+                    end.push_back(to_u4(step.word()));
+                else
+                    end.push_back(to_u4(gp::rank_to_word(hi, j.p.k, j.p.b, j.p.L)));
                 wjob.push_back((uint8_t)ji);
             }
         }
@@ -348,6 +358,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     ea.win_job = A + off_wjob;
     ea.nwin = nwin;
     ea.incomplete = reinterpret_cast<int*>(ctr + kIncomplete);
+    ea.next_win = ctr + kNextWin;
     ea.status = c->status.as<int>();
 
     // ---- one iteration of the pipeline on stream s (branches per job)

@@ -175,7 +175,7 @@ __device__ __forceinline__ bool job_full(const EnumJob& j) {
     return (int64_t)*reinterpret_cast<volatile unsigned long long*>(j.count) >= j.soft_cap;
 }
 
-// Each thread walks the windows tid, tid + nthreads, ...  A window whose job
+// Each thread takes windows from a global counter.  A window whose job
 // has reached its soft capacity is left (position saved) and the thread goes
 // on with its next window, so one full job does not idle the others.
 // MINB = 1: registers as needed (4 CTAs of 256 per SM); MINB = 8: capped
@@ -190,8 +190,10 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-    int64_t win = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // current window
+    // windows are handed out dynamically: a thread takes the next unvisited
+    // one from a global counter when it needs work (long windows do not
+    // hold up a statically assigned share)
+    int64_t win = (int64_t)atomicAdd(a.next_win, 1ull);  // current window
     bool active = win < a.nwin;
     W128 w = {0, 0}, end = {0, 0};
     JobView jv{};
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
                 if (!have) a.cur[win] = a.end[win];  // window finished
             }
             if (!have) {
-                win += nthreads;
+                win = (int64_t)atomicAdd(a.next_win, 1ull);
                 active = win < a.nwin;
             }
         }
@@ -245,7 +247,7 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
             if (np == 0 || !lt(w, end)) {
                 have = false;
                 a.cur[win] = a.end[win];
-                win += nthreads;
+                win = (int64_t)atomicAdd(a.next_win, 1ull);
                 active = win < a.nwin;
             } else {
                 p = np;
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
             a.cur[win] = to_u4(w);
             have = false;
             parked_any = true;
-            win += nthreads;
+            win = (int64_t)atomicAdd(a.next_win, 1ull);
             active = win < a.nwin;
         }
     }
@@ -286,8 +288,17 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
 cudaError_t launch_enumerate(const EnumArgs& a, int num_sms, cudaStream_t st, int variant) {
     if (a.nwin <= 0) return cudaSuccess;
     if (a.njobs < 1 || a.njobs > kMaxEnumJobs) return cudaErrorInvalidValue;
+    // one wave of resident blocks: windows are handed out dynamically
+    static int resident[2] = {0, 0};
+    int& per_sm = resident[variant == 1 ? 1 : 0];
+    if (per_sm == 0) {
+        cudaError_t e = variant == 1
+                            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<8>, 256, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<1>, 256, 0);
+        if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    }
     int64_t blocks = (a.nwin + 255) / 256;
-    const int64_t maxb = (int64_t)num_sms * 8;
+    const int64_t maxb = (int64_t)num_sms * per_sm;
     if (blocks > maxb) blocks = maxb;
     if (variant == 1)
         enumerate_kernel<8><<<(unsigned)blocks, 256, 0, st>>>(a);

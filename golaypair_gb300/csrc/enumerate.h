@@ -40,6 +40,7 @@ struct EnumArgs {
     const uint4* end;          // per window: first word past the window
     const uint8_t* win_job;    // per window: its job
     int64_t nwin;
+    unsigned long long* next_win;  // window handout counter (zero before the launch)
     int* incomplete;           // out: 1 if some window is unfinished
     int* status;
 };

@@ -83,6 +83,38 @@ inline u128 rank_to_word(u128 r, int k, int b, int L) {
     return w;
 }
 
+// Words of the ranks r0, r0 + step, r0 + 2 step, ...: the rank's base-k
+// digits are kept and the step's digits added with carry, so each word
+// costs L small additions instead of L 128-bit divisions.
+struct RankStepper {
+    int k, b, L;
+    std::vector<int> d, s;  // digit 0 most significant
+    bool past_end = false;  // the rank reached k^L
+    RankStepper(u128 r0, u128 step, int k_, int b_, int L_) : k(k_), b(b_), L(L_), d(L_), s(L_) {
+        for (int j = L - 1; j >= 0; --j) {
+            d[j] = (int)(r0 % (u128)k);
+            r0 /= (u128)k;
+            s[j] = (int)(step % (u128)k);
+            step /= (u128)k;
+        }
+        past_end = r0 != 0 || step != 0;  // inputs of k^L or more
+    }
+    u128 word() const {
+        u128 w = 0;
+        for (int j = 0; j < L; ++j) w = (w << b) | (u128)d[j];
+        return w;
+    }
+    void advance() {
+        int carry = 0;
+        for (int j = L - 1; j >= 0; --j) {
+            int v = d[j] + s[j] + carry;
+            carry = v >= k;
+            d[j] = carry ? v - k : v;
+        }
+        if (carry) past_end = true;
+    }
+};
+
 inline int word_digit_h(u128 w, int b, int L, int j) { return (int)((w >> (b * (L - 1 - j))) & (((u128)1 << b) - 1)); }
 
 // Rank of a word (inverse of rank_to_word).  A bound past the last word
