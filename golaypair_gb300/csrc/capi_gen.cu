@@ -261,7 +261,9 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     const int64_t nwin = (int64_t)cur.size();
     t_win = since(tb);
     // ---- capacities and the device arena
-    const int64_t slack = threads * 8 + 4096;  // appends after a job met its soft cap
+    // appends after a job met its soft cap: a lane sees the count at most 16
+    // steps late (one per step), plus up to 63 queued per warp
+    const int64_t slack = threads * 16 + threads / 32 * 64 + 4096;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;

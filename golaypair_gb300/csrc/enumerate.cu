@@ -178,18 +178,61 @@ __device__ __forceinline__ bool job_full(const EnumJob& j) {
 // Each thread takes windows from a global counter.  A window whose job
 // has reached its soft capacity is left (position saved) and the thread goes
 // on with its next window, so one full job does not idle the others.
-// MINB = 1: registers as needed (4 CTAs of 256 per SM); MINB = 8: capped
+// MINB = 4: at most 64 registers (4 CTAs of 256 per SM); MINB = 8: capped
 // at 32 registers for full occupancy (some spills).  The tuner picks.
+//
+// Candidates go to a per-warp queue in shared memory first; the warp writes
+// them out when 32 or more are queued, with one counter atomic per job
+// present.  (An atomic per step, whose returned offset the whole warp waits
+// for, made the kernel memory-latency bound.)  A job's soft capacity is
+// checked on a count loaded at the previous check, so the load's latency
+// overlaps the steps in between.
+constexpr int kQueue = 64;  // per warp: < 32 queued + 32 from one step
+
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
     __shared__ uint8_t role_tab[kMaxEnumJobs][kMaxDigitSum + 1];
     __shared__ EnumJob jobs[kMaxEnumJobs];
+    __shared__ uint4 q_word[8][kQueue];
+    __shared__ uint8_t q_role[8][kQueue];
+    __shared__ uint8_t q_job[8][kQueue];
     for (int i = threadIdx.x; i < a.njobs * (kMaxDigitSum + 1); i += blockDim.x)
         role_tab[i / (kMaxDigitSum + 1)][i % (kMaxDigitSum + 1)] = a.roles[i];
     if (threadIdx.x < a.njobs) jobs[threadIdx.x] = a.jobs[threadIdx.x];
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    const int wq = threadIdx.x >> 5;  // this warp's queue
     const uint32_t lt_mask = (1u << lane) - 1u;
+    int qlen = 0;                     // queued candidates (the same in every lane)
+    // writes the warp's queue out (every lane of the warp calls it)
+    auto flush = [&]() {
+        __syncwarp();
+        for (int base = 0; base < qlen; base += 32) {
+            const int e = base + lane;
+            const bool has = e < qlen;
+            const uint32_t hm = __ballot_sync(0xFFFFFFFFu, has);
+            if (has) {
+                const int jb = q_job[wq][e];
+                const uint32_t grp = __match_any_sync(hm, jb);
+                const int leader = __ffs(grp) - 1;
+                const EnumJob& J = jobs[jb];
+                unsigned long long pos0 = 0;
+                if (lane == leader) pos0 = atomicAdd(J.count, (unsigned long long)__popc(grp));
+                pos0 = __shfl_sync(grp, pos0, leader);
+                const unsigned long long pos = pos0 + __popc(grp & lt_mask);
+                if ((int64_t)pos < J.cap) {
+                    J.words[pos] = q_word[wq][e];
+                    J.out_roles[pos] = q_role[wq][e];
+                } else {
+                    atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
+                }
+            }
+        }
+        qlen = 0;
+        __syncwarp();
+    };
+    unsigned long long seen_count = 0;  // count of job seen_job, loaded at the previous check
+    int seen_job = -1;
     // windows are handed out dynamically: a thread takes the next unvisited
     // one from a global counter when it needs work (long windows do not
     // hold up a statically assigned share)
@@ -253,32 +296,34 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
                 p = np;
             }
         }
-        // append: lanes grouped by job, one atomic per group
+        // queue this step's candidates; write the queue out from 32
         const uint32_t want = __ballot_sync(0xFFFFFFFFu, role != 0);
-        if (role) {
-            const uint32_t grp = __match_any_sync(want, job);
-            const int leader = __ffs(grp) - 1;
-            const EnumJob& J = jobs[job];
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(J.count, (unsigned long long)__popc(grp));
-            base = __shfl_sync(grp, base, leader);
-            const unsigned long long pos = base + __popc(grp & lt_mask);
-            if ((int64_t)pos < J.cap) {
-                J.words[pos] = to_u4(cand);
-                J.out_roles[pos] = role;
-            } else {
-                atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
+        if (want) {
+            if (role) {
+                const int slot = qlen + __popc(want & lt_mask);
+                q_word[wq][slot] = to_u4(cand);
+                q_role[wq][slot] = role;
+                q_job[wq][slot] = (uint8_t)job;
             }
+            qlen += __popc(want);
+            if (qlen >= 32) flush();
         }
         // every 8 steps: leave a window whose job reached its soft capacity
-        if ((step & 7) == 0 && active && have && job_full(jobs[job])) {
-            a.cur[win] = to_u4(w);
-            have = false;
-            parked_any = true;
-            win = (int64_t)atomicAdd(a.next_win, 1ull);
-            active = win < a.nwin;
+        // (by the count loaded 8 steps ago), then load the count afresh
+        if ((step & 7) == 0 && active && have) {
+            if (seen_job == job && (int64_t)seen_count >= jobs[job].soft_cap) {
+                a.cur[win] = to_u4(w);
+                have = false;
+                parked_any = true;
+                win = (int64_t)atomicAdd(a.next_win, 1ull);
+                active = win < a.nwin;
+            } else {
+                seen_count = *reinterpret_cast<volatile unsigned long long*>(jobs[job].count);
+                seen_job = job;
+            }
         }
     }
+    flush();
     if (parked_any) *a.incomplete = 1;
     if (necklaces) atomicAdd(jobs[job].necklaces, necklaces);
 }
@@ -294,7 +339,7 @@ cudaError_t launch_enumerate(const EnumArgs& a, int num_sms, cudaStream_t st, in
     if (per_sm == 0) {
         cudaError_t e = variant == 1
                             ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<8>, 256, 0)
-                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<1>, 256, 0);
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<4>, 256, 0);
         if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     }
     int64_t blocks = (a.nwin + 255) / 256;
@@ -303,7 +348,7 @@ cudaError_t launch_enumerate(const EnumArgs& a, int num_sms, cudaStream_t st, in
     if (variant == 1)
         enumerate_kernel<8><<<(unsigned)blocks, 256, 0, st>>>(a);
     else
-        enumerate_kernel<1><<<(unsigned)blocks, 256, 0, st>>>(a);
+        enumerate_kernel<4><<<(unsigned)blocks, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
