@@ -182,12 +182,13 @@ __device__ __forceinline__ bool job_full(const EnumJob& j) {
 // at 32 registers for full occupancy (some spills).  The tuner picks.
 //
 // Candidates go to a per-warp queue in shared memory first; the warp writes
-// them out when 32 or more are queued, with one counter atomic per job
-// present.  (An atomic per step, whose returned offset the whole warp waits
+// them out when kFlushAt or more are queued, with one counter atomic per
+// job present.  (An atomic per step, whose returned offset the whole warp waits
 // for, made the kernel memory-latency bound.)  A job's soft capacity is
 // checked on a count loaded at the previous check, so the load's latency
 // overlaps the steps in between.
-constexpr int kQueue = 64;  // per warp: < 32 queued + 32 from one step
+constexpr int kFlushAt = 128;
+constexpr int kQueue = kFlushAt + 32;  // per warp: < kFlushAt queued + 32 from one step
 
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
@@ -296,7 +297,7 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
                 p = np;
             }
         }
-        // queue this step's candidates; write the queue out from 32
+        // queue this step's candidates; write the queue out from kFlushAt
         const uint32_t want = __ballot_sync(0xFFFFFFFFu, role != 0);
         if (want) {
             if (role) {
@@ -306,7 +307,7 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
                 q_job[wq][slot] = (uint8_t)job;
             }
             qlen += __popc(want);
-            if (qlen >= 32) flush();
+            if (qlen >= kFlushAt) flush();
         }
         // every 8 steps: leave a window whose job reached its soft capacity
         // (by the count loaded 8 steps ago), then load the count afresh
