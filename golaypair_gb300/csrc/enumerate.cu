@@ -237,7 +237,15 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
     // windows are handed out dynamically: a thread takes the next unvisited
     // one from a global counter when it needs work (long windows do not
     // hold up a statically assigned share)
-    int64_t win = (int64_t)atomicAdd(a.next_win, 1ull);  // current window
+    // The index of the window after the current one is fetched when the
+    // current one starts, so the atomic's latency is hidden by its steps.
+    int64_t pref = -1;
+    auto take = [&]() -> int64_t {
+        const int64_t w0 = pref >= 0 ? pref : (int64_t)atomicAdd(a.next_win, 1ull);
+        pref = -1;
+        return w0;
+    };
+    int64_t win = take();  // current window
     bool active = win < a.nwin;
     W128 w = {0, 0}, end = {0, 0};
     JobView jv{};
@@ -265,10 +273,11 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
                     p = first_prenecklace(w, jv.b, jv.L);
                     have = lt(w, end);
                 }
+                if (have && pref < 0) pref = (int64_t)atomicAdd(a.next_win, 1ull);
                 if (!have) a.cur[win] = a.end[win];  // window finished
             }
             if (!have) {
-                win = (int64_t)atomicAdd(a.next_win, 1ull);
+                win = take();
                 active = win < a.nwin;
             }
         }
@@ -291,7 +300,7 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
             if (np == 0 || !lt(w, end)) {
                 have = false;
                 a.cur[win] = a.end[win];
-                win = (int64_t)atomicAdd(a.next_win, 1ull);
+                win = take();
                 active = win < a.nwin;
             } else {
                 p = np;
@@ -316,7 +325,7 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
                 a.cur[win] = to_u4(w);
                 have = false;
                 parked_any = true;
-                win = (int64_t)atomicAdd(a.next_win, 1ull);
+                win = take();
                 active = win < a.nwin;
             } else {
                 seen_count = *reinterpret_cast<volatile unsigned long long*>(jobs[job].count);
