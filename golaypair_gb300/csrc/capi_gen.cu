@@ -82,7 +82,7 @@ int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, const char
     std::sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return recs.words[x] < recs.words[y]; });
     FILE* f = fopen(path, "w");
     if (!f) return c->fail(GP_ERR_IO, "cannot open %s for writing", path);
-    const size_t per_block = 1 << 16;  // lines per formatting task
+    const size_t per_block = 1 << 13;  // lines per formatting task
     const size_t nblocks = (n + per_block - 1) / per_block;
     unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     if (nblocks < nthreads) nthreads = (unsigned)std::max<size_t>(1, nblocks);
