@@ -211,6 +211,7 @@ int gp_ctx_destroy(gp_ctx* c) {
     for (auto& kv : c->twiddles) kv.second.release();
     for (auto& kv : c->twiddles64) kv.second.release();
     for (auto& b : c->scratch) b.release();
+    for (auto& b : c->ux) b.release();
     for (auto& b : c->hscratch) b.release();
     if (c->s_comp) cudaStreamDestroy(c->s_comp);
     if (c->s_copy) cudaStreamDestroy(c->s_copy);

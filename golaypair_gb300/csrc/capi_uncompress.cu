@@ -214,7 +214,8 @@ int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int n
     side.n = 0;
     if (e.total == 0) return GP_OK;
     cudaStream_t s = c->s_comp;
-    DevBuf dcnt, doff, dvals, dwords, dmask, dunsure, didx, dmisc;
+    DevBuf &dcnt = c->ux[0], &doff = c->ux[1], &dvals = c->ux[2], &dwords = c->ux[3], &dmask = c->ux[4],
+           &dunsure = c->ux[5], &didx = c->ux[6], &dmisc = c->ux[7];
     const int64_t chunk = (int64_t)std::min<uint64_t>(e.total, uint64_t(1) << 24);
     if (!dcnt.ensure(L * 4) || !doff.ensure(L * 4) || !dvals.ensure(e.vals.size() + 16) || !dwords.ensure(chunk * 16) ||
         !dmask.ensure((chunk + 31) / 32 * 4) || !dunsure.ensure(chunk * 4) || !didx.ensure(chunk * 4) ||
@@ -310,7 +311,7 @@ int join_sides(gp_ctx* c, Side& A, Side& B, int Lnew, int new_compress, int paf,
         rb[i] = m[i].second;
     }
     cudaStream_t s = c->s_comp;
-    DevBuf dra, drb, wa, wb, sa, sb;
+    DevBuf &dra = c->ux[8], &drb = c->ux[9], &wa = c->ux[10], &wb = c->ux[11], &sa = c->ux[12], &sb = c->ux[13];
     if (!dra.ensure(nm * 4) || !drb.ensure(nm * 4) || !wa.ensure(nm * 16) || !wb.ensure(nm * 16) ||
         !sa.ensure(nm * S * 2 + 16) || !sb.ensure(nm * S * 2 + 16))
         return c->fail(GP_ERR_NOMEM, "uncompress: gather");

@@ -115,6 +115,9 @@ struct gp_ctx {
     }
     // generic scratch arenas used by the stage pipelines
     DevBuf scratch[16];
+    // grow-only scratch of the uncompression stage (kept across pairs: a
+    // cudaFree per pair would synchronise the device every pair)
+    DevBuf ux[32];
     HostPinned hscratch[4];
     // batched generation: one stream per job branch, fork/join events
     static constexpr int kJobStreams = 8;

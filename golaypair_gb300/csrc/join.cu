@@ -171,7 +171,9 @@ int device_join(gp_ctx* c, const JoinSide& A, const JoinSide& B, int L, int pack
     cudaStream_t s = c->s_comp;
     const int S = L - 1, H = L / 2;
     const int64_t na = A.n, nb = B.n;
-    DevBuf ka, kb, ia, ib, tmp, ha, hb, pa, pb, lb, cnt, off, stmp, outp, misc;
+    DevBuf &ka = c->ux[14], &kb = c->ux[15], &ia = c->ux[16], &ib = c->ux[17], &tmp = c->ux[18], &ha = c->ux[19],
+           &hb = c->ux[20], &pa = c->ux[21], &pb = c->ux[22], &lb = c->ux[23], &cnt = c->ux[24], &off = c->ux[25],
+           &stmp = c->ux[26], &outp = c->ux[27], &misc = c->ux[28];
     const int64_t nmax = std::max(na, nb);
     if (!ka.ensure(na * 8) || !kb.ensure(nb * 8) || !ia.ensure(na * 4) || !ib.ensure(nb * 4) ||
         !tmp.ensure(radix_sort_tmp_bytes(nmax)) || !ha.ensure(na * 8) || !hb.ensure(nb * 8) ||
