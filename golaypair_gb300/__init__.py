@@ -102,6 +102,7 @@ _STAGE_SIGS = {
     "gp_sort": [_P, _P, _i32, _cp],
     "gp_match": [_P, _i32, _i32, _i32, _cp, _cp, _cp, _i32, _P],
     "gp_uncompress": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp],
+    "gp_uncompress_lines": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp, _i64, _i64, _i64],
     "gp_equiv_filter": [_P, _i32, _i32, _cp, _cp],
 }
 

@@ -379,7 +379,16 @@ extern "C" {
 
 int gp_uncompress(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
                   const char* out_pairs, const char* work_dir, const char* prefix) {
+    return gp_uncompress_lines(c, order, compress, new_compress, paf, in_pairs, out_pairs, work_dir, prefix, 0,
+                               INT64_MAX, 1);
+}
+
+int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
+                        const char* out_pairs, const char* work_dir, const char* prefix, int64_t first, int64_t end_line,
+                        int64_t step) {
     if (!c || !in_pairs || !out_pairs) return GP_ERR_ARG;
+    if (first < 0 || step < 1) return c->fail(GP_ERR_ARG, "uncompress: bad line range (first %lld, step %lld)",
+                                              (long long)first, (long long)step);
     (void)work_dir;
     (void)prefix;
     cudaSetDevice(c->device);
@@ -410,6 +419,14 @@ int gp_uncompress(gp_ctx* c, int order, int compress, int new_compress, int paf,
     while (p < end && rc == GP_OK) {
         const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
         if (!nl) nl = end;
+        // lines outside [first, end_line) or off the step are left out
+        const int64_t this_line = line_no;
+        if (this_line < first || this_line >= end_line || (this_line - first) % step != 0) {
+            ++line_no;
+            p = nl + 1;
+            if (this_line >= end_line) break;
+            continue;
+        }
         std::vector<int> vals;
         std::string line(p, nl);
         const char* q = line.c_str();

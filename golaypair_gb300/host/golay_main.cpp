@@ -16,6 +16,7 @@
 // 88-90,147-149).  Every stage runs on the GPU through the C ABI in
 // include/golaypair_gb300.h; there is no CPU path.
 #include <cerrno>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -51,6 +52,10 @@ struct MatchOpts {
 struct UncompressOpts {
     std::string input_prefix = "pairs", internal_prefix = "filtered", sorted_prefix = "filtered_sorted";
     std::string output_prefix = "pairs", temp_prefix;
+    // the reference parses these but does not use them; here they select the
+    // input lines of the first level: --line N (1-based) or lines
+    // range_begin, range_begin + range_step, ... < range_end (0-based)
+    long long line = -1, range_begin = 0, range_end = -1, range_step = 1;
 };
 struct FilterOpts { std::string input_prefix = "pairs", output_prefix = "unique"; };
 
@@ -140,8 +145,20 @@ int stage_uncompress(const Options& o, const UncompressOpts& u) {
         const std::string prefix = i == 0 ? u.input_prefix : u.output_prefix;
         const std::string in = match_file(o, prefix, (int)i);
         const std::string out = match_file(o, u.output_prefix, (int)i + 1);
-        const int rc = gp_uncompress(g_ctx, o.order, o.compress[i], o.compress[i + 1], o.paf_constant, in.c_str(),
-                                     out.c_str(), o.work_dir().c_str(), u.temp_prefix.c_str());
+        int64_t first = 0, end = INT64_MAX, step = 1;
+        if (i == 0) {
+            if (u.line >= 1) {
+                first = u.line - 1;
+                end = u.line;
+            } else {
+                first = u.range_begin;
+                end = u.range_end >= 0 ? u.range_end : INT64_MAX;
+                step = u.range_step;
+            }
+        }
+        const int rc = gp_uncompress_lines(g_ctx, o.order, o.compress[i], o.compress[i + 1], o.paf_constant,
+                                           in.c_str(), out.c_str(), o.work_dir().c_str(), u.temp_prefix.c_str(),
+                                           first, end, step);
         if (rc < 0) return die("uncompress", rc);
     }
     return 0;
@@ -196,6 +213,8 @@ void usage() {
         "  sort                        File sorting step (-i,--input -o,--output)\n"
         "  match                       Candidate matching step (-i,--input -o,--output -a,--append BOOL)\n"
         "  uncompress                  Pair uncompression step (-i -o --internal --sorted -l -b -e -s -p,--prefix\n"
+        "                              -l N: only input line N (1-based); -b B -e E -s S: input lines\n"
+        "                              B, B+S, ... below E (0-based), for splitting one uncompression\n"
         "                              -d,--device [cpu,gpu]; both devices run on the GPU here)\n"
         "  filter                      Pair equivalence filter step\n");
 }
@@ -273,12 +292,11 @@ int main(int argc, char** argv) {
             if (a == "--internal") { unc.internal_prefix = next("--internal"); continue; }
             if (a == "--sorted") { unc.sorted_prefix = next("--sorted"); continue; }
             if (a == "-p" || a == "--prefix") { unc.temp_prefix = next("--prefix"); continue; }
-            // parsed but unused by the reference's stage_uncompress (src/main.cpp:110-113,192-195)
-            if (a == "-l" || a == "--line" || a == "-b" || a == "--range_begin" || a == "-e" || a == "--range_end" ||
-                a == "-s" || a == "--range_step") {
-                (void)next(a.c_str());
-                continue;
-            }
+            // parsed but unused by the reference (src/main.cpp:110-113,192-195): a line split here
+            if (a == "-l" || a == "--line") { unc.line = atoll(next("--line").c_str()); continue; }
+            if (a == "-b" || a == "--range_begin") { unc.range_begin = atoll(next("--range_begin").c_str()); continue; }
+            if (a == "-e" || a == "--range_end") { unc.range_end = atoll(next("--range_end").c_str()); continue; }
+            if (a == "-s" || a == "--range_step") { unc.range_step = atoll(next("--range_step").c_str()); continue; }
             if (a == "-d" || a == "--device") {
                 std::string v = next("--device");
                 for (auto& ch : v) ch = (char)tolower(ch);

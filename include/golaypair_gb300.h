@@ -242,6 +242,17 @@ int gp_match(gp_ctx* ctx, int order, int compress, int paf, const char* path_a, 
 int gp_uncompress(gp_ctx* ctx, int order, int compress, int new_compress, int paf, const char* in_pairs,
                   const char* out_pairs, const char* work_dir, const char* prefix);
 
+/* Same over the input lines first, first + step, ... below end_line
+ * (0-based; end_line = INT64_MAX: to the end), so that several processes
+ * or GPUs can split one uncompression: contiguous ranges whose outputs are
+ * concatenated in range order give the file of one call over all lines.
+ * This wires the reference's parsed-but-unused uncompress options --line,
+ * --range_begin, --range_end, --range_step (src/main.cpp:110-113,192-195),
+ * whose meaning the reference leaves undefined. */
+int gp_uncompress_lines(gp_ctx* ctx, int order, int compress, int new_compress, int paf, const char* in_pairs,
+                        const char* out_pairs, const char* work_dir, const char* prefix, int64_t first,
+                        int64_t end_line, int64_t step);
+
 /*
  * Replaces int cache_filter(int ORDER, int COMPRESS, const std::string& in,
  * const std::string& out) (src/core/filter/filter.h, filter.cpp:18-163):

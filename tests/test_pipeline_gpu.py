@@ -135,3 +135,24 @@ def test_sort_dedups_and_orders_bytewise(tmp_path):
         ctx.check(ctx._lib.gp_sort(ctx.handle, ctypes.cast(arr, ctypes.c_void_p), 1, str(out).encode()), "gp_sort")
     want = b"".join(sorted(set(lines)))
     assert out.read_bytes() == want
+
+
+def test_uncompress_line_ranges_split_the_work(tmp_path, golden_manifest):
+    """--range_begin/--range_end/--line (parsed but unused by the
+    reference): contiguous ranges, concatenated in order, give the file of
+    one uncompression over all lines; --line N gives line N's pairs."""
+    golay(["26", "-c", "2", "1", "gen", "sort", "match"], tmp_path)
+    _, wd = golay(["26", "-c", "2", "1", "uncompress"], tmp_path)
+    full = read(os.path.join(wd, "26-pairs-1"))
+    assert full == read(os.path.join(GOLDEN, "n26", "26-pairs-1"))
+    golay(["26", "-c", "2", "1", "uncompress", "-o", "pa", "-b", "0", "-e", "25"], tmp_path)
+    golay(["26", "-c", "2", "1", "uncompress", "-o", "pb", "-b", "25"], tmp_path)
+    parts = read(os.path.join(wd, "26-pa-1")) + read(os.path.join(wd, "26-pb-1"))
+    assert parts == full
+    # every line on its own, in order, also adds up to the whole file
+    n_in = read(os.path.join(wd, "26-pairs-2")).count(b"\n")
+    pieces = b""
+    for line in range(1, n_in + 1):
+        golay(["26", "-c", "2", "1", "uncompress", "-o", "pl", "--line", str(line)], tmp_path)
+        pieces += read(os.path.join(wd, "26-pl-1"))
+    assert pieces == full
