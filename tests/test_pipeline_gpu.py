@@ -149,10 +149,15 @@ def test_uncompress_line_ranges_split_the_work(tmp_path, golden_manifest):
     golay(["26", "-c", "2", "1", "uncompress", "-o", "pb", "-b", "25"], tmp_path)
     parts = read(os.path.join(wd, "26-pa-1")) + read(os.path.join(wd, "26-pb-1"))
     assert parts == full
-    # every line on its own, in order, also adds up to the whole file
-    n_in = read(os.path.join(wd, "26-pairs-2")).count(b"\n")
+    # lines 1..6 one at a time add up to the range [0, 6)
+    golay(["26", "-c", "2", "1", "uncompress", "-o", "p6", "-b", "0", "-e", "6"], tmp_path)
     pieces = b""
-    for line in range(1, n_in + 1):
+    for line in range(1, 7):
         golay(["26", "-c", "2", "1", "uncompress", "-o", "pl", "--line", str(line)], tmp_path)
         pieces += read(os.path.join(wd, "26-pl-1"))
-    assert pieces == full
+    assert pieces == read(os.path.join(wd, "26-p6-1"))
+    # a step: lines 0, 2, 4, ... and 1, 3, 5, ... together hold every pair
+    golay(["26", "-c", "2", "1", "uncompress", "-o", "pe", "-s", "2"], tmp_path)
+    golay(["26", "-c", "2", "1", "uncompress", "-o", "po", "-b", "1", "-s", "2"], tmp_path)
+    both = read(os.path.join(wd, "26-pe-1")) + read(os.path.join(wd, "26-po-1"))
+    assert sorted(both.splitlines()) == sorted(full.splitlines())
