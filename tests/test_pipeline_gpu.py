@@ -24,12 +24,10 @@ SUBCOMMANDS = {"gen", "sort", "match", "uncompress", "filter", "all"}
 
 
 def golay(args, tmp, check=True):
-    """Runs the golay driver with --dir between the options and the trailing
-    subcommands (global options precede subcommands)."""
+    """Runs the golay driver with --dir before the first subcommand (global
+    options precede subcommands)."""
     d = str(tmp)
-    i = len(args)
-    while i > 0 and args[i - 1] in SUBCOMMANDS:
-        i -= 1
+    i = next((k for k, a in enumerate(args) if a in SUBCOMMANDS), len(args))
     argv = [gp.CLI_PATH] + args[:i] + ["--dir", d] + args[i:]
     r = subprocess.run(argv, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=ENV)
     if check:
