@@ -241,6 +241,27 @@ __device__ __forceinline__ void psd_chunk(uint32_t taddr, int c0, float& pmax, f
     }
 }
 
+// The hi twiddles alone: eight bins from column c0, p = c_hi^2 + s_hi^2.
+template <int HB>
+__device__ __forceinline__ void psd_chunk_hi(uint32_t taddr, int c0, float& pmax, float& x0) {
+    float chi[8], shi[8];
+    tmem_ld8(taddr + c0, chi);
+    tmem_ld8(taddr + HB + c0, shi);
+    tmem_wait_ld();
+#pragma unroll
+    for (int k = 0; k < 8; k += 2) {
+        const float2 re = make_float2(chi[k], chi[k + 1]);
+        const float2 im = make_float2(shi[k], shi[k + 1]);
+        const float2 p = __ffma2_rn(re, re, __fmul2_rn(im, im));
+        if (c0 + k + 1 == HB - 1) {
+            pmax = fmaxf(pmax, p.x);
+            x0 = re.y;  // the ones row has no lo part: X_0 is exact here
+        } else {
+            pmax = fmax3(pmax, p.x, p.y);
+        }
+    }
+}
+
 // TR: per-role cycle counters (diagnostics build of the kernel).
 template <int K, int B, bool WRITE_PSD, bool TR>
 __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(PsdTcArgs a, SmemLayout lay) {
@@ -413,10 +434,25 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         const int q = warp & 3;  // TMEM lane quarter (warps 4..7)
         const float thr = a.thr;
         const float sq = sqrtf(thr);
-        // packed rows: |value| <= c, so sum|x| <= L c for every row
-        const float d_const = a.err_coef * (float)L * (float)a.alpha_c;
-        const float g_const = fmaxf(a.guard_cfg, 2.f * sq * d_const + 3.f * d_const * d_const + 1e-4f);
         constexpr int HB = K / 2;  // bins per half (cos block then sin block)
+        // Guard for a per-bin error bound |X^_k - X_k| <= coef * sum|x|.
+        // Packed rows: |value| <= c, so sum|x| <= L c.  int8 rows: by
+        // Parseval and Cauchy-Schwarz, S = sum|x| satisfies S^2 <= L sum x^2
+        // = X_0^2 + 2 sum_{k=1..H} p_k <= X_0^2 + 2H (sqrt(max p^) + coef S)^2
+        // (bin L/2 of an even L counted twice: still a bound), so
+        // S <= (|X_0| + sqrt(2H max p^)) / (1 - sqrt(2H) coef).
+        const float m2h = sqrtf(2.f * (float)(L / 2));
+        auto guard = [&](float pm, float x0v, float coef) {
+            float S;
+            if constexpr (B == 0)
+                S = (fabsf(x0v) + m2h * sqrtf(pm)) / (1.f - m2h * coef);
+            else
+                S = (float)L * (float)a.alpha_c;
+            const float d = coef * S;
+            return fmaxf(a.guard_cfg, 2.f * sq * d + 3.f * d * d + 1e-4f);
+        };
+        // the hi twiddles alone are within 2^-12 of the exact ones
+        const float coef_hi = a.err_coef + 2.44140625e-4f;
         Ring acc;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
@@ -432,19 +468,26 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const bool valid = row < n;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * C::N);
             // accumulator columns: [0, HB) cos hi, [HB, K) sin hi, [K, K + HB)
-            // cos lo, [K + HB, 2K) sin lo; cos column HB - 1 is the row sum X_0
-            float pmax = 0.f, x0 = 0.f;
+            // cos lo, [K + HB, 2K) sin lo; cos column HB - 1 is the row sum X_0.
+            // First the hi columns alone, with the wider hi-only guard: a
+            // row clearly below or above the bound is decided there.  Only
+            // a warp with a row inside that band reads the lo columns too
+            // (rare: about 1e-5 of the rows of the int8 workload).
+            float pmax = 0.f, x0 = 0.f, g = 0.f;
+            bool exact = WRITE_PSD;
+            if constexpr (!WRITE_PSD) {
 #pragma unroll
-            for (int c0 = 0; c0 < HB; c0 += 8)
-                psd_chunk<HB, WRITE_PSD>(taddr, c0, pmax, x0, valid ? a.psd_out + row * HB : nullptr);
-            float g = g_const;
-            if constexpr (B == 0) {
-                // Parseval: L sum x^2 = X_0^2 + 2 sum_{k=1..H} p_k (an upper
-                // bound for even L) <= X_0^2 + 2 H max_k p_k, raised by 1 % and
-                // by L for the fp32 error of the p_k; sum|x| <= sqrt(L sum x^2).
-                const float l_sumsq = fmaf(x0, x0, 2.f * (float)(L / 2) * pmax) * 1.01f + (float)L;
-                const float d = a.err_coef * sqrtf(l_sumsq);
-                g = fmaxf(a.guard_cfg, 2.f * sq * d + 3.f * d * d + 1e-4f);
+                for (int c0 = 0; c0 < HB; c0 += 8) psd_chunk_hi<HB>(taddr, c0, pmax, x0);
+                g = guard(pmax, x0, coef_hi);
+                const bool near = valid && pmax >= thr - g && pmax <= thr + g;
+                exact = __any_sync(0xFFFFFFFFu, near);
+            }
+            if (exact) {
+                pmax = 0.f;
+#pragma unroll
+                for (int c0 = 0; c0 < HB; c0 += 8)
+                    psd_chunk<HB, WRITE_PSD>(taddr, c0, pmax, x0, valid ? a.psd_out + row * HB : nullptr);
+                g = guard(pmax, x0, a.err_coef);
             }
             tc_fence_before();
             __syncwarp();
