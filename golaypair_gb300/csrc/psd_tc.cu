@@ -442,17 +442,24 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         // (bin L/2 of an even L counted twice: still a bound), so
         // S <= (|X_0| + sqrt(2H max p^)) / (1 - sqrt(2H) coef).
         const float m2h = sqrtf(2.f * (float)(L / 2));
-        auto guard = [&](float pm, float x0v, float coef) {
-            float S;
+        // per error coefficient: int8 rows d = coef / (1 - sqrt(2H) coef) *
+        // (|X_0| + sqrt(2H max p)); packed rows d = coef L c
+        struct Coef {
+            float sc, dc;
+        };
+        auto coef_of = [&](float coef) {
+            return Coef{coef / (1.f - m2h * coef), coef * (float)L * (float)a.alpha_c};
+        };
+        auto guard = [&](float pm, float x0v, Coef k) {
+            float d;
             if constexpr (B == 0)
-                S = (fabsf(x0v) + m2h * sqrtf(pm)) / (1.f - m2h * coef);
+                d = k.sc * fmaf(m2h, sqrtf(pm), fabsf(x0v));
             else
-                S = (float)L * (float)a.alpha_c;
-            const float d = coef * S;
-            return fmaxf(a.guard_cfg, 2.f * sq * d + 3.f * d * d + 1e-4f);
+                d = k.dc;
+            return fmaxf(a.guard_cfg, fmaf(2.f * sq, d, fmaf(3.f * d, d, 1e-4f)));
         };
         // the hi twiddles alone are within 2^-12 of the exact ones
-        const float coef_hi = a.err_coef + 2.44140625e-4f;
+        const Coef sc_hi = coef_of(a.err_coef + 2.44140625e-4f), sc_lo = coef_of(a.err_coef);
         Ring acc;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
@@ -478,7 +485,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             if constexpr (!WRITE_PSD) {
 #pragma unroll
                 for (int c0 = 0; c0 < HB; c0 += 8) psd_chunk_hi<HB>(taddr, c0, pmax, x0);
-                g = guard(pmax, x0, coef_hi);
+                g = guard(pmax, x0, sc_hi);
                 const bool near = valid && pmax >= thr - g && pmax <= thr + g;
                 exact = __any_sync(0xFFFFFFFFu, near);
             }
@@ -487,7 +494,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
 #pragma unroll
                 for (int c0 = 0; c0 < HB; c0 += 8)
                     psd_chunk<HB, WRITE_PSD>(taddr, c0, pmax, x0, valid ? a.psd_out + row * HB : nullptr);
-                g = guard(pmax, x0, a.err_coef);
+                g = guard(pmax, x0, sc_lo);
             }
             tc_fence_before();
             __syncwarp();
