@@ -458,8 +458,9 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 d = k.dc;
             return fmaxf(a.guard_cfg, fmaf(2.f * sq, d, fmaf(3.f * d, d, 1e-4f)));
         };
-        // the hi twiddles alone are within 2^-12 of the exact ones
-        const Coef sc_hi = coef_of(a.err_coef + 2.44140625e-4f), sc_lo = coef_of(a.err_coef);
+        // the hi twiddles alone are within 2^-12 of the exact ones per
+        // component: sqrt 2 * 2^-12 = 3.45267e-4 more on the modulus
+        const Coef sc_hi = coef_of(a.err_coef + 3.4527e-4f), sc_lo = coef_of(a.err_coef);
         Ring acc;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
@@ -733,13 +734,14 @@ bool tc_packed_supported(int L, int b) {
     return true;
 }
 
-// |X_k - X^_k| <= sum|x| * err_coef:  twiddle residual after the hi + lo
-// split (<= 2^-24) plus fp32 accumulation in the tensor core, bounded
-// generously as 17 roundings of relative size 2^-22 per UMMA step (2K/16
-// steps + the final) applied to partial sums no larger than sum|x|.
+// |X_k - X^_k| <= sum|x| * err_coef:  per component (real or imaginary
+// part) the twiddle residual after the hi + lo split (<= 2^-24) plus fp32
+// accumulation in the tensor core, bounded generously as 17 roundings of
+// relative size 2^-22 per UMMA step (2K/16 steps + the final) applied to
+// partial sums no larger than sum|x|; times sqrt 2 for the modulus.
 float tc_err_coef(int K) {
     const double steps = 2.0 * K / 16.0 + 1.0;
-    return (float)(std::ldexp(1.0, -24) + steps * 17.0 * std::ldexp(1.0, -22));
+    return (float)(std::sqrt(2.0) * (std::ldexp(1.0, -24) + steps * 17.0 * std::ldexp(1.0, -22)));
 }
 
 size_t build_twiddle_image(int L, int K, void* out) {
