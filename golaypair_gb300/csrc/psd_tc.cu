@@ -262,6 +262,30 @@ __device__ __forceinline__ void psd_chunk_hi(uint32_t taddr, int c0, float& pmax
     }
 }
 
+// The hi twiddles alone over all HB bins: every load issued before one wait.
+template <int HB>
+__device__ __forceinline__ void psd_hi_all(uint32_t taddr, float& pmax, float& x0) {
+    float chi[HB], shi[HB];
+#pragma unroll
+    for (int c0 = 0; c0 < HB; c0 += 8) {
+        tmem_ld8(taddr + c0, chi + c0);
+        tmem_ld8(taddr + HB + c0, shi + c0);
+    }
+    tmem_wait_ld();
+#pragma unroll
+    for (int k = 0; k < HB; k += 2) {
+        const float2 re = make_float2(chi[k], chi[k + 1]);
+        const float2 im = make_float2(shi[k], shi[k + 1]);
+        const float2 p = __ffma2_rn(re, re, __fmul2_rn(im, im));
+        if (k + 1 == HB - 1) {
+            pmax = fmaxf(pmax, p.x);
+            x0 = re.y;  // the ones row has no lo part: X_0 is exact here
+        } else {
+            pmax = fmax3(pmax, p.x, p.y);
+        }
+    }
+}
+
 // TR: per-role cycle counters (diagnostics build of the kernel).
 template <int K, int B, bool WRITE_PSD, bool TR>
 __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(PsdTcArgs a, SmemLayout lay) {
@@ -484,8 +508,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             float pmax = 0.f, x0 = 0.f, g = 0.f;
             bool exact = WRITE_PSD;
             if constexpr (!WRITE_PSD) {
-#pragma unroll
-                for (int c0 = 0; c0 < HB; c0 += 8) psd_chunk_hi<HB>(taddr, c0, pmax, x0);
+                psd_hi_all<HB>(taddr, pmax, x0);
                 g = guard(pmax, x0, sc_hi);
                 const bool near = valid && pmax >= thr - g && pmax <= thr + g;
                 exact = __any_sync(0xFFFFFFFFu, near);
