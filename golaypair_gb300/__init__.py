@@ -240,9 +240,9 @@ class Context:
         self._lib.gp_kernel_time(self._h, ctypes.byref(ms), ctypes.byref(n))
         return ms.value, n.value
 
-    TRACE_NAMES = ["conv_wait_raw", "conv_wait_a", "conv_work", "epi_wait_acc", "epi_wait_stash", "epi_work",
+    TRACE_NAMES = ["conv_wait_raw", "conv_wait_a", "conv_work", "epi_wait_acc", "epi_ld", "epi_work",
                    "mma_wait_a", "mma_wait_acc", "mma_issue", "prod_wait", "prod_issue", "tiles", "conv_fence",
-                   "mma_commit"]
+                   "mma_commit", "conv_st", "epi_tail"]
 
     def tc_trace(self, enable):
         """Reads (and resets) the tensor-core filter's per-role cycle counters."""

@@ -41,12 +41,16 @@ struct PsdTcArgs {
 };
 
 // Diagnostics counters written when PsdTcArgs::trace is set (summed over
-// CTAs, in SM clock cycles, one sample per warp and tile).
+// CTAs, in SM clock cycles, one sample per warp and tile).  conv_work
+// includes conv_st (the TMEM stores and their wait); epi_work includes
+// epi_ld (up to the hi accumulator columns landing in registers) and
+// epi_tail (after the accumulator is released).
 enum TcTrace {
     kTrConvWaitRaw = 0, kTrConvWaitA, kTrConvWork,
-    kTrEpiWaitAcc, kTrEpiWaitStash, kTrEpiWork,
+    kTrEpiWaitAcc, kTrEpiLd, kTrEpiWork,
     kTrMmaWaitA, kTrMmaWaitAcc, kTrMmaIssue,
-    kTrProdWait, kTrProdIssue, kTrTiles, kTrConvFence, kTrMmaCommit, kTrCount
+    kTrProdWait, kTrProdIssue, kTrTiles, kTrConvFence, kTrMmaCommit,
+    kTrConvSt, kTrEpiTail, kTrCount
 };
 
 // Builds the B-operand image (hi and lo twiddles) for length L, K = padded L.

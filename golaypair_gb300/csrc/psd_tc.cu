@@ -263,8 +263,9 @@ __device__ __forceinline__ void psd_chunk_hi(uint32_t taddr, int c0, float& pmax
 }
 
 // The hi twiddles alone over all HB bins: every load issued before one wait.
-template <int HB>
-__device__ __forceinline__ void psd_hi_all(uint32_t taddr, float& pmax, float& x0) {
+// t_ld: the cycle counter when the loads have landed (TR builds).
+template <int HB, bool TR>
+__device__ __forceinline__ void psd_hi_all(uint32_t taddr, float& pmax, float& x0, long long& t_ld) {
     float chi[HB], shi[HB];
 #pragma unroll
     for (int c0 = 0; c0 < HB; c0 += 8) {
@@ -272,6 +273,7 @@ __device__ __forceinline__ void psd_hi_all(uint32_t taddr, float& pmax, float& x
         tmem_ld8(taddr + HB + c0, shi + c0);
     }
     tmem_wait_ld();
+    t_ld = tclock<TR>();
 #pragma unroll
     for (int k = 0; k < HB; k += 2) {
         const float2 re = make_float2(chi[k], chi[k + 1]);
@@ -359,7 +361,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16) + (uint32_t)C::A_COL0;
         int it = 0;
         Ring raw, ast;
-        unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
+        unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0, tr4 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it, raw.next(RS), ast.next(C::AS)) {
             const int rs = raw.slot;
             const uint32_t rph = raw.phase;
@@ -433,11 +435,13 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 packed_row<B, 0, C::KCH>(sw, sLut, h);
             }
             const uint32_t aaddr = lane_base + (uint32_t)(as * (K / 2));
+            const long long c25t = tclock<TR>();
 #pragma unroll
             for (int g = 0; g < K / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
+            tmem_wait_st();
             const long long c3t = tclock<TR>();
             tr3 += c3t - c2t;
-            tmem_wait_st();
+            tr4 += c3t - c25t;
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
@@ -451,6 +455,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             atomicAdd(&a.trace[kTrConvWaitA], tr1);
             atomicAdd(&a.trace[kTrConvWork], tr3);
             atomicAdd(&a.trace[kTrConvFence], tr2 - tr3);
+            atomicAdd(&a.trace[kTrConvSt], tr4);
             if (warp == 0) atomicAdd(&a.trace[kTrTiles], (unsigned long long)it);
         }
     } else if (warp < kConvWarps + 4) {
@@ -474,10 +479,15 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         auto coef_of = [&](float coef) {
             return Coef{coef / (1.f - m2h * coef), coef * (float)L * (float)a.alpha_c};
         };
+        // sqrt(pm) <= (pm + T) / (2 sqrt T) (AM-GM; equality at pm = T, the
+        // only rows whose verdict the band can change); 1 + 2^-20 covers
+        // the rounding of the factor
+        const float hs = 0.5f / sq * 1.00000095367431640625f;
+        const float m2h_hs = m2h * hs, m2h_hs_t = m2h * hs * thr;
         auto guard = [&](float pm, float x0v, Coef k) {
             float d;
             if constexpr (B == 0)
-                d = k.sc * fmaf(m2h, sqrtf(pm), fabsf(x0v));
+                d = k.sc * (fmaf(m2h_hs, pm, m2h_hs_t) + fabsf(x0v));
             else
                 d = k.dc;
             return fmaxf(a.guard_cfg, fmaf(2.f * sq, d, fmaf(3.f * d, d, 1e-4f)));
@@ -486,7 +496,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         // component: sqrt 2 * 2^-12 = 3.45267e-4 more on the modulus
         const Coef sc_hi = coef_of(a.err_coef + 3.4527e-4f), sc_lo = coef_of(a.err_coef);
         Ring acc;
-        unsigned long long tr0 = 0, tr1 = 0, tr2 = 0;
+        unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
             const int b = acc.slot;
             const uint32_t ph = acc.phase;
@@ -506,9 +516,10 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             // a warp with a row inside that band reads the lo columns too
             // (rare: about 1e-5 of the rows of the int8 workload).
             float pmax = 0.f, x0 = 0.f, g = 0.f;
+            long long c_ld = c1t;
             bool exact = WRITE_PSD;
             if constexpr (!WRITE_PSD) {
-                psd_hi_all<HB>(taddr, pmax, x0);
+                psd_hi_all<HB, TR>(taddr, pmax, x0, c_ld);
                 g = guard(pmax, x0, sc_hi);
                 const bool near = valid && pmax >= thr - g && pmax <= thr + g;
                 exact = __any_sync(0xFFFFFFFFu, near);
@@ -523,6 +534,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[b]);
+            const long long c_rel = tclock<TR>();
+            tr1 += c_ld - c1t;
             const bool sure = valid && pmax < thr - g;
             const bool unsure = valid && !sure && pmax <= thr + g;
             const uint32_t bits = __ballot_sync(0xFFFFFFFFu, sure || unsure);
@@ -541,12 +554,15 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
                 }
             }
-            tr2 += tclock<TR>() - c1t;
+            const long long c_end = tclock<TR>();
+            tr2 += c_end - c1t;
+            tr3 += c_end - c_rel;
         }
         if (a.trace && lane == 0) {
             atomicAdd(&a.trace[kTrEpiWaitAcc], tr0);
-            atomicAdd(&a.trace[kTrEpiWaitStash], tr1);
-            atomicAdd(&a.trace[kTrEpiWork], tr2 - tr1);
+            atomicAdd(&a.trace[kTrEpiLd], tr1);
+            atomicAdd(&a.trace[kTrEpiWork], tr2);
+            atomicAdd(&a.trace[kTrEpiTail], tr3);
         }
     } else if (warp == kConvWarps + 4) {
         // ------------------------------------------------ producer
