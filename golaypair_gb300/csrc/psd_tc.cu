@@ -274,18 +274,21 @@ __device__ __forceinline__ void psd_hi_all(uint32_t taddr, float& pmax, float& x
     }
     tmem_wait_ld();
     t_ld = tclock<TR>();
+    float pm[2] = {pmax, 0.f};  // two independent max chains
 #pragma unroll
     for (int k = 0; k < HB; k += 2) {
         const float2 re = make_float2(chi[k], chi[k + 1]);
         const float2 im = make_float2(shi[k], shi[k + 1]);
         const float2 p = __ffma2_rn(re, re, __fmul2_rn(im, im));
+        float& m = pm[(k >> 1) & 1];
         if (k + 1 == HB - 1) {
-            pmax = fmaxf(pmax, p.x);
+            m = fmaxf(m, p.x);
             x0 = re.y;  // the ones row has no lo part: X_0 is exact here
         } else {
-            pmax = fmax3(pmax, p.x, p.y);
+            m = fmax3(m, p.x, p.y);
         }
     }
+    pmax = fmaxf(pm[0], pm[1]);
 }
 
 // TR: per-role cycle counters (diagnostics build of the kernel).
@@ -318,11 +321,14 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         const int64_t nd = (int64_t)*reinterpret_cast<const volatile unsigned long long*>(a.n_dev);
         if (nd < n) n = nd;
     }
-    const int64_t ntiles = (n + kTileM - 1) / kTileM;
+    // tile and row indices fit 32 bits (the launch refuses n >= 2^31)
+    const int ntiles = (int)((n + kTileM - 1) / kTileM);
     const int RS = (int)lay.raw_stages;
     const int row_bytes = B == 0 ? L : 16;
     const bool aligned =
         (reinterpret_cast<uintptr_t>(B == 0 ? (const void*)a.seqs : (const void*)a.words) & 15) == 0;
+    // tiles below nfull are whole and bulk-copied into shared memory
+    const int nfull = aligned ? (int)(n / kTileM) : 0;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < RS; ++i) {
@@ -362,7 +368,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         int it = 0;
         Ring raw, ast;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0, tr4 = 0;
-        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it, raw.next(RS), ast.next(C::AS)) {
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it, raw.next(RS), ast.next(C::AS)) {
             const int rs = raw.slot;
             const uint32_t rph = raw.phase;
             const int as = ast.slot;
@@ -375,8 +381,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             tr0 += c1t - c0t;
             tr1 += c2t - c1t;
             tc_fence_after();
-            const int64_t row = t * kTileM + r;
-            const bool full_tile = aligned && (t + 1) * kTileM <= n;
+            const int row = t * kTileM + r;
+            const bool full_tile = t < nfull;
             uint32_t h[K / 2];  // the row as fp16 pairs
             if constexpr (B == 0) {
                 if (full_tile) {
@@ -396,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                     }
                 } else {
                     const bool valid = row < n;
-                    const int8_t* src = a.seqs + (valid ? row : 0) * (int64_t)L;
+                    const int8_t* src = a.seqs + (int64_t)(valid ? row : 0) * L;
 #pragma unroll
                     for (int c = 0; c < C::KCH; ++c) {
                         uint32_t w[2] = {0u, 0u};
@@ -497,7 +503,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         const Coef sc_hi = coef_of(a.err_coef + 3.4527e-4f), sc_lo = coef_of(a.err_coef);
         Ring acc;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
-        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
             const int b = acc.slot;
             const uint32_t ph = acc.phase;
             const long long c0t = tclock<TR>();
@@ -506,7 +512,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             tr0 += c1t - c0t;
             tc_fence_after();
             const int r = q * 32 + lane;
-            const int64_t row = t * kTileM + r;
+            const int row = t * kTileM + r;
             const bool valid = row < n;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * C::N);
             // accumulator columns: [0, HB) cos hi, [HB, K) sin hi, [K, K + HB)
@@ -521,14 +527,16 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             if constexpr (!WRITE_PSD) {
                 psd_hi_all<HB, TR>(taddr, pmax, x0, c_ld);
                 g = guard(pmax, x0, sc_hi);
-                const bool near = valid && pmax >= thr - g && pmax <= thr + g;
+                // only picks the warps that redo the row exactly: the verdict
+                // below is taken with the same bounds either way
+                const bool near = valid && fabsf(pmax - thr) <= g;
                 exact = __any_sync(0xFFFFFFFFu, near);
             }
             if (exact) {
                 pmax = 0.f;
 #pragma unroll
                 for (int c0 = 0; c0 < HB; c0 += 8)
-                    psd_chunk<HB, WRITE_PSD>(taddr, c0, pmax, x0, valid ? a.psd_out + row * HB : nullptr);
+                    psd_chunk<HB, WRITE_PSD>(taddr, c0, pmax, x0, valid ? a.psd_out + (int64_t)row * HB : nullptr);
                 g = guard(pmax, x0, sc_lo);
             }
             tc_fence_before();
@@ -539,7 +547,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const bool sure = valid && pmax < thr - g;
             const bool unsure = valid && !sure && pmax <= thr + g;
             const uint32_t bits = __ballot_sync(0xFFFFFFFFu, sure || unsure);
-            const int64_t word = t * 4 + q;
+            const int word = t * 4 + q;
             if (lane == 0 && word < a.mask_words) a.mask[word] = bits;
             const uint32_t ub = __ballot_sync(0xFFFFFFFFu, unsure);
             if (ub) {
@@ -574,18 +582,18 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                                         : reinterpret_cast<const uint8_t*>(a.words);
             unsigned long long tr0 = 0, tr1 = 0;
             Ring raw;
-            for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it, raw.next(RS)) {
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it, raw.next(RS)) {
                 const int rs = raw.slot;
                 const uint32_t ph = raw.phase;
                 const long long c0 = tclock<TR>();
                 if (!mbar_wait(&raw_empty[rs], ph ^ 1u, abort_flag, a.status, 4)) break;
                 const long long c1 = tclock<TR>();
                 tr0 += c1 - c0;
-                const bool full_tile = aligned && (t + 1) * kTileM <= n;
+                const bool full_tile = t < nfull;
                 if (full_tile) {
                     const uint32_t bytes = (uint32_t)(kTileM * row_bytes);
                     mbar_arrive_expect_tx(&raw_full[rs], bytes);
-                    bulk_g2s(sRaw + rs * lay.raw_stride, src + t * kTileM * (int64_t)row_bytes, bytes, &raw_full[rs]);
+                    bulk_g2s(sRaw + rs * lay.raw_stride, src + (int64_t)t * kTileM * row_bytes, bytes, &raw_full[rs]);
                 } else {
                     mbar_arrive(&raw_full[rs]);
                 }
@@ -628,7 +636,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             bool ok = mbar_wait(b_full, 0, abort_flag, a.status, 5);
             Ring ast, acc;
             unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
-            for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ast.next(C::AS), acc.next(C::NACC)) {
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ast.next(C::AS), acc.next(C::NACC)) {
                 const int as = ast.slot;
                 const uint32_t aph = ast.phase;
                 const int b = acc.slot;
@@ -687,6 +695,7 @@ cudaError_t launch_kb(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
     const SmemLayout lay = smem_layout<K>(B == 0 ? a.L : 16);
     const int64_t ntiles = (a.n + kTileM - 1) / kTileM;
     if (ntiles == 0) return cudaSuccess;
+    if (a.n >= (int64_t(1) << 31)) return cudaErrorInvalidValue;  // 32-bit row indices
     // the counting variant exists for the int8 input only (diagnostics)
     auto kern = psd_tc_kernel<K, B, WP, false>;
     if constexpr (B == 0 && !WP)
