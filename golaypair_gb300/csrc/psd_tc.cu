@@ -310,6 +310,10 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     uint64_t* acc_empty = acc_full + C::NACC;
     uint64_t* b_full = acc_empty + C::NACC;
     uint64_t* final_bar = b_full + 1;
+    // 32-bit shared-window addresses of the barrier rings (8 bytes apart)
+    const uint32_t u_raw_full = smem_u32(raw_full), u_raw_empty = smem_u32(raw_empty);
+    const uint32_t u_a_full = smem_u32(a_full), u_a_empty = smem_u32(a_empty);
+    const uint32_t u_acc_full = smem_u32(acc_full), u_acc_empty = smem_u32(acc_empty);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + lay.misc_off);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + lay.misc_off + 4);
 
@@ -323,6 +327,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
     }
     // tile and row indices fit 32 bits (the launch refuses n >= 2^31)
     const int ntiles = (int)((n + kTileM - 1) / kTileM);
+    const int n32 = (int)n;
     const int RS = (int)lay.raw_stages;
     const int row_bytes = B == 0 ? L : 16;
     const bool aligned =
@@ -374,9 +379,9 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const int as = ast.slot;
             const uint32_t aph = ast.phase;
             const long long c0t = tclock<TR>();
-            if (!mbar_wait(&raw_full[rs], rph, abort_flag, a.status, 1)) break;
+            if (!mbar_wait(u_raw_full + 8u * rs, rph, abort_flag, a.status, 1)) break;
             const long long c1t = tclock<TR>();
-            if (!mbar_wait(&a_empty[as], aph ^ 1u, abort_flag, a.status, 2)) break;
+            if (!mbar_wait(u_a_empty + 8u * as, aph ^ 1u, abort_flag, a.status, 2)) break;
             const long long c2t = tclock<TR>();
             tr0 += c1t - c0t;
             tr1 += c2t - c1t;
@@ -451,8 +456,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
-                mbar_arrive(&a_full[as]);
-                mbar_arrive(&raw_empty[rs]);
+                mbar_arrive(u_a_full + 8u * as);
+                mbar_arrive(u_raw_empty + 8u * rs);
             }
             tr2 += tclock<TR>() - c2t;
         }
@@ -501,19 +506,20 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         // the hi twiddles alone are within 2^-12 of the exact ones per
         // component: sqrt 2 * 2^-12 = 3.45267e-4 more on the modulus
         const Coef sc_hi = coef_of(a.err_coef + 3.4527e-4f), sc_lo = coef_of(a.err_coef);
+        const int mask_words = (int)a.mask_words;
         Ring acc;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
             const int b = acc.slot;
             const uint32_t ph = acc.phase;
             const long long c0t = tclock<TR>();
-            if (!mbar_wait(&acc_full[b], ph, abort_flag, a.status, 3)) break;
+            if (!mbar_wait(u_acc_full + 8u * b, ph, abort_flag, a.status, 3)) break;
             const long long c1t = tclock<TR>();
             tr0 += c1t - c0t;
             tc_fence_after();
             const int r = q * 32 + lane;
             const int row = t * kTileM + r;
-            const bool valid = row < n;
+            const bool valid = row < n32;
             const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * C::N);
             // accumulator columns: [0, HB) cos hi, [HB, K) sin hi, [K, K + HB)
             // cos lo, [K + HB, 2K) sin lo; cos column HB - 1 is the row sum X_0.
@@ -541,14 +547,14 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_empty[b]);
+            if (lane == 0) mbar_arrive(u_acc_empty + 8u * b);
             const long long c_rel = tclock<TR>();
             tr1 += c_ld - c1t;
             const bool sure = valid && pmax < thr - g;
             const bool unsure = valid && !sure && pmax <= thr + g;
             const uint32_t bits = __ballot_sync(0xFFFFFFFFu, sure || unsure);
             const int word = t * 4 + q;
-            if (lane == 0 && word < a.mask_words) a.mask[word] = bits;
+            if (lane == 0 && word < mask_words) a.mask[word] = bits;
             const uint32_t ub = __ballot_sync(0xFFFFFFFFu, unsure);
             if (ub) {
                 unsigned long long basei = 0;
@@ -578,6 +584,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
         if (lane == 0) {
             mbar_arrive_expect_tx(b_full, C::B_BYTES);
             bulk_g2s(sB, a.bimage, C::B_BYTES, b_full);
+            const uint32_t u_raw = smem_u32(sRaw);
             const uint8_t* src = B == 0 ? reinterpret_cast<const uint8_t*>(a.seqs)
                                         : reinterpret_cast<const uint8_t*>(a.words);
             unsigned long long tr0 = 0, tr1 = 0;
@@ -586,16 +593,17 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 const int rs = raw.slot;
                 const uint32_t ph = raw.phase;
                 const long long c0 = tclock<TR>();
-                if (!mbar_wait(&raw_empty[rs], ph ^ 1u, abort_flag, a.status, 4)) break;
+                if (!mbar_wait(u_raw_empty + 8u * rs, ph ^ 1u, abort_flag, a.status, 4)) break;
                 const long long c1 = tclock<TR>();
                 tr0 += c1 - c0;
                 const bool full_tile = t < nfull;
                 if (full_tile) {
                     const uint32_t bytes = (uint32_t)(kTileM * row_bytes);
-                    mbar_arrive_expect_tx(&raw_full[rs], bytes);
-                    bulk_g2s(sRaw + rs * lay.raw_stride, src + (int64_t)t * kTileM * row_bytes, bytes, &raw_full[rs]);
+                    mbar_arrive_expect_tx(u_raw_full + 8u * rs, bytes);
+                    bulk_g2s(u_raw + (uint32_t)rs * lay.raw_stride, src + (int64_t)t * kTileM * row_bytes, bytes,
+                             u_raw_full + 8u * rs);
                 } else {
-                    mbar_arrive(&raw_full[rs]);
+                    mbar_arrive(u_raw_full + 8u * rs);
                 }
                 tr1 += tclock<TR>() - c1;
             }
@@ -642,9 +650,9 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 const int b = acc.slot;
                 const uint32_t bph = acc.phase;
                 const long long c0 = tclock<TR>();
-                if (!mbar_wait(&a_full[as], aph, abort_flag, a.status, 6)) break;
+                if (!mbar_wait(u_a_full + 8u * as, aph, abort_flag, a.status, 6)) break;
                 const long long c1 = tclock<TR>();
-                if (!mbar_wait(&acc_empty[b], bph ^ 1u, abort_flag, a.status, 9)) break;
+                if (!mbar_wait(u_acc_empty + 8u * b, bph ^ 1u, abort_flag, a.status, 9)) break;
                 const long long c2 = tclock<TR>();
                 tr0 += c1 - c0;
                 tr1 += c2 - c1;
@@ -658,8 +666,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                     umma_f16_ts(d, a0 + (uint32_t)(8 * ks), bdesc0 + (uint64_t)((2 * ks * C::B_KSTRIDE) >> 4), idesc,
                                 ks != 0 ? 1u : 0u);
                 const long long c3 = tclock<TR>();
-                umma_commit(&a_empty[as]);
-                umma_commit(&acc_full[b]);
+                umma_commit(u_a_empty + 8u * as);
+                umma_commit(u_acc_full + 8u * b);
                 const long long c4 = tclock<TR>();
                 tr2 += c3 - c2;
                 tr3 += c4 - c3;
