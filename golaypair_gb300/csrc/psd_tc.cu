@@ -291,6 +291,41 @@ __device__ __forceinline__ void psd_hi_all(uint32_t taddr, float& pmax, float& x
     pmax = fmaxf(pm[0], pm[1]);
 }
 
+// A row of a tile that is not whole or not bulk-copied (the last tile, or
+// an input not 16-byte aligned): byte loads from global memory, zeros past
+// row n or column L, stored as the A row at TMEM address aaddr.  Out of line: it runs at most once per CTA on aligned
+// input, and keeps its unrolled loads out of the hot loop's code.
+template <int K>
+__device__ __noinline__ void partial_row_store(const int8_t* seqs, int row, int n, int L, uint32_t aaddr) {
+    uint32_t h[K / 2];
+    const bool valid = row < n;
+    const int8_t* src = seqs + (int64_t)(valid ? row : 0) * L;
+#pragma unroll
+    for (int c = 0; c < K / 8; ++c) {
+        uint32_t w[2] = {0u, 0u};
+#pragma unroll
+        for (int bb = 0; bb < 8; ++bb) {
+            const int j = 8 * c + bb;
+            const uint32_t v = (valid && j < L) ? (uint32_t)(uint8_t)src[j] : 0u;
+            w[bb >> 2] |= v << (8 * (bb & 3));
+        }
+        i8x4_to_h2x2(w[0], h[4 * c], h[4 * c + 1]);
+        i8x4_to_h2x2(w[1], h[4 * c + 2], h[4 * c + 3]);
+    }
+#pragma unroll
+    for (int g = 0; g < K / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
+}
+
+// Both twiddle halves over all HB bins (the exact pass): max p and X_0.
+// Out of line: it runs for about 1e-5 of the warps of the int8 workload.
+template <int HB, bool WRITE_PSD>
+__device__ __noinline__ float2 exact_pass(uint32_t taddr, float* psd_row) {
+    float pmax = 0.f, x0 = 0.f;
+#pragma unroll
+    for (int c0 = 0; c0 < HB; c0 += 8) psd_chunk<HB, WRITE_PSD>(taddr, c0, pmax, x0, psd_row);
+    return make_float2(pmax, x0);
+}
+
 // TR: per-role cycle counters (diagnostics build of the kernel).
 template <int K, int B, bool WRITE_PSD, bool TR>
 __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(PsdTcArgs a, SmemLayout lay) {
@@ -389,6 +424,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const int row = t * kTileM + r;
             const bool full_tile = t < nfull;
             uint32_t h[K / 2];  // the row as fp16 pairs
+            const uint32_t aaddr = lane_base + (uint32_t)(as * (K / 2));
+            const long long c25t = tclock<TR>();
             if constexpr (B == 0) {
                 if (full_tile) {
                     const uint8_t* raw = sRaw + rs * lay.raw_stride;
@@ -406,20 +443,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                         i8x4_to_h2x2(hi, h[4 * c + 2], h[4 * c + 3]);
                     }
                 } else {
-                    const bool valid = row < n;
-                    const int8_t* src = a.seqs + (int64_t)(valid ? row : 0) * L;
-#pragma unroll
-                    for (int c = 0; c < C::KCH; ++c) {
-                        uint32_t w[2] = {0u, 0u};
-#pragma unroll
-                        for (int bb = 0; bb < 8; ++bb) {
-                            const int j = 8 * c + bb;
-                            const uint32_t v = (valid && j < L) ? (uint32_t)(uint8_t)src[j] : 0u;
-                            w[bb >> 2] |= v << (8 * (bb & 3));
-                        }
-                        i8x4_to_h2x2(w[0], h[4 * c], h[4 * c + 1]);
-                        i8x4_to_h2x2(w[1], h[4 * c + 2], h[4 * c + 3]);
-                    }
+                    partial_row_store<K>(a.seqs, row, n32, L, aaddr);
                 }
             } else {
                 uint4 wv;
@@ -445,10 +469,10 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 }
                 packed_row<B, 0, C::KCH>(sw, sLut, h);
             }
-            const uint32_t aaddr = lane_base + (uint32_t)(as * (K / 2));
-            const long long c25t = tclock<TR>();
+            if (B != 0 || full_tile) {
 #pragma unroll
-            for (int g = 0; g < K / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
+                for (int g = 0; g < K / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
+            }
             tmem_wait_st();
             const long long c3t = tclock<TR>();
             tr3 += c3t - c2t;
@@ -539,10 +563,9 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 exact = __any_sync(0xFFFFFFFFu, near);
             }
             if (exact) {
-                pmax = 0.f;
-#pragma unroll
-                for (int c0 = 0; c0 < HB; c0 += 8)
-                    psd_chunk<HB, WRITE_PSD>(taddr, c0, pmax, x0, valid ? a.psd_out + (int64_t)row * HB : nullptr);
+                const float2 px = exact_pass<HB, WRITE_PSD>(taddr, valid ? a.psd_out + (int64_t)row * HB : nullptr);
+                pmax = px.x;
+                x0 = px.y;
                 g = guard(pmax, x0, sc_lo);
             }
             tc_fence_before();
