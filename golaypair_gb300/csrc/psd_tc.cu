@@ -266,17 +266,11 @@ __device__ __forceinline__ void psd_chunk_hi(uint32_t taddr, int c0, float& pmax
 // t_ld: the cycle counter when the loads have landed (TR builds).
 template <int HB, bool TR>
 __device__ __forceinline__ void psd_hi_all(uint32_t taddr, float& pmax, float& x0, long long& t_ld) {
-    float chi[HB], shi[HB];
-    // 16-column loads, then an 8-column one when HB is not a multiple of 16
-#pragma unroll
-    for (int c0 = 0; c0 + 16 <= HB; c0 += 16) {
-        tmem_ld16(taddr + c0, chi + c0);
-        tmem_ld16(taddr + HB + c0, shi + c0);
-    }
-    if constexpr (HB % 16 != 0) {
-        tmem_ld8(taddr + HB - 8, chi + HB - 8);
-        tmem_ld8(taddr + 2 * HB - 8, shi + HB - 8);
-    }
+    // the cosine and sine columns are contiguous: [0, HB) and [HB, 2 HB)
+    float v[2 * HB];
+    tmem_ld_cols<2 * HB>(taddr, v);
+    const float* chi = v;
+    const float* shi = v + HB;
     tmem_wait_ld();
     t_ld = tclock<TR>();
     float pm[2] = {pmax, 0.f};  // two independent max chains
