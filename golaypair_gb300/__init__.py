@@ -20,6 +20,8 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "golaypair_gb300.h")
 
 GP_PSD_FP64 = 0
 GP_PSD_TC_GUARDED = 1
+GP_FORMAT_TEXT = 0
+GP_FORMAT_BINARY = 1
 
 _lib = None
 
@@ -104,6 +106,8 @@ _STAGE_SIGS = {
     "gp_uncompress": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp],
     "gp_uncompress_lines": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp, _i64, _i64, _i64],
     "gp_equiv_filter": [_P, _i32, _i32, _cp, _cp],
+    "gp_set_output_format": [_P, _i32],
+    "gp_export_text": [_P, _cp, _cp],
 }
 
 
@@ -113,6 +117,14 @@ def header_symbols():
     with open(HEADER) as f:
         text = f.read()
     return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(gp_\w+)\s*\(", text, re.M)))
+
+
+def export_text(in_path, out_path):
+    """gp_export_text without a context (host only): the text lines of a
+    binary survivor file."""
+    rc = lib().gp_export_text(None, str(in_path).encode(), str(out_path).encode())
+    if rc != 0:
+        raise GPError(f"gp_export_text failed ({rc}) on {in_path}")
 
 
 class Context:
@@ -180,6 +192,10 @@ class Context:
         self.check(self._lib.gp_psd_filter(self._h, seqs_ptr, n, L, order, paf, mode, mask_ptr, ctypes.byref(st)),
                    "gp_psd_filter")
         return st
+
+    def set_output_format(self, fmt):
+        """GP_FORMAT_TEXT or GP_FORMAT_BINARY for the generation files."""
+        self.check(self._lib.gp_set_output_format(self._h, fmt), "gp_set_output_format")
 
     def generate_window(self, order, compress, paf, begin, end, path_a, path_b):
         """gp_generate_window over word ranks [begin, end); returns GenStats."""

@@ -23,6 +23,7 @@
 #include "enumerate.h"
 #include "finalize.h"
 #include "host_math.h"
+#include "survivors.h"
 
 namespace {
 
@@ -40,46 +41,24 @@ struct GenPlan {
     std::vector<std::pair<int, int>> dec;
 };
 
-void put_uint(std::string& s, unsigned v) {
-    char tmp[12];
-    int n = 0;
-    do {
-        tmp[n++] = (char)('0' + v % 10);
-        v /= 10;
-    } while (v);
-    while (n) s.push_back(tmp[--n]);
-}
-
-void put_int(std::string& s, int v) {
-    if (v < 0) {
-        s.push_back('-');
-        put_uint(s, (unsigned)(-(long long)v));
-    } else {
-        put_uint(s, (unsigned)v);
-    }
-}
-
 // src/utils/io.cpp:14-36 line format
 void format_line(std::string& out, const GenPlan& p, gp::u128 word, const uint16_t* sig) {
-    out += "PSD";
-    for (int k = 0; k < p.L - 1; ++k) put_uint(out, sig[k]);
-    out.push_back(' ');
-    for (int j = 0; j < p.L; ++j) {
-        put_int(out, p.alpha[gp::word_digit_h(word, p.b, p.L, j)]);
-        out.push_back(' ');
-    }
-    out.push_back('\n');
+    gp::format_survivor_line(out, p.L, p.b, p.alpha.data(), word, sig);
 }
 
 // Writes the records in word order (the reference's FKM order).  Lines
 // are formatted by several host threads into per-thread buffers, then
 // written in order.
-int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, const char* path) {
+int write_records_binary(gp_ctx* c, const GenPlan& p, const RecordSet& recs, const std::vector<uint32_t>& order,
+                         int role, const char* path);
+
+int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, int role, const char* path) {
     const size_t n = recs.size();
     const int S = p.L - 1;
     std::vector<uint32_t> order(n);
     for (size_t i = 0; i < n; ++i) order[i] = (uint32_t)i;
     std::sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return recs.words[x] < recs.words[y]; });
+    if (c->out_format == GP_FORMAT_BINARY) return write_records_binary(c, p, recs, order, role, path);
     FILE* f = fopen(path, "w");
     if (!f) return c->fail(GP_ERR_IO, "cannot open %s for writing", path);
     const size_t per_block = 1 << 13;  // lines per formatting task
@@ -108,6 +87,43 @@ int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, const char
         for (unsigned t = 0; t < m; ++t)
             if (fwrite(bufs[t].data(), 1, bufs[t].size(), f) != bufs[t].size()) ok = false;
     }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? GP_OK : c->fail(GP_ERR_IO, "write failed: %s", path);
+}
+
+// The same records as a binary survivor file (survivors.h), in the same
+// order.
+int write_records_binary(gp_ctx* c, const GenPlan& p, const RecordSet& recs, const std::vector<uint32_t>& order,
+                         int role, const char* path) {
+    const size_t n = recs.size();
+    const int S = p.L - 1;
+    gp::SurvHeader h;
+    std::memset(&h, 0, sizeof h);
+    std::memcpy(h.magic, gp::kSurvMagic, 8);
+    h.version = 1;
+    h.order = p.order;
+    h.compress = p.compress;
+    h.paf = p.paf;
+    h.L = p.L;
+    h.k = p.k;
+    h.bits = p.b;
+    h.role = role;
+    uint16_t mx = 0;
+    for (uint16_t v : recs.sigs) mx = std::max(mx, v);
+    h.sig_bytes = mx <= 255 ? 1 : 2;
+    h.word_bytes = (p.b * p.L + 7) / 8;
+    h.count = n;
+    for (int i = 0; i < p.k && i < 16; ++i) h.alpha[i] = (int8_t)p.alpha[i];
+    const size_t rb = gp::surv_record_bytes(h);
+    std::vector<uint8_t> body(n * rb);
+    for (size_t i = 0; i < n; ++i) {
+        const uint32_t r = order[i];
+        gp::surv_put_record(body.data() + i * rb, h, recs.words[r], recs.sigs.data() + (size_t)r * S);
+    }
+    FILE* f = fopen(path, "wb");
+    if (!f) return c->fail(GP_ERR_IO, "cannot open %s for writing", path);
+    bool ok = fwrite(&h, sizeof h, 1, f) == 1;
+    if (n) ok = ok && fwrite(body.data(), 1, body.size(), f) == body.size();
     ok = (fclose(f) == 0) && ok;
     return ok ? GP_OK : c->fail(GP_ERR_IO, "write failed: %s", path);
 }
@@ -617,9 +633,9 @@ int plan_for(gp_ctx* c, int order, int compress, int paf, GenPlan& p) {
 
 int finish(gp_ctx* c, const GenPlan& p, const RecordSet& ra, const RecordSet& rb, const char* path_a,
            const char* path_b, gp_gen_stats* st) {
-    int rc = write_records(c, p, ra, path_a);
+    int rc = write_records(c, p, ra, 0, path_a);
     if (rc) return rc;
-    rc = write_records(c, p, rb, path_b);
+    rc = write_records(c, p, rb, 1, path_b);
     if (rc) return rc;
     st->written_a = (int64_t)ra.size();
     st->written_b = (int64_t)rb.size();

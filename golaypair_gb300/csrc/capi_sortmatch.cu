@@ -23,6 +23,7 @@
 
 #include "ctx.h"
 #include "prims.h"
+#include "survivors.h"
 
 namespace {
 
@@ -381,6 +382,12 @@ int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
     std::string all, one;
     for (int i = 0; i < n_in; ++i) {
         if (!slurp(in_paths[i], one)) return c->fail(GP_ERR_IO, "sort: cannot read %s", in_paths[i]);
+        gp::SurvHeader h;
+        const uint8_t* body = nullptr;
+        const int kind = gp::surv_parse(one, h, &body);
+        if (kind < 0 || (kind > 0 && !gp::surv_to_text(h, body, all)))
+            return c->fail(GP_ERR_FORMAT, "sort: malformed survivor file %s", in_paths[i]);
+        if (kind > 0) continue;
         all += one;
         if (!one.empty() && one.back() != '\n') all.push_back('\n');
     }

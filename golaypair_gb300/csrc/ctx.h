@@ -78,6 +78,7 @@ struct HostPinned {
 struct gp_ctx {
     int device = 0;
     int num_sms = 0;
+    int out_format = 0;  // GP_FORMAT_TEXT or GP_FORMAT_BINARY (generation files)
     cudaStream_t s_comp = nullptr;
     cudaStream_t s_copy = nullptr;
     static constexpr int kCopyStreams = 4;   // host->device copies of a chunk are split over these

@@ -10,7 +10,9 @@
 //   subcommands (any number, run in pipeline order): all gen sort match
 //   uncompress filter, with the reference's per-subcommand options; gen
 //   also takes --checkpoint FILE [--max-seconds S] [--max-iterations N]
-//   (not in the reference) for searches that stop and resume.
+//   (not in the reference) for searches that stop and resume, and --binary
+//   (binary survivor files, which sort reads and the export subcommand turns
+//   into the reference's text; export runs on the host without a GPU).
 //
 // Files and their names are the reference's (src/main.cpp:32-44,62-67,
 // 88-90,147-149).  Every stage runs on the GPU through the C ABI in
@@ -43,7 +45,10 @@ struct GenOpts {
     std::string checkpoint;  // not in the reference: resumable generation
     double max_seconds = 0;
     int max_iterations = 0;
+    bool binary = false;     // not in the reference: binary survivor files
 };
+// not in the reference: binary survivor files -> the reference's text
+struct ExportOpts { std::string input_prefix = "filtered", output_prefix = "filtered"; };
 struct SortOpts { std::string input_prefix = "filtered", output_prefix = "filtered_sorted"; };
 struct MatchOpts {
     std::string input_prefix = "filtered_sorted", output_prefix = "pairs";
@@ -81,6 +86,10 @@ std::string match_file(const Options& o, const std::string& prefix, int ci) {
 // src/main.cpp:47-54
 int stage_generate(const Options& o, const GenOpts& g) {
     gp_gen_stats st;
+    if (g.binary) {
+        const int frc = gp_set_output_format(g_ctx, GP_FORMAT_BINARY);
+        if (frc) return die("gen", frc);
+    }
     const std::string fa = cand_file(o, g.file_prefix, 'a', o.job_id);
     const std::string fb = cand_file(o, g.file_prefix, 'b', o.job_id);
     int done = 1;
@@ -105,6 +114,41 @@ int stage_generate(const Options& o, const GenOpts& g) {
            (long long)(st.written_a + st.written_b));
     printf("[gpu] candidates %lld, exact PSD passes %lld, tensor-core unsure %lld, %.3f s\n",
            (long long)st.candidates, (long long)st.psd_pass, (long long)st.unsure, st.seconds);
+    return 0;
+}
+
+// Text files of this job's binary survivor files (in place by default:
+// written to a temporary file, then renamed over the binary one).  Text
+// inputs are left as they are, or copied when the output is elsewhere.
+int stage_export(const Options& o, const ExportOpts& e) {
+    for (char ab : {'a', 'b'}) {
+        const std::string in = cand_file(o, e.input_prefix, ab, o.job_id);
+        const std::string out = cand_file(o, e.output_prefix, ab, o.job_id);
+        const std::string tmp = out + ".tmp";
+        int rc = gp_export_text(nullptr, in.c_str(), tmp.c_str());
+        if (rc == GP_ERR_FORMAT) {  // a text file already
+            std::remove(tmp.c_str());
+            if (in == out) continue;
+            FILE* fi = fopen(in.c_str(), "rb");
+            FILE* fo = fi ? fopen(tmp.c_str(), "wb") : nullptr;
+            bool ok = fi && fo;
+            char buf[1 << 16];
+            size_t got;
+            while (ok && (got = fread(buf, 1, sizeof buf, fi)) > 0) ok = fwrite(buf, 1, got, fo) == got;
+            if (fi) fclose(fi);
+            if (fo) ok = (fclose(fo) == 0) && ok;
+            rc = ok ? GP_OK : GP_ERR_IO;
+        }
+        if (rc) {
+            std::remove(tmp.c_str());
+            fprintf(stderr, "export: %s -> %s failed (%d)\n", in.c_str(), out.c_str(), rc);
+            return 1;
+        }
+        if (std::rename(tmp.c_str(), out.c_str()) != 0) {
+            fprintf(stderr, "export: cannot rename %s: %s\n", tmp.c_str(), strerror(errno));
+            return 1;
+        }
+    }
     return 0;
 }
 
@@ -210,6 +254,9 @@ void usage() {
         "  gen                         Candidate generation step (-o,--output)\n"
         "                              --checkpoint FILE [--max-seconds S] [--max-iterations N]:\n"
         "                              stop early and resume from FILE (exit code 75 = stopped)\n"
+        "                              --binary: write binary survivor files (see export)\n"
+        "  export                      Binary survivor files of this job -> the reference's text\n"
+        "                              (-i,--input -o,--output; default in place); sort reads both\n"
         "  sort                        File sorting step (-i,--input -o,--output)\n"
         "  match                       Candidate matching step (-i,--input -o,--output -a,--append BOOL)\n"
         "  uncompress                  Pair uncompression step (-i -o --internal --sorted -l -b -e -s -p,--prefix\n"
@@ -228,7 +275,9 @@ int main(int argc, char** argv) {
     MatchOpts mat;
     UncompressOpts unc;
     FilterOpts fil;
+    ExportOpts exp;
     bool s_all = false, s_gen = false, s_sort = false, s_match = false, s_unc = false, s_filter = false;
+    bool s_export = false;
     std::string ctx;  // current subcommand ("" = global)
     bool compress_given = false;
     for (int i = 1; i < argc; ++i) {
@@ -244,8 +293,10 @@ int main(int argc, char** argv) {
             usage();
             return 0;
         }
-        if (a == "all" || a == "gen" || a == "sort" || a == "match" || a == "uncompress" || a == "filter") {
+        if (a == "all" || a == "gen" || a == "sort" || a == "match" || a == "uncompress" || a == "filter" ||
+            a == "export") {
             ctx = a;
+            s_export |= a == "export";
             s_all |= a == "all";
             s_gen |= a == "gen";
             s_sort |= a == "sort";
@@ -275,6 +326,10 @@ int main(int argc, char** argv) {
             if (a == "--checkpoint") { gen.checkpoint = next("--checkpoint"); continue; }
             if (a == "--max-seconds") { gen.max_seconds = atof(next("--max-seconds").c_str()); continue; }
             if (a == "--max-iterations") { gen.max_iterations = atoi(next("--max-iterations").c_str()); continue; }
+            if (a == "--binary") { gen.binary = true; continue; }
+        } else if (ctx == "export") {
+            if (a == "-i" || a == "--input") { exp.input_prefix = next("--input"); continue; }
+            if (a == "-o" || a == "--output") { exp.output_prefix = next("--output"); continue; }
         } else if (ctx == "sort") {
             if (a == "-i" || a == "--input") { srt.input_prefix = next("--input"); continue; }
             if (a == "-o" || a == "--output") { srt.output_prefix = next("--output"); continue; }
@@ -322,7 +377,7 @@ int main(int argc, char** argv) {
         fprintf(stderr, "order is required\nRun with --help for more information.\n");
         return 106;
     }
-    if (!(s_all || s_gen || s_sort || s_match || s_unc || s_filter)) {
+    if (!(s_all || s_gen || s_sort || s_match || s_unc || s_filter || s_export)) {
         fprintf(stderr, "A subcommand is required\nRun with --help for more information.\n");
         return 106;
     }
@@ -330,6 +385,8 @@ int main(int argc, char** argv) {
         fprintf(stderr, "Failed to create temp directories: %s\n", strerror(errno));
         return 1;
     }
+    if (s_export && !(s_all || s_gen || s_sort || s_match || s_unc || s_filter))
+        return stage_export(opts, exp);  // host only: no GPU needed
     const char* dev = getenv("GP_DEVICE");
     int rc = gp_ctx_create(&g_ctx, dev ? atoi(dev) : 0);
     if (rc) {
@@ -338,6 +395,7 @@ int main(int argc, char** argv) {
     }
     int status = 0;
     if (!status && (s_gen || s_all)) status = stage_generate(opts, gen);
+    if (!status && s_export) status = stage_export(opts, exp);
     if (!status && (s_sort || s_all)) status = stage_sort(opts, srt);
     if (!status && (s_match || s_all)) status = stage_match(opts, mat);
     if (!status && (s_unc || s_all)) status = stage_uncompress(opts, unc);

@@ -165,6 +165,29 @@ int gp_generate_window_resumable(gp_ctx* ctx, int order, int compress, int paf, 
                                  const char* checkpoint_path, int max_iterations, double max_seconds, int* done,
                                  gp_gen_stats* stats);
 
+/*
+ * Format of the A and B files the generation entry points write (all of
+ * them, this context, from the next call on):
+ *   GP_FORMAT_TEXT   the reference's lines (src/utils/io.cpp:14-36), default;
+ *   GP_FORMAT_BINARY a binary survivor file: an 80-byte header (magic
+ *                    "GPSURV01", order, compress, paf, length, alphabet,
+ *                    bits per digit, role, field widths, record count) and
+ *                    one fixed-size record per line, in line order: the
+ *                    packed word, then the line's L-1 signature values in 1
+ *                    or 2 bytes each.  About a quarter of the text's size.
+ * gp_sort reads either format.  No counterpart in the reference, whose
+ * binary sketch (src/utils/binary.cpp:74-117) is never called.
+ */
+#define GP_FORMAT_TEXT 0
+#define GP_FORMAT_BINARY 1
+int gp_set_output_format(gp_ctx* ctx, int format);
+
+/* The text lines of a binary survivor file, byte for byte what the
+ * generation call that wrote it writes as text.  Host only: ctx may be NULL
+ * (then errors are only returned).  GP_ERR_FORMAT if in_path is not a valid
+ * survivor file. */
+int gp_export_text(gp_ctx* ctx, const char* in_path, const char* out_path);
+
 /* One job of a batched generation: the words of one order / compression
  * whose rank lies in [begin, end) (end clipped to the word space), written
  * to its own A and B files. */
@@ -211,7 +234,8 @@ int gp_tuned_settings(const gp_ctx* ctx, char* buf, int cap);
  * Replaces GNU_sort(const std::vector<std::string>& in, const std::string& out,
  * const std::string& tmpdir) (src/core/sort/sort.cpp:7-22), which runs
  * `sort | uniq` over the files: lines of all inputs, byte order (C locale),
- * adjacent duplicates removed, written to out_path.
+ * adjacent duplicates removed, written to out_path.  An input that is a
+ * binary survivor file (gp_set_output_format) contributes its text lines.
  */
 int gp_sort(gp_ctx* ctx, const char** in_paths, int n_in, const char* out_path);
 
