@@ -174,7 +174,8 @@ int gp_generate_window_resumable(gp_ctx* ctx, int order, int compress, int paf, 
  *                    bits per digit, role, field widths, record count) and
  *                    one fixed-size record per line, in line order: the
  *                    packed word, then the line's L-1 signature values in 1
- *                    or 2 bytes each.  About a quarter of the text's size.
+ *                    or 2 bytes each.  About a quarter of the text's size
+ *                    (3.9x smaller at order 57, compression 3).
  * gp_sort reads either format.  No counterpart in the reference, whose
  * binary sketch (src/utils/binary.cpp:74-117) is never called.
  */
