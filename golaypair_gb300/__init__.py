@@ -88,6 +88,7 @@ def lib():
         fn = getattr(L, name, None)
         if fn is not None:
             fn.argtypes = args
+    L.gp_debug_pair_generator_count.restype = ctypes.c_int64
     _lib = L
     return L
 
@@ -108,6 +109,7 @@ _STAGE_SIGS = {
     "gp_equiv_filter": [_P, _i32, _i32, _cp, _cp],
     "gp_set_output_format": [_P, _i32],
     "gp_export_text": [_P, _cp, _cp],
+    "gp_debug_pair_generator_count": [_i32, _i32],
 }
 
 

@@ -286,6 +286,11 @@ int gp_uncompress_lines(gp_ctx* ctx, int order, int compress, int new_compress, 
  */
 int gp_equiv_filter(gp_ctx* ctx, int order, int compress, const char* in_path, const char* out_path);
 
+/* Diagnostics: size of the pair-equivalence generator set gp_equiv_filter
+ * builds for length L (the closure of src/core/filter/filter.cpp:70-87), or
+ * -1 for an unsupported length.  Host only. */
+int64_t gp_debug_pair_generator_count(int L, int compress);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,3 +107,15 @@ def test_psd_batch_matches_scalar(oracle_lib):
         ok = all(psd[k] <= 2 * order + 0.001 for k in range(1, L // 2 + 1))
         assert ver[i] == ok
     assert n == ver.sum()
+
+
+@pytest.mark.parametrize("compress", [1, 2])
+def test_pair_generator_set_matches_oracle_closure(oracle_lib, compress):
+    """gp_equiv_filter builds the generator group from a generating subset
+    of the reference's operations; its size must equal the oracle's closure
+    under all of them (the subset's closure is contained in the full one, so
+    equal sizes mean equal sets)."""
+    import golaypair_gb300 as gp
+    lib = gp.lib()
+    for L in range(2, 23):
+        assert lib.gp_debug_pair_generator_count(L, compress) == oracle_lib.gpo_pair_generator_count(L, compress), L

@@ -159,3 +159,36 @@ def test_uncompress_line_ranges_split_the_work(tmp_path, golden_manifest):
     golay(["26", "-c", "2", "1", "uncompress", "-o", "po", "-b", "1", "-s", "2"], tmp_path)
     both = read(os.path.join(wd, "26-pe-1")) + read(os.path.join(wd, "26-po-1"))
     assert sorted(both.splitlines()) == sorted(full.splitlines())
+
+
+def _filter_gpu_vs_oracle(oracle_lib, tmp_path, order, pairs_file):
+    with gp.Context(0) as ctx:
+        ctx.check(ctx._lib.gp_equiv_filter(ctx.handle, order, 1, str(pairs_file).encode(),
+                                           str(tmp_path / "gpu").encode()), "gp_equiv_filter")
+    assert oracle_lib.gpo_equiv_filter(order, 1, str(pairs_file).encode(), str(tmp_path / "orc").encode()) == 0
+    got, want = read(tmp_path / "gpu"), read(tmp_path / "orc")
+    assert got == want
+    return got
+
+
+def test_filter_n32_matches_oracle(oracle_lib, tmp_path, golden_manifest):
+    """Equivalence filter of order-32 pairs at compression 1 (even length: the
+    alternating-negation generators are in the set): the first 3000 of the
+    90,320 pairs the 4 -> 2 -> 1 pipeline writes (checked against the
+    reference's hash by test_gen_matches_reference_hash)."""
+    _, wd = golay(golden_manifest["runs"]["n32_c421"]["argv"], tmp_path)
+    lines = read(os.path.join(wd, "32-pairs-1")).splitlines(keepends=True)
+    sub = tmp_path / "pairs3000"
+    sub.write_bytes(b"".join(lines[:3000]))
+    out = _filter_gpu_vs_oracle(oracle_lib, tmp_path, 32, sub)
+    assert 0 < out.count(b"\n") < 3000
+
+
+def test_filter_n57_matches_oracle(oracle_lib, tmp_path):
+    """Order 57, paf -2: the pairs at compression 1 of the first 200 pairs at
+    compression 3 (8208 generators per pair, several CTAs per pair)."""
+    golay(["57", "-c", "3", "1", "--paf", "-2", "gen", "sort", "match"], tmp_path)
+    _, wd = golay(["57", "-c", "3", "1", "--paf", "-2", "uncompress", "-e", "200"], tmp_path)
+    pairs = os.path.join(wd, "57-pairs-1")
+    assert read(pairs).count(b"\n") > 10
+    _filter_gpu_vs_oracle(oracle_lib, tmp_path, 57, pairs)
