@@ -415,7 +415,11 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const long long c0t = tclock<TR>();
             if (!mbar_wait(u_raw_full + 8u * rs, rph, abort_flag, a.status, 1)) break;
             const long long c1t = tclock<TR>();
-            if (!mbar_wait(u_a_empty + 8u * as, aph ^ 1u, abort_flag, a.status, 2)) break;
+            // with as many A stages as accumulators, the MMAs of the tile that
+            // last used this A stage completed when its accumulator was
+            // committed full: acc_full of the same slot stands for a_empty
+            if (!mbar_wait((C::AS == C::NACC ? u_acc_full : u_a_empty) + 8u * as, aph ^ 1u, abort_flag, a.status, 2))
+                break;
             const long long c2t = tclock<TR>();
             tr0 += c1t - c0t;
             tr1 += c2t - c1t;
@@ -688,7 +692,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                     umma_f16_ts(d, a0 + (uint32_t)(8 * ks), bdesc0 + (uint64_t)((2 * ks * C::B_KSTRIDE) >> 4), idesc,
                                 ks != 0 ? 1u : 0u);
                 const long long c3 = tclock<TR>();
-                umma_commit(u_a_empty + 8u * as);
+                if constexpr (C::AS != C::NACC) umma_commit(u_a_empty + 8u * as);
                 umma_commit(u_acc_full + 8u * b);
                 const long long c4 = tclock<TR>();
                 tr2 += c3 - c2;
