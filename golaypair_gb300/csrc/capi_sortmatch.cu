@@ -23,6 +23,7 @@
 
 #include "ctx.h"
 #include "prims.h"
+#include "host_par.h"
 #include "survivors.h"
 
 namespace {
@@ -138,53 +139,76 @@ struct Cand {
     size_t n = 0;
 };
 
-// Parses candidate lines: a first token, then exactly L integers.
+// Parses candidate lines: a first token, then exactly L integers.  Chunks
+// of whole lines are parsed by host threads, then joined in order.
 bool parse_candidates(const std::string& text, int L, Cand& out, std::string& err) {
-    const char* p = text.data();
-    const char* end = p + text.size();
-    while (p < end) {
-        const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
-        if (!nl) nl = end;
-        const char* q = p;
-        while (q < nl && *q == ' ') ++q;
-        if (q < nl) {
-            const char* t = q;
-            while (q < nl && *q != ' ') ++q;
-            out.tok_off.push_back((uint32_t)(t - text.data()));
-            out.tok_len.push_back((uint32_t)(q - t));
-            int got = 0;
-            while (got < L) {
-                while (q < nl && *q == ' ') ++q;
-                if (q >= nl) break;
-                char* e;
-                const long v = strtol(q, &e, 10);
-                if (e == q) break;
-                out.seqs.push_back((int8_t)v);
-                ++got;
-                q = e;
+    const char* base = text.data();
+    const char* tend = base + text.size();
+    const std::vector<size_t> cut = gp::line_chunks(base, text.size(), std::min<size_t>(4 * gp::host_threads(), text.size() / (1 << 18) + 1));
+    const size_t nc = cut.size() - 1;
+    std::vector<Cand> part(nc);
+    std::vector<char> bad(nc, 0);
+    gp::par_for(nc, [&](size_t k) {
+        Cand& o = part[k];
+        const char* p = base + cut[k];
+        const char* end = base + cut[k + 1];
+        while (p < end) {
+            const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
+            if (!nl) nl = end;
+            const char* q = p;
+            while (q < nl && *q == ' ') ++q;
+            if (q < nl) {
+                const char* t = q;
+                while (q < nl && *q != ' ') ++q;
+                o.tok_off.push_back((uint32_t)(t - base));
+                o.tok_len.push_back((uint32_t)(q - t));
+                int got = 0;
+                while (got < L) {
+                    while (q < nl && *q == ' ') ++q;
+                    if (q >= nl) break;
+                    const char* e;
+                    const long v = gp::read_long(q, tend, &e);
+                    if (e == q) break;
+                    o.seqs.push_back((int8_t)v);
+                    ++got;
+                    q = e;
+                }
+                if (got != L) {
+                    bad[k] = 1;
+                    return;
+                }
+                o.n++;
             }
-            if (got != L) {
-                err = "candidate line with fewer than L values";
-                return false;
-            }
-            out.n++;
+            p = nl + 1;
         }
-        p = nl + 1;
+    });
+    for (size_t k = 0; k < nc; ++k)
+        if (bad[k]) {
+            err = "candidate line with fewer than L values";
+            return false;
+        }
+    size_t n = 0, ns = 0;
+    for (const Cand& o : part) {
+        n += o.n;
+        ns += o.seqs.size();
+    }
+    out.tok_off.reserve(n);
+    out.tok_len.reserve(n);
+    out.seqs.reserve(ns);
+    for (const Cand& o : part) {
+        out.tok_off.insert(out.tok_off.end(), o.tok_off.begin(), o.tok_off.end());
+        out.tok_len.insert(out.tok_len.end(), o.tok_len.begin(), o.tok_len.end());
+        out.seqs.insert(out.seqs.end(), o.seqs.begin(), o.seqs.end());
+        out.n += o.n;
     }
     return true;
 }
 
+// src/io.cpp PairWriter line: a entries, one more space, b entries
 void put_pair(std::string& s, const int8_t* a, const int8_t* b, int L) {
-    char tmp[8];
-    for (int i = 0; i < L; ++i) {
-        int n = snprintf(tmp, sizeof tmp, "%d ", a[i]);
-        s.append(tmp, (size_t)n);
-    }
+    for (int i = 0; i < L; ++i) gp::put_int_sp(s, a[i]);
     s.push_back(' ');
-    for (int i = 0; i < L; ++i) {
-        int n = snprintf(tmp, sizeof tmp, "%d ", b[i]);
-        s.append(tmp, (size_t)n);
-    }
+    for (int i = 0; i < L; ++i) gp::put_int_sp(s, b[i]);
     s.push_back('\n');
 }
 
@@ -251,14 +275,27 @@ int gp_match_texts(gp_ctx* c, int L, int compress, int paf, const std::string& t
     GP_CUDA_TRY(c, cudaStreamSynchronize(s));
     std::vector<uint32_t> keep(nk);
     if (nk) GP_CUDA_TRY(c, cudaMemcpy(keep.data(), dlist.p, (size_t)nk * 4, cudaMemcpyDeviceToHost));
-    size_t g = 0;
-    for (uint32_t w : keep) {
-        while (g + 1 < gps.size() && gps[g + 1].first <= w) ++g;
-        const uint64_t off = w - gps[g].first;
-        const uint32_t ia = gps[g].a0 + (uint32_t)(off / gps[g].nb);
-        const uint32_t ib = gps[g].b0 + (uint32_t)(off % gps[g].nb);
-        put_pair(out, A.seqs.data() + (size_t)ia * L, B.seqs.data() + (size_t)ib * L, L);
-    }
+    // pair lines in order, formatted in blocks by host threads
+    const size_t per = 1 << 14;
+    const size_t nblk = (keep.size() + per - 1) / per;
+    std::vector<std::string> blk(nblk);
+    gp::par_for(nblk, [&](size_t bi) {
+        const size_t lo = bi * per, hi = std::min(keep.size(), lo + per);
+        std::string& o = blk[bi];
+        o.reserve((hi - lo) * (size_t)(6 * L + 2));
+        size_t g = (size_t)(std::upper_bound(gps.begin(), gps.end(), (uint64_t)keep[lo],
+                                             [](uint64_t w, const GroupPair& x) { return w < x.first; }) -
+                            gps.begin()) - 1;
+        for (size_t k = lo; k < hi; ++k) {
+            const uint32_t w = keep[k];
+            while (g + 1 < gps.size() && gps[g + 1].first <= w) ++g;
+            const uint64_t off = w - gps[g].first;
+            const uint32_t ia = gps[g].a0 + (uint32_t)(off / gps[g].nb);
+            const uint32_t ib = gps[g].b0 + (uint32_t)(off % gps[g].nb);
+            put_pair(o, A.seqs.data() + (size_t)ia * L, B.seqs.data() + (size_t)ib * L, L);
+        }
+    });
+    for (const std::string& o : blk) out += o;
     if (n_pairs) *n_pairs = nk;
     return GP_OK;
 }
@@ -302,21 +339,42 @@ int gp_sort_text(gp_ctx* c, const std::string& text, std::string& out) {
     size_t maxlen = 0;
     bool nibble = true;
     {
-        const char* p = text.data();
-        const char* end = p + text.size();
-        while (p < end) {
-            const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
-            const size_t l = nl ? (size_t)(nl - p) : (size_t)(end - p);
-            start.push_back((uint64_t)(p - text.data()));
-            len.push_back((uint32_t)l);
-            maxlen = std::max(maxlen, l);
-            p += l + 1;
-        }
-        for (unsigned char ch : text)
-            if (ch != '\n' && code4(ch) < 0) {
-                nibble = false;
-                break;
+        // lines and the character check, by chunks of whole lines on host
+        // threads, joined in order
+        const char* base = text.data();
+        const std::vector<size_t> cut = gp::line_chunks(base, text.size(), std::min<size_t>(4 * gp::host_threads(), text.size() / (1 << 18) + 1));
+        const size_t nc = cut.size() - 1;
+        std::vector<std::vector<uint64_t>> ps(nc);
+        std::vector<std::vector<uint32_t>> pl(nc);
+        std::vector<size_t> pmax(nc, 0);
+        std::vector<char> pnib(nc, 1);
+        gp::par_for(nc, [&](size_t k) {
+            const char* p = base + cut[k];
+            const char* end = base + cut[k + 1];
+            for (const char* q = p; q < end; ++q)
+                if (*q != '\n' && code4((unsigned char)*q) < 0) {
+                    pnib[k] = 0;
+                    break;
+                }
+            while (p < end) {
+                const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
+                const size_t l = nl ? (size_t)(nl - p) : (size_t)(end - p);
+                ps[k].push_back((uint64_t)(p - base));
+                pl[k].push_back((uint32_t)l);
+                pmax[k] = std::max(pmax[k], l);
+                p += l + 1;
             }
+        });
+        size_t tot = 0;
+        for (size_t k = 0; k < nc; ++k) tot += ps[k].size();
+        start.reserve(tot);
+        len.reserve(tot);
+        for (size_t k = 0; k < nc; ++k) {
+            start.insert(start.end(), ps[k].begin(), ps[k].end());
+            len.insert(len.end(), pl[k].begin(), pl[k].end());
+            maxlen = std::max(maxlen, pmax[k]);
+            nibble = nibble && pnib[k];
+        }
     }
     const int64_t n = (int64_t)start.size();
     out.clear();
@@ -350,11 +408,20 @@ int gp_sort_text(gp_ctx* c, const std::string& text, std::string& out) {
     GP_CUDA_TRY(c, cudaStreamSynchronize(s));
     std::vector<uint32_t> order(nu);
     if (nu) GP_CUDA_TRY(c, cudaMemcpy(order.data(), dout.p, (size_t)nu * 4, cudaMemcpyDeviceToHost));
-    out.reserve(text.size() + 1);
-    for (uint32_t i : order) {
-        out.append(text.data() + start[i], len[i]);
-        out.push_back('\n');
-    }
+    // output: each kept line and its newline at a prefix-sum offset, copied
+    // by host threads
+    std::vector<size_t> at(nu + 1, 0);
+    for (uint32_t k = 0; k < nu; ++k) at[k + 1] = at[k] + len[order[k]] + 1;
+    out.resize(at[nu]);
+    const size_t lines_per = 1 << 15;
+    gp::par_for((nu + lines_per - 1) / lines_per, [&](size_t bi) {
+        const size_t lo = bi * lines_per, hi = std::min<size_t>(nu, lo + lines_per);
+        for (size_t k = lo; k < hi; ++k) {
+            const uint32_t i = order[k];
+            std::memcpy(&out[at[k]], text.data() + start[i], len[i]);
+            out[at[k] + len[i]] = '\n';
+        }
+    });
     return GP_OK;
 }
 
