@@ -109,6 +109,7 @@ _STAGE_SIGS = {
     "gp_equiv_filter": [_P, _i32, _i32, _cp, _cp],
     "gp_set_output_format": [_P, _i32],
     "gp_export_text": [_P, _cp, _cp],
+    "gp_set_spectral_prune": [_P, _i32],
     "gp_debug_pair_generator_count": [_i32, _i32],
 }
 
@@ -194,6 +195,11 @@ class Context:
         self.check(self._lib.gp_psd_filter(self._h, seqs_ptr, n, L, order, paf, mode, mask_ptr, ctypes.byref(st)),
                    "gp_psd_filter")
         return st
+
+    def set_spectral_prune(self, on):
+        """Drop generation candidates that cannot have a complementary partner
+        (gp_set_spectral_prune)."""
+        self.check(self._lib.gp_set_spectral_prune(self._h, 1 if on else 0), "gp_set_spectral_prune")
 
     def set_output_format(self, fmt):
         """GP_FORMAT_TEXT or GP_FORMAT_BINARY for the generation files."""

@@ -421,6 +421,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
             fa.rec_cap = j.rcap;
             fa.psd_pass = ctr + kCumBase + ji * kCumSlots + 2;
             fa.status = c->status.as<int>();
+            fa.prune_tab = c->spectral_prune && fa.bound < kPruneTab ? c->prune_tab.as<uint8_t>() : nullptr;
             GP_CUDA_TRY(c, gp::launch_finalize(fa, j.hard, c->num_sms, sj));
             GP_CUDA_TRY(c, cudaEventRecord(c->ev_join[ji], sj));
             GP_CUDA_TRY(c, cudaStreamWaitEvent(s, c->ev_join[ji], 0));

@@ -1,7 +1,9 @@
-// capi_survivors.cu -- the output format switch of generation and the text
-// exporter of binary survivor files (format in survivors.h).  Host code only.
+// capi_survivors.cu -- generation output options: the file format switch,
+// the text exporter of binary survivor files (format in survivors.h), and
+// the spectral pruning switch (its lookup table).
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "ctx.h"
 #include "survivors.h"
@@ -33,6 +35,23 @@ int gp_set_output_format(gp_ctx* c, int format) {
     if (format != GP_FORMAT_TEXT && format != GP_FORMAT_BINARY)
         return c->fail(GP_ERR_ARG, "unknown output format %d", format);
     c->out_format = format;
+    return GP_OK;
+}
+
+int gp_set_spectral_prune(gp_ctx* c, int on) {
+    if (!c) return GP_ERR_ARG;
+    if (on && !c->prune_tab.p) {
+        // m <= kPruneTab - 1: squares, and norms x^2 + xy + y^2 (x, y >= 0;
+        // the same set as a^2 - ab + b^2 over all integers)
+        std::vector<uint8_t> tab(kPruneTab, 0);
+        for (int x = 0; x * x < kPruneTab; ++x) tab[x * x] |= 1;
+        for (int x = 0; x * x < kPruneTab; ++x)
+            for (int y = 0; y <= x && x * x + x * y + y * y < kPruneTab; ++y) tab[x * x + x * y + y * y] |= 2;
+        cudaSetDevice(c->device);
+        if (!c->prune_tab.ensure(kPruneTab)) return c->fail(GP_ERR_NOMEM, "spectral prune table");
+        GP_CUDA_TRY(c, cudaMemcpy(c->prune_tab.p, tab.data(), kPruneTab, cudaMemcpyHostToDevice));
+    }
+    c->spectral_prune = on ? 1 : 0;
     return GP_OK;
 }
 

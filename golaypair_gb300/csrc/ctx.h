@@ -75,10 +75,16 @@ struct HostPinned {
     }
 };
 
+// entries of the spectral pruning table (values 0 .. kPruneTab - 1; orders
+// whose bound 2n - paf is larger are not pruned)
+constexpr int kPruneTab = 4096;
+
 struct gp_ctx {
     int device = 0;
     int num_sms = 0;
     int out_format = 0;  // GP_FORMAT_TEXT or GP_FORMAT_BINARY (generation files)
+    int spectral_prune = 0;  // gp_set_spectral_prune
+    DevBuf prune_tab;        // uint8_t[kPruneTab]: bit 0 square, bit 1 Eisenstein norm
     cudaStream_t s_comp = nullptr;
     cudaStream_t s_copy = nullptr;
     static constexpr int kCopyStreams = 4;   // host->device copies of a chunk are split over these

@@ -82,6 +82,20 @@ __global__ void __launch_bounds__(kWarps * 32) finalize_kernel(FinalizeArgs a) {
         __syncwarp();
         if (fail) continue;
         if (lane == 0) atomicAdd(a.psd_pass, 1ull);
+        if (a.prune_tab) {
+            // p(L/2) is the square of the alternating sum and p(L/3) the norm
+            // of an Eisenstein integer: both exact integers here
+            bool keep = true;
+            if (L % 2 == 0) {
+                const int m = a.bound - __double2int_rn(psd[L / 2]);
+                keep = m >= 0 && m <= a.bound && (a.prune_tab[m] & 1);
+            }
+            if (keep && L % 3 == 0) {
+                const int m = a.bound - __double2int_rn(psd[L / 3]);
+                keep = m >= 0 && m <= a.bound && (a.prune_tab[m] & 2);
+            }
+            if (!keep) continue;
+        }
         const uint8_t roles = a.roles ? a.roles[row] : a.fixed_role;
         for (int r = 0; r < 2; ++r) {
             if (!((roles >> r) & 1)) continue;

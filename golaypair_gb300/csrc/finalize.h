@@ -31,6 +31,12 @@ struct FinalizeArgs {
     int64_t rec_cap;
     unsigned long long* psd_pass;
     int* status;
+    // optional spectral pruning (nullptr = off): prune_tab[m] bit 0 = m is a
+    // square, bit 1 = m is a norm a^2 - ab + b^2 of an Eisenstein integer,
+    // for 0 <= m <= bound.  A candidate is dropped when bound - p(L/2) (even
+    // L) is not a square, or bound - p(L/3) (L divisible by 3) not a norm:
+    // no complementary partner can exist (p_A(k) + p_B(k) = bound exactly).
+    const uint8_t* prune_tab = nullptr;
 };
 
 // Lists the set bits of mask[0 .. n) (n = min(n, *n_dev) when n_dev is set).

@@ -46,6 +46,7 @@ struct GenOpts {
     double max_seconds = 0;
     int max_iterations = 0;
     bool binary = false;     // not in the reference: binary survivor files
+    bool prune = false;      // not in the reference: spectral pruning of candidates
 };
 // not in the reference: binary survivor files -> the reference's text
 struct ExportOpts { std::string input_prefix = "filtered", output_prefix = "filtered"; };
@@ -89,6 +90,10 @@ int stage_generate(const Options& o, const GenOpts& g) {
     if (g.binary) {
         const int frc = gp_set_output_format(g_ctx, GP_FORMAT_BINARY);
         if (frc) return die("gen", frc);
+    }
+    if (g.prune) {
+        const int prc = gp_set_spectral_prune(g_ctx, 1);
+        if (prc) return die("gen", prc);
     }
     const std::string fa = cand_file(o, g.file_prefix, 'a', o.job_id);
     const std::string fb = cand_file(o, g.file_prefix, 'b', o.job_id);
@@ -255,6 +260,8 @@ void usage() {
         "                              --checkpoint FILE [--max-seconds S] [--max-iterations N]:\n"
         "                              stop early and resume from FILE (exit code 75 = stopped)\n"
         "                              --binary: write binary survivor files (see export)\n"
+        "                              --spectral-prune: leave out candidates that cannot have a\n"
+        "                              partner (p(L/2), p(L/3) tests); pair files are unchanged\n"
         "  export                      Binary survivor files of this job -> the reference's text\n"
         "                              (-i,--input -o,--output; default in place); sort reads both\n"
         "  sort                        File sorting step (-i,--input -o,--output)\n"
@@ -327,6 +334,7 @@ int main(int argc, char** argv) {
             if (a == "--max-seconds") { gen.max_seconds = atof(next("--max-seconds").c_str()); continue; }
             if (a == "--max-iterations") { gen.max_iterations = atoi(next("--max-iterations").c_str()); continue; }
             if (a == "--binary") { gen.binary = true; continue; }
+            if (a == "--spectral-prune") { gen.prune = true; continue; }
         } else if (ctx == "export") {
             if (a == "-i" || a == "--input") { exp.input_prefix = next("--input"); continue; }
             if (a == "-o" || a == "--output") { exp.output_prefix = next("--output"); continue; }

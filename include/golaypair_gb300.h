@@ -183,6 +183,20 @@ int gp_generate_window_resumable(gp_ctx* ctx, int order, int compress, int paf, 
 #define GP_FORMAT_BINARY 1
 int gp_set_output_format(gp_ctx* ctx, int format);
 
+/*
+ * Spectral pruning of the generation files (off by default; this context,
+ * from the next call on).  Every complementary pair (A, B) has
+ * p_A(k) + p_B(k) = 2n - paf exactly for k != 0 (Parseval with the PAF
+ * condition and the row sums), and p(L/2) is the square of an integer (even
+ * L) and p(L/3) a norm a^2 - ab + b^2 of an Eisenstein integer (L divisible
+ * by 3).  With pruning on, a candidate whose 2n - paf - p(L/2) is not a
+ * square, or whose 2n - paf - p(L/3) is not such a norm, is not written: it
+ * has no partner.  The pair files that match writes are unchanged; the
+ * candidate files are smaller.  No counterpart in the reference, whose
+ * sketches of these checks (src/utils/fourier.cpp:75-195) are never called.
+ */
+int gp_set_spectral_prune(gp_ctx* ctx, int on);
+
 /* The text lines of a binary survivor file, byte for byte what the
  * generation call that wrote it writes as text.  Host only: ctx may be NULL
  * (then errors are only returned).  GP_ERR_FORMAT if in_path is not a valid

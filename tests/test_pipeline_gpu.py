@@ -192,3 +192,57 @@ def test_filter_n57_matches_oracle(oracle_lib, tmp_path):
     pairs = os.path.join(wd, "57-pairs-1")
     assert read(pairs).count(b"\n") > 10
     _filter_gpu_vs_oracle(oracle_lib, tmp_path, 57, pairs)
+
+
+def _lines(path):
+    return read(path).count(b"\n")
+
+
+def test_spectral_prune_keeps_reference_pairs_n16(tmp_path, golden_manifest):
+    """Length 8 (even): gen --spectral-prune writes fewer candidates, and the
+    sorted-match pairs are still the reference's."""
+    files = golden_manifest["runs"]["n16"]["files"]
+    _, wd = golay(["16", "-c", "2", "gen", "--spectral-prune", "sort", "match"], tmp_path)
+    assert hashlib.sha256(read(os.path.join(wd, "16-pairs-2"))).hexdigest() == files["16-pairs-2"]["sha256"]
+    kept = _lines(os.path.join(wd, "16-filtered-a#0")) + _lines(os.path.join(wd, "16-filtered-b#0"))
+    assert kept < files["16-filtered-a#0"]["lines"] + files["16-filtered-b#0"]["lines"]
+
+
+def test_spectral_prune_keeps_reference_pairs_n32(tmp_path, golden_manifest):
+    """Order 32 at compression 4 (length 8), uncompressed 4 -> 2 -> 1: every
+    pair file equals the reference's."""
+    rec = golden_manifest["runs"]["n32_c421"]
+    argv = list(rec["argv"])
+    argv.insert(argv.index("gen") + 1, "--spectral-prune")
+    _, wd = golay(argv, tmp_path)
+    for fn in ("32-pairs-4", "32-pairs-2", "32-pairs-1"):
+        assert hashlib.sha256(read(os.path.join(wd, fn))).hexdigest() == rec["files"][fn]["sha256"], fn
+
+
+@pytest.mark.parametrize("order,compress,paf", [(36, 2, 0), (21, 1, -2)])
+def test_spectral_prune_same_pairs(tmp_path, order, compress, paf):
+    """Lengths 18 (both the L/2 and the L/3 test apply) and 21 (the L/3 test):
+    the same pair file with and without pruning, from no more candidates."""
+    args = [str(order), "-c", str(compress), "--paf", str(paf)]
+    _, w0 = golay(args + ["gen", "sort", "match"], tmp_path / "plain")
+    _, w1 = golay(args + ["gen", "--spectral-prune", "sort", "match"], tmp_path / "pruned")
+    pairs = f"{order}-pairs-{compress}"
+    assert read(os.path.join(w1, pairs)) == read(os.path.join(w0, pairs))
+    n0 = _lines(os.path.join(w0, f"{order}-filtered_sorted-a")) + _lines(os.path.join(w0, f"{order}-filtered_sorted-b"))
+    n1 = _lines(os.path.join(w1, f"{order}-filtered_sorted-a")) + _lines(os.path.join(w1, f"{order}-filtered_sorted-b"))
+    assert n1 < n0
+
+
+def test_spectral_identity_at_third_bin_order57(tmp_path):
+    """p_A(L/3) + p_B(L/3) = 2n - paf on the order-57 pairs at compression 1
+    (length 57): the identity the L/3 test rests on, on real pairs."""
+    golay(["57", "-c", "3", "1", "--paf", "-2", "gen", "sort", "match"], tmp_path)
+    _, wd = golay(["57", "-c", "3", "1", "--paf", "-2", "uncompress", "-e", "200"], tmp_path)
+    lines = read(os.path.join(wd, "57-pairs-1")).decode().splitlines()
+    assert lines
+    for line in lines:
+        v = [int(x) for x in line.split()]
+        pa = np.abs(np.fft.fft(np.array(v[:57]))) ** 2
+        pb = np.abs(np.fft.fft(np.array(v[57:]))) ** 2
+        assert abs(pa[19] + pb[19] - (2 * 57 + 2)) < 1e-6
+        assert abs(pa[19] - round(pa[19])) < 1e-6

@@ -117,3 +117,23 @@ def test_cli_export_runs_without_a_gpu(tmp_path):
     assert r.returncode == 0, r.stderr
     for ab in "ab":
         assert (wd / f"26-filtered-{ab}#0").read_bytes() == read(os.path.join(GOLDEN, "n26", f"26-filtered-{ab}_0"))
+
+
+@pytest.mark.parametrize("name,order,fn,L", [("n16", 16, "16-pairs-2", 8), ("n16", 16, "16-pairs-1", 16),
+                                             ("n26", 26, "26-pairs-1", 26)])
+def test_spectral_identity_on_reference_pairs(name, order, fn, L):
+    """The identity spectral pruning rests on, on the reference's own pairs:
+    p_A(k) + p_B(k) = 2n - paf for every k != 0, in particular at k = L/2
+    where both are squares of integers (the alternating sums)."""
+    bound = 2 * order
+    lines = read(os.path.join(GOLDEN, name, fn)).decode().splitlines()
+    assert lines
+    sign = np.array([(-1) ** j for j in range(L)])
+    for line in lines:
+        v = [int(x) for x in line.split()]
+        a, b = np.array(v[:L]), np.array(v[L:])
+        pa = np.abs(np.fft.fft(a)) ** 2
+        pb = np.abs(np.fft.fft(b)) ** 2
+        assert np.allclose(pa[1:] + pb[1:], bound, atol=1e-6)
+        sa, sb = int(a @ sign), int(b @ sign)
+        assert sa * sa + sb * sb == bound
