@@ -40,7 +40,9 @@ struct ExpandArgs {
     int b;          // bits per new digit
     int cnew;       // new alphabet offset: digit = (value + cnew) / 2
     uint64_t rank0;
-    int64_t n;
+    int64_t n;          // ranks rank0 .. rank0 + n - 1, n <= 2^24
+    int d0[kMaxPos];    // mixed-radix digits of rank0 (position L-1 least significant)
+    const uint64_t* inv;  // ceil(2^40 / cnt[i]): t / cnt[i] = t * inv[i] >> 40 for t < 2^24
     const int* cnt;     // choices per position
     const int* off;     // offset of position i's table in vals (entries)
     const int8_t* vals; // choice values, r per choice
@@ -54,13 +56,26 @@ __global__ void expand_kernel(ExpandArgs a) {
         s_off[i] = a.off[i];
     }
     __syncthreads();
+    __shared__ uint64_t s_inv[kMaxPos];
+    __shared__ int s_d0[kMaxPos];
+    for (int i = threadIdx.x; i < a.L; i += blockDim.x) {
+        s_inv[i] = a.inv[i];
+        s_d0[i] = a.d0[i];
+    }
+    __syncthreads();
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.n; t += (int64_t)gridDim.x * blockDim.x) {
-        uint64_t rank = a.rank0 + (uint64_t)t;
+        // digits of rank0 + t: the digits of t (exact reciprocal division,
+        // t < 2^24) added to those of rank0 with carry
+        uint32_t rest = (uint32_t)t;
+        int carry = 0;
         uint64_t lo = 0, hi = 0;
         for (int i = a.L - 1; i >= 0; --i) {
-            const uint64_t c = (uint64_t)s_cnt[i];
-            const int d = (int)(rank % c);
-            rank /= c;
+            const int c = s_cnt[i];
+            const uint32_t q = (uint32_t)(((uint64_t)rest * s_inv[i]) >> 40);
+            int d = (int)(rest - q * (uint32_t)c) + s_d0[i] + carry;
+            rest = q;
+            carry = d >= c;
+            if (carry) d -= c;
             const int8_t* v = a.vals + (int64_t)(s_off[i] + d) * a.r;
             for (int q = 0; q < a.r; ++q) {
                 const int p = i + a.L * q;
@@ -215,7 +230,7 @@ int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int n
     if (e.total == 0) return GP_OK;
     cudaStream_t s = c->s_comp;
     DevBuf &dcnt = c->ux[0], &doff = c->ux[1], &dvals = c->ux[2], &dwords = c->ux[3], &dmask = c->ux[4],
-           &dunsure = c->ux[5], &didx = c->ux[6], &dmisc = c->ux[7];
+           &dunsure = c->ux[5], &didx = c->ux[6], &dmisc = c->ux[7], &dinv = c->ux[29];
     const int64_t chunk = (int64_t)std::min<uint64_t>(e.total, uint64_t(1) << 24);
     if (!dcnt.ensure(L * 4) || !doff.ensure(L * 4) || !dvals.ensure(e.vals.size() + 16) || !dwords.ensure(chunk * 16) ||
         !dmask.ensure((chunk + 31) / 32 * 4) || !dunsure.ensure(chunk * 4) || !didx.ensure(chunk * 4) ||
@@ -225,6 +240,13 @@ int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int n
     side.cap = (int64_t)std::min<uint64_t>(e.total, uint64_t(1) << 26);
     if (!side.words.ensure((size_t)side.cap * 16) || !side.sig.ensure((size_t)side.cap * 2 * (Lnew - 1) + 16))
         return c->fail(GP_ERR_NOMEM, "uncompress: record arena");
+    // exact for offsets below 2^24 while every count is at most 2^16
+    for (int i = 0; i < L; ++i)
+        if (e.cnt[i] > (1 << 16)) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %d choices for one entry", e.cnt[i]);
+    std::vector<uint64_t> inv(L);
+    for (int i = 0; i < L; ++i) inv[i] = ((uint64_t(1) << 40) + (uint64_t)e.cnt[i] - 1) / (uint64_t)e.cnt[i];
+    if (!dinv.ensure(L * 8)) return c->fail(GP_ERR_NOMEM, "uncompress: device allocation");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dinv.p, inv.data(), L * 8, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(dcnt.p, e.cnt.data(), L * 4, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(doff.p, e.off.data(), L * 4, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(dvals.p, e.vals.data(), e.vals.size(), cudaMemcpyHostToDevice, s));
@@ -235,8 +257,26 @@ int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int n
     if (!tw) return c->fail(GP_ERR_NOMEM, "twiddles");
     for (uint64_t r0 = 0; r0 < e.total; r0 += (uint64_t)chunk) {
         const int64_t n = (int64_t)std::min<uint64_t>((uint64_t)chunk, e.total - r0);
-        ExpandArgs ea{L, r, Lnew, b, new_compress, r0, n, dcnt.as<int>(), doff.as<int>(), dvals.as<int8_t>(),
-                      dwords.as<uint4>()};
+        ExpandArgs ea{};
+        ea.L = L;
+        ea.r = r;
+        ea.Lnew = Lnew;
+        ea.b = b;
+        ea.cnew = new_compress;
+        ea.rank0 = r0;
+        ea.n = n;
+        {
+            uint64_t q = r0;  // digits of r0, position L-1 least significant
+            for (int i = L - 1; i >= 0; --i) {
+                ea.d0[i] = (int)(q % (uint64_t)e.cnt[i]);
+                q /= (uint64_t)e.cnt[i];
+            }
+        }
+        ea.inv = dinv.as<uint64_t>();
+        ea.cnt = dcnt.as<int>();
+        ea.off = doff.as<int>();
+        ea.vals = dvals.as<int8_t>();
+        ea.words = dwords.as<uint4>();
         int64_t blocks = (n + 255) / 256;
         if (blocks > (int64_t)c->num_sms * 16) blocks = (int64_t)c->num_sms * 16;
         expand_kernel<<<(unsigned)blocks, 256, 0, s>>>(ea);
