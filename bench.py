@@ -42,10 +42,8 @@ WORKLOAD = {"workload": "synthetic PSD-filter throughput: 2^28 x 45 int8, order 
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from golaypair_gb300.replicas import dist_env as env
+    return env()
 
 
 def oracle_lib():
@@ -202,6 +200,7 @@ def run_gpu(args):
     import torch
 
     import golaypair_gb300 as gp
+    from golaypair_gb300.replicas import max_over_ranks
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -247,10 +246,7 @@ def run_gpu(args):
         ms = e0.elapsed_time(e1)
         kms, klaunch = ctx.kernel_time()
         ctx.kernel_timing(False)
-        if ws > 1:
-            t = torch.tensor([ms], device=dev, dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
         return ms, kms, klaunch
 
     # exact-verdict spot check of this very batch against the FP64 kernel
@@ -310,10 +306,7 @@ def run_gpu(args):
         ctx.psd_filter_host_raw(hseqs.data_ptr(), ROWS, L, ORDER, PAF, gp.GP_PSD_TC_GUARDED, hmask.data_ptr())
     barrier()
     e_el = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e_el], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e_el = float(t.item())
+    e_el = max_over_ranks(e_el, dev)
     e2e_value = ROWS * ws * e_steps / e_el
     e2e_equal = bool(torch.equal(hmask, tc_mask.cpu()))
 

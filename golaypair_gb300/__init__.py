@@ -89,6 +89,7 @@ def lib():
         if fn is not None:
             fn.argtypes = args
     L.gp_debug_pair_generator_count.restype = ctypes.c_int64
+    L.gp_job_ranges.restype = ctypes.c_int64
     _lib = L
     return L
 
@@ -110,6 +111,7 @@ _STAGE_SIGS = {
     "gp_set_output_format": [_P, _i32],
     "gp_export_text": [_P, _cp, _cp],
     "gp_set_spectral_prune": [_P, _i32],
+    "gp_job_ranges": [_i32, _i32, _i32, _i32, _i32, _P, _i64],
     "gp_debug_pair_generator_count": [_i32, _i32],
 }
 
@@ -120,6 +122,18 @@ def header_symbols():
     with open(HEADER) as f:
         text = f.read()
     return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(gp_\w+)\s*\(", text, re.M)))
+
+
+def job_ranges(order, compress, paf, proc_id, proc_num):
+    """gp_job_ranges: the word-rank ranges [begin, end) of job proc_id of
+    proc_num (host only)."""
+    L = lib()
+    n = L.gp_job_ranges(order, compress, paf, proc_id, proc_num, None, 0)
+    if n < 0:
+        raise GPError(f"gp_job_ranges failed ({n})")
+    buf = (ctypes.c_uint64 * (4 * max(n, 1)))()
+    L.gp_job_ranges(order, compress, paf, proc_id, proc_num, buf, n)
+    return [((buf[4 * i] << 64) | buf[4 * i + 1], (buf[4 * i + 2] << 64) | buf[4 * i + 3]) for i in range(n)]
 
 
 def export_text(in_path, out_path):

@@ -810,6 +810,29 @@ int generate_resumable(gp_ctx* c, const GenPlan& p, const std::string& spec,
 
 extern "C" {
 
+int64_t gp_job_ranges(int order, int compress, int paf, int proc_id, int proc_num, uint64_t* out, int64_t cap) {
+    (void)paf;
+    if (compress < 1 || order < 1 || order % compress || proc_num < 1 || proc_id < 0 || proc_id >= proc_num)
+        return GP_ERR_ARG;
+    GenPlan p;
+    p.order = order;
+    p.compress = compress;
+    p.paf = paf;
+    p.L = order / compress;
+    p.alpha = gp::alphabet(compress);
+    p.k = (int)p.alpha.size();
+    p.b = gp::bits_for(p.k);
+    if (p.b * p.L > 126) return GP_ERR_UNSUPPORTED;
+    const auto ranges = shard_ranges(p, proc_id, proc_num);
+    for (size_t i = 0; i < ranges.size() && (int64_t)i < cap && out; ++i) {
+        out[4 * i + 0] = (uint64_t)(ranges[i].first >> 64);
+        out[4 * i + 1] = (uint64_t)ranges[i].first;
+        out[4 * i + 2] = (uint64_t)(ranges[i].second >> 64);
+        out[4 * i + 3] = (uint64_t)ranges[i].second;
+    }
+    return (int64_t)ranges.size();
+}
+
 int gp_generate(gp_ctx* c, int order, int compress, int paf, int proc_id, int proc_num, const char* path_a,
                 const char* path_b, gp_gen_stats* stats) {
     if (!c || !path_a || !path_b) return GP_ERR_ARG;

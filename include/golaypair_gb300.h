@@ -133,6 +133,14 @@ typedef struct {
 int gp_generate(gp_ctx* ctx, int order, int compress, int paf, int proc_id, int proc_num, const char* path_a,
                 const char* path_b, gp_gen_stats* stats);
 
+/* The word-rank ranges [begin, end) job proc_id of proc_num searches
+ * (src/utils/lyndon.cpp:93-106: prenecklace prefixes of the first length
+ * with at least proc_num * 10000 necklaces, dealt out round robin; one job
+ * takes the whole space).  Writes up to cap ranges to out as (begin_hi,
+ * begin_lo, end_hi, end_lo) and returns how many there are, or a negative
+ * error.  Host only: replicas on several GPUs take disjoint jobs. */
+int64_t gp_job_ranges(int order, int compress, int paf, int proc_id, int proc_num, uint64_t* out, int64_t cap);
+
 /* Same over the words whose lexicographic rank (base-|alphabet| number,
  * first entry most significant) lies in [begin, end), 128-bit bounds as
  * (hi, lo) pairs.  No counterpart in the reference, which only splits by
