@@ -32,6 +32,9 @@
 namespace {
 
 constexpr int kMaxPos = 128;
+// context scratch buffers of the two sides' expansions (c->ux[slot .. slot+8];
+// join.cu and the gather below use ux[8 .. 28])
+constexpr int kSlotA = 30, kSlotB = 39;
 
 struct ExpandArgs {
     int L;          // compressed length
@@ -200,6 +203,8 @@ void put_uint(std::string& s, unsigned v) {
 struct Side {
     DevBuf words, sig;
     int64_t n = 0, cap = 0;
+    unsigned long long* nrec = nullptr;  // pinned: record count, copied back by the expansion's stream
+    bool pending = false;                // enqueued, count not read yet
 };
 
 __global__ void gather_records_kernel(const uint4* words, const uint16_t* sig, int S, const uint32_t* rows, int64_t n,
@@ -211,11 +216,13 @@ __global__ void gather_records_kernel(const uint4* words, const uint16_t* sig, i
     }
 }
 
-// Expands one compressed sequence on the device and keeps, in `side`, every
-// expansion that passes the PSD filter, with its signature
-// (uncompression.cpp:195-207; invert selects bound - rint(psd)).
+// Enqueues on stream s the expansion of one compressed sequence, keeping in
+// `side` every expansion that passes the PSD filter, with its signature
+// (uncompression.cpp:195-207; invert selects bound - rint(psd)).  Device
+// scratch: the nine context buffers from c->ux[slot].  finish_side reads the
+// record count once the stream is done.
 int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int new_compress, int paf, bool invert,
-                Side& side, int64_t* n_exp) {
+                Side& side, int64_t* n_exp, cudaStream_t s, int slot) {
     const int L = (int)orig.size();
     Expansion e = plan_expansion(orig, compress, new_compress);
     if (e.overflow) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: more than 2^62 expansions");
@@ -227,10 +234,11 @@ int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int n
         return c->fail(GP_ERR_UNSUPPORTED, "uncompress: length %d over %d letters", Lnew, (int)nalpha.size());
     *n_exp += (int64_t)e.total;
     side.n = 0;
+    side.pending = false;
     if (e.total == 0) return GP_OK;
-    cudaStream_t s = c->s_comp;
-    DevBuf &dcnt = c->ux[0], &doff = c->ux[1], &dvals = c->ux[2], &dwords = c->ux[3], &dmask = c->ux[4],
-           &dunsure = c->ux[5], &didx = c->ux[6], &dmisc = c->ux[7], &dinv = c->ux[29];
+    DevBuf* ux = c->ux + slot;
+    DevBuf &dcnt = ux[0], &doff = ux[1], &dvals = ux[2], &dwords = ux[3], &dmask = ux[4], &dunsure = ux[5],
+           &didx = ux[6], &dmisc = ux[7], &dinv = ux[8];
     const int64_t chunk = (int64_t)std::min<uint64_t>(e.total, uint64_t(1) << 24);
     if (!dcnt.ensure(L * 4) || !doff.ensure(L * 4) || !dvals.ensure(e.vals.size() + 16) || !dwords.ensure(chunk * 16) ||
         !dmask.ensure((chunk + 31) / 32 * 4) || !dunsure.ensure(chunk * 4) || !didx.ensure(chunk * 4) ||
@@ -311,12 +319,19 @@ int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int n
         fa.status = c->status.as<int>();
         GP_CUDA_TRY(c, gp::launch_finalize(fa, n, c->num_sms, s));
     }
-    unsigned long long nrec = 0;
-    GP_CUDA_TRY(c, cudaMemcpyAsync(&nrec, misc + 2, 8, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(side.nrec, misc + 2, 8, cudaMemcpyDeviceToHost, s));
+    side.pending = true;
+    return GP_OK;
+}
+
+// Waits for a side's expansion on stream s and takes its record count.
+int finish_side(gp_ctx* c, Side& side, cudaStream_t s) {
+    if (!side.pending) return GP_OK;
+    side.pending = false;
     GP_CUDA_TRY(c, cudaStreamSynchronize(s));
     int rc = c->check_status("uncompress");
     if (rc) return rc;
-    side.n = (int64_t)std::min<unsigned long long>(nrec, (unsigned long long)side.cap);
+    side.n = (int64_t)std::min<unsigned long long>(*side.nrec, (unsigned long long)side.cap);
     return GP_OK;
 }
 
@@ -432,6 +447,8 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
     (void)work_dir;
     (void)prefix;
     cudaSetDevice(c->device);
+    if (!c->ensure_job_streams() || !c->h_ux.ensure(64))
+        return c->fail(GP_ERR_CUDA, "uncompress: streams / pinned counts");
     // the reference constructs its PairReader / PairWriter before the
     // pipeline runs (src/main.cpp:122-123): the output is truncated even
     // when nothing is uncompressed
@@ -456,6 +473,8 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
     long line_no = 0;
     int rc = GP_OK;
     Side side_a, side_b;
+    side_a.nrec = c->h_ux.as<unsigned long long>();
+    side_b.nrec = c->h_ux.as<unsigned long long>() + 1;
     while (p < end && rc == GP_OK) {
         const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
         if (!nl) nl = end;
@@ -490,9 +509,14 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
         std::vector<int> a(vals.begin(), vals.begin() + L), b(vals.begin() + L, vals.end());
         std::string pairs;
         int64_t na = 0, nb = 0;
-        rc = expand_side(c, a, order, compress, new_compress, paf, true, side_a, &na);
+        // the two sides expand on two streams, each with its own scratch
+        rc = expand_side(c, a, order, compress, new_compress, paf, true, side_a, &na, c->s_comp, kSlotA);
         if (rc) break;
-        rc = expand_side(c, b, order, compress, new_compress, paf, false, side_b, &nb);
+        rc = expand_side(c, b, order, compress, new_compress, paf, false, side_b, &nb, c->s_jobs[0], kSlotB);
+        if (rc) break;
+        rc = finish_side(c, side_a, c->s_comp);
+        if (rc) break;
+        rc = finish_side(c, side_b, c->s_jobs[0]);
         if (rc) break;
         rc = join_sides(c, side_a, side_b, order / new_compress, new_compress, paf, pairs);
         if (rc) break;

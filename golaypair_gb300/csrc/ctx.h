@@ -97,6 +97,7 @@ struct gp_ctx {
     DevBuf status;          // int
     DevBuf counts;          // unsigned long long [8]
     HostPinned h_counts;    // mirror of counts, per chunk
+    HostPinned h_ux;        // uncompression: record counts of the two sides
     // PSD filter staging
     DevBuf seq_buf[2];
     DevBuf mask_buf[2];
@@ -124,7 +125,7 @@ struct gp_ctx {
     DevBuf scratch[16];
     // grow-only scratch of the uncompression stage (kept across pairs: a
     // cudaFree per pair would synchronise the device every pair)
-    DevBuf ux[32];
+    DevBuf ux[48];
     HostPinned hscratch[4];
     // batched generation: one stream per job branch, fork/join events
     static constexpr int kJobStreams = 8;
