@@ -254,12 +254,26 @@ std::vector<int16_t> as_sources(const int16_t* item, int L) {
     return out;
 }
 
+// Size of the generator group: 4 phi(L) L^2, times 8 sign patterns with the
+// alternating negation (exact for L >= 3, an upper bound at L = 2).
+uint64_t pair_group_size(int L, int compress) {
+    uint64_t phi = 0;
+    for (int u = 1; u <= L; ++u)
+        if (std::gcd(u, L) == 1) ++phi;
+    const bool use_alt = !(compress > 1 || L % 2 == 1);
+    return 4 * phi * (uint64_t)L * (uint64_t)L * (use_alt ? 8 : 1);
+}
+
+// The group's items take 2L int16 each on the host and again on the device.
+constexpr uint64_t kMaxGroupBytes = uint64_t(1) << 32;
+
 }  // namespace
 
 extern "C" {
 
 int64_t gp_debug_pair_generator_count(int L, int compress) {
     if (L < 1 || 2 * L > kMaxW || compress < 1) return -1;
+    if (pair_group_size(L, compress) * (uint64_t)(4 * L) > kMaxGroupBytes) return -1;
     return (int64_t)(pair_generators(L, compress).size() / (size_t)(2 * L));
 }
 
@@ -270,6 +284,9 @@ int gp_equiv_filter(gp_ctx* c, int order, int compress, const char* in_path, con
     const int L = order / compress;
     const int W = 2 * L;
     if (W > kMaxW) return c->fail(GP_ERR_UNSUPPORTED, "equivalence filter: length %d", L);
+    if (pair_group_size(L, compress) * (uint64_t)(2 * W) > kMaxGroupBytes)
+        return c->fail(GP_ERR_UNSUPPORTED, "equivalence filter: %llu generators at length %d exceed %llu bytes",
+                       (unsigned long long)pair_group_size(L, compress), L, (unsigned long long)kMaxGroupBytes);
     FILE* out = fopen(out_path, "w");  // filter.cpp:24 opens the output first
     FILE* in = fopen(in_path, "rb");
     if (!in) {

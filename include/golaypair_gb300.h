@@ -304,7 +304,10 @@ int gp_uncompress_lines(gp_ctx* ctx, int order, int compress, int new_compress, 
  * Replaces int cache_filter(int ORDER, int COMPRESS, const std::string& in,
  * const std::string& out) (src/core/filter/filter.h, filter.cpp:18-163):
  * keeps the first pair of every equivalence class (in the reference's set
- * order and erase rules) and writes them in sorted order.
+ * order and erase rules) and writes them in sorted order.  The generator
+ * group has 4 phi(L) L^2 elements (8 times more at compression 1 with even
+ * L); GP_ERR_UNSUPPORTED when its table would exceed 4 GB (e.g. L = 128 at
+ * compression 1), where the reference would run out of memory.
  */
 int gp_equiv_filter(gp_ctx* ctx, int order, int compress, const char* in_path, const char* out_path);
 

@@ -119,3 +119,6 @@ def test_pair_generator_set_matches_oracle_closure(oracle_lib, compress):
     lib = gp.lib()
     for L in range(2, 23):
         assert lib.gp_debug_pair_generator_count(L, compress) == oracle_lib.gpo_pair_generator_count(L, compress), L
+    # 4 phi(L) L^2 (x 8 at compression 1, even L) for L >= 3; too large a table is refused
+    assert lib.gp_debug_pair_generator_count(57, compress) == 4 * 36 * 57 * 57
+    assert lib.gp_debug_pair_generator_count(128, 1) == -1
