@@ -42,7 +42,8 @@ struct PsdTcArgs {
 
 // Diagnostics counters written when PsdTcArgs::trace is set (summed over
 // CTAs, in SM clock cycles, one sample per warp and tile).  conv_work
-// includes conv_st (the TMEM stores and their wait); epi_work includes
+// includes conv_st (from the converted row to the end of the TMEM stores'
+// wait); epi_work includes
 // epi_ld (up to the hi accumulator columns landing in registers) and
 // epi_tail (after the accumulator is released).
 enum TcTrace {

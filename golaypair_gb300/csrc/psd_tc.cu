@@ -435,7 +435,6 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
             const bool full_tile = t < nfull;
             uint32_t h[K / 2];  // the row as fp16 pairs
             const uint32_t aaddr = lane_base + (uint32_t)(as * (K / 2));
-            const long long c25t = tclock<TR>();
             if constexpr (B == 0) {
                 if (full_tile) {
                     const uint8_t* raw = sRaw + rs * lay.raw_stride;
@@ -479,6 +478,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 }
                 packed_row<B, 0, C::KCH>(sw, sLut, h);
             }
+            const long long c25t = tclock<TR>();
             if (B != 0 || full_tile) {
 #pragma unroll
                 for (int g = 0; g < K / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
