@@ -112,6 +112,7 @@ _STAGE_SIGS = {
     "gp_export_text": [_P, _cp, _cp],
     "gp_set_spectral_prune": [_P, _i32],
     "gp_job_ranges": [_i32, _i32, _i32, _i32, _i32, _P, _i64],
+    "gp_debug_wait_timeout": [_P, _i64],
     "gp_debug_pair_generator_count": [_i32, _i32],
 }
 

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "ctx.h"
+#include "gp_device.cuh"
 
 namespace {
 
@@ -132,6 +133,31 @@ bool gp_ctx::ensure_job_streams() {
     return cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) == cudaSuccess;
 }
 
+namespace {
+
+// One thread waits on an mbarrier that nothing arrives on.  The wait is the
+// bounded loop of every pipeline kernel, with the caller's limit: it gives
+// up, records its site in the status word and returns.
+__global__ void wait_timeout_kernel(uint64_t limit_ns, int* status) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        gp::mbar_init(&bar, 1);
+        gp::mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint64_t t0 = gp::globaltimer_ns();
+        while (!gp::mbar_try_wait(&bar, 0)) {
+            if (gp::globaltimer_ns() - t0 > limit_ns) {
+                atomicCAS(status, 0, GP_KSTATUS_TIMEOUT_BASE + 99);
+                break;
+            }
+        }
+    }
+}
+
+}  // namespace
+
 int gp_ctx::check_status(const char* what) {
     int st = 0;
     cudaError_t e = cudaMemcpy(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost);
@@ -145,6 +171,15 @@ int gp_ctx::check_status(const char* what) {
 }
 
 extern "C" {
+
+int gp_debug_wait_timeout(gp_ctx* c, int64_t limit_ns) {
+    if (!c || limit_ns < 0 || limit_ns > (int64_t)gp::kWaitTimeoutNs) return GP_ERR_ARG;
+    cudaSetDevice(c->device);
+    wait_timeout_kernel<<<1, 32, 0, c->s_comp>>>((uint64_t)limit_ns, c->status.as<int>());
+    GP_CUDA_TRY(c, cudaGetLastError());
+    GP_CUDA_TRY(c, cudaStreamSynchronize(c->s_comp));
+    return c->check_status("gp_debug_wait_timeout");
+}
 
 int gp_ctx_create(gp_ctx** out, int device) {
     if (!out) return GP_ERR_ARG;

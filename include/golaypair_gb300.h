@@ -80,6 +80,11 @@ int gp_kernel_time(gp_ctx* ctx, double* total_ms, int64_t* launches);
  * previous call.  Copies up to nout counters, resets them, and turns the
  * counting on (enable != 0) or off for later launches. */
 int gp_debug_tc_trace(gp_ctx* ctx, int enable, uint64_t* out, int nout);
+/* Diagnostics: runs the bounded device wait of the pipeline kernels on a
+ * barrier that nothing completes, with a limit of limit_ns (at most 2 s).
+ * Returns GP_ERR_TIMEOUT (the kernel gave up and reported it); the context
+ * stays usable.  Tests failure detection without faulting the GPU. */
+int gp_debug_wait_timeout(gp_ctx* ctx, int64_t limit_ns);
 
 /*
  * The batched tensor-core PSD filter for callers that cannot allocate device

@@ -122,3 +122,41 @@ def test_pair_generator_set_matches_oracle_closure(oracle_lib, compress):
     # 4 phi(L) L^2 (x 8 at compression 1, even L) for L >= 3; too large a table is refused
     assert lib.gp_debug_pair_generator_count(57, compress) == 4 * 36 * 57 * 57
     assert lib.gp_debug_pair_generator_count(128, 1) == -1
+
+
+# Known answers recorded in the reference's notes (NOTES.md:455,459 and :436)
+NOTES_ORDER26_A = [-1, -1, -1, -1, 1, 1, -1, -1, 1, 1, 1, -1, 1, -1, 1, -1, 1, 1, -1, 1, 1, -1, 1, 1, 1, 1]
+NOTES_ORDER26_A_C2 = [-2, 0, -2, 0, 2, 0, 0, 0, 0, 2, 2, 0, 2]
+NOTES_ORDER72_C6 = ([-6, 0, 0, 0, 0, 0, 6, 0, 0, 0, 0, 0], [0, 0, 0, 0, 0, 6, 0, 0, 0, 0, 0, 6])
+
+
+def test_notes_order26_candidate_has_a_representative():
+    """The order-26 A candidate of the notes compresses (entry j + entry j+13)
+    to the recorded 2-compressed form, and the reference's order-26 A file
+    holds a member of that form's class (shifts, decimations by units,
+    reversal: the A-side equivalences)."""
+    a, L = NOTES_ORDER26_A, 13
+    assert [a[j] + a[j + L] for j in range(L)] == NOTES_ORDER26_A_C2
+    x = NOTES_ORDER26_A_C2
+    orbit = set()
+    for u in (u for u in range(1, L) if math.gcd(u, L) == 1):
+        for s in range(L):
+            y = tuple(x[(s + u * i) % L] for i in range(L))
+            orbit.add(y)
+            orbit.add(y[::-1])
+    lines = read(os.path.join(GOLDEN, "n26", "26-filtered-a_0")).decode().splitlines()
+    seqs = {tuple(int(v) for v in ln.split()[1:]) for ln in lines}
+    assert orbit & seqs
+
+
+def test_notes_order72_compression6_candidate_is_a_pair(oracle_lib):
+    """The order-72, compression-6 candidate the notes record (found by a
+    generation run and matching a published compression) is a complementary
+    compressed pair for the reference's check_if_pair as it stands (the notes
+    describe an earlier version rejecting it): every PAF sum is 0 and every
+    PSD sum is 2n = 144."""
+    a, b = (np.array(v, dtype=np.int32) for v in NOTES_ORDER72_C6)
+    assert oracle_lib.gpo_check_if_pair(a.ctypes.data, b.ctypes.data, 12, 0, 6) == 1
+    assert [int((a * np.roll(a, -s)).sum() + (b * np.roll(b, -s)).sum()) for s in range(1, 7)] == [0] * 6
+    psd = np.abs(np.fft.fft(a)) ** 2 + np.abs(np.fft.fft(b)) ** 2
+    assert np.allclose(psd[1:], 144)

@@ -246,3 +246,25 @@ def test_spectral_identity_at_third_bin_order57(tmp_path):
         pb = np.abs(np.fft.fft(np.array(v[57:]))) ** 2
         assert abs(pa[19] + pb[19] - (2 * 57 + 2)) < 1e-6
         assert abs(pa[19] - round(pa[19])) < 1e-6
+
+
+def test_every_emitted_pair_is_complementary_order57(tmp_path):
+    """Property over all 196,216 pairs match writes at order 57 (paf -2,
+    compression 3): PAF_a(s) + PAF_b(s) = paf * c for s = 1 .. L/2, the
+    reference's check_if_pair (src/utils/golay.cpp:27-44)."""
+    _, wd = golay(["57", "-c", "3", "--paf", "-2", "gen", "sort", "match"], tmp_path)
+    arr = np.array(read(os.path.join(wd, "57-pairs-3")).split(), dtype=np.int64).reshape(-1, 38)
+    assert len(arr) == 196216
+    a, b = arr[:, :19], arr[:, 19:]
+    for s in range(1, 10):
+        paf = (a * np.roll(a, -s, axis=1)).sum(axis=1) + (b * np.roll(b, -s, axis=1)).sum(axis=1)
+        assert (paf == -2 * 3).all(), s
+
+
+def test_sort_of_a_missing_file_fails(tmp_path):
+    """Injected failure: the sort stage with an input file that does not
+    exist reports the error (the reference's GNU_sort returns 1,
+    src/core/sort/sort.cpp:18-21)."""
+    r, _ = golay(["26", "-c", "2", "sort"], tmp_path, check=False)
+    assert r.returncode != 0
+    assert "sort" in (r.stderr + r.stdout).lower()

@@ -114,3 +114,20 @@ def test_fp64_values_match_oracle(ctx, oracle_lib):
             s = (ctypes.c_int * L)(*seqs[i].tolist())
             oracle_lib.gpo_psd(s, L, psd)
             assert np.allclose(got[i], np.array(psd[:]), rtol=0, atol=1e-9)
+
+
+def test_bounded_wait_gives_up_and_context_stays_usable(ctx, oracle_lib):
+    """Failure detection without a GPU fault: a device wait on a barrier that
+    nothing completes gives up after its limit and reports GP_ERR_TIMEOUT;
+    the same context then filters correctly."""
+    import time
+    t0 = time.time()
+    rc = ctx._lib.gp_debug_wait_timeout(ctx.handle, 50_000_000)  # 50 ms
+    assert rc == -3  # GP_ERR_TIMEOUT
+    assert time.time() - t0 < 5
+    assert b"timed out" in ctx._lib.gp_last_error(ctx.handle)
+    seqs = np.array(list(itertools.product([-2, 0, 2], repeat=8)), dtype=np.int8)
+    want = np.zeros(len(seqs), dtype=np.uint8)
+    oracle_lib.gpo_psd_filter_batch(seqs.ctypes.data, len(seqs), 8, 16, 0, want.ctypes.data, 1)
+    got, _ = ctx.psd_filter(seqs, 16, 0, gp.GP_PSD_TC_GUARDED)
+    assert np.array_equal(got.astype(bool), want.astype(bool))

@@ -79,3 +79,32 @@ def test_two_replicas_cover_the_single_job(tmp_path, oracle_lib):
     whole = sorted([("a", ln) for ln in open(a).read().splitlines()] +
                    [("b", ln) for ln in open(b).read().splitlines()])
     assert sorted(x for _, lines in gathered for x in lines) == whole
+
+
+def _lossy_worker(rank, world, port, outdir):
+    import datetime
+
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=20))
+    if rank == 1:
+        return  # this replica is lost before the step's collective
+    try:
+        replicas.max_over_ranks(1.0)
+        outcome = "no error"
+    except Exception as e:  # the loss surfaces on the host as an error
+        outcome = "detected: " + type(e).__name__
+    with open(os.path.join(outdir, "lossy"), "w") as f:
+        f.write(outcome)
+
+
+def test_lost_replica_is_detected_on_the_host(tmp_path):
+    """A replica that leaves between steps: the others learn of it on the
+    host when they next meet (an error from the collective, bounded by the
+    process group's timeout), not by a hang."""
+    import time
+    t0 = time.time()
+    torch.multiprocessing.spawn(_lossy_worker, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)
+    assert (tmp_path / "lossy").read_text().startswith("detected")
+    assert time.time() - t0 < 60
