@@ -278,6 +278,7 @@ int64_t gp_debug_pair_generator_count(int L, int compress) {
 }
 
 int gp_equiv_filter(gp_ctx* c, int order, int compress, const char* in_path, const char* out_path) {
+    StageRange nvtx_range("gp_equiv_filter");
     if (!c || !in_path || !out_path) return GP_ERR_ARG;
     if (compress < 1 || order % compress) return c->fail(GP_ERR_ARG, "order %d not divisible by %d", order, compress);
     cudaSetDevice(c->device);

@@ -232,6 +232,7 @@ double since(std::chrono::steady_clock::time_point t) {
 }
 
 int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* iterations, StopCtl* stop = nullptr) {
+    StageRange nvtx_range("generate");
     static const bool timing = getenv("GP_GEN_TIMING") != nullptr;
     const auto tb = std::chrono::steady_clock::now();
     double t_win = 0, t_setup = 0, t_capture = 0, t_iter = 0, t_drain = 0;

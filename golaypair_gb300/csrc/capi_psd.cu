@@ -338,6 +338,7 @@ static int check_args(gp_ctx* c, int64_t n, int L, int mode) {
 
 int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, int paf, int mode,
                   uint32_t* pass_mask, gp_psd_stats* stats) {
+    StageRange nvtx_range("gp_psd_filter");
     int rc = check_args(c, n, L, mode);
     if (rc) return rc;
     if (n > 0 && (!seqs || !pass_mask)) return c->fail(GP_ERR_ARG, "null buffer");
@@ -413,6 +414,7 @@ int gp_psd_filter(gp_ctx* c, const int8_t* seqs, int64_t n, int L, int order, in
 
 int gp_psd_filter_device(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int order, int paf, int mode,
                          uint32_t* d_mask, void* stream, gp_psd_stats* stats) {
+    StageRange nvtx_range("gp_psd_filter_device");
     int rc = check_args(c, n, L, mode);
     if (rc) return rc;
     if (n >= (int64_t(1) << 31)) return c->fail(GP_ERR_ARG, "device batch too large (n < 2^31)");

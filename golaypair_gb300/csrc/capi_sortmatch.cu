@@ -444,6 +444,7 @@ int gp_tuned_settings(const gp_ctx* c, char* buf, int cap) {
 }
 
 int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
+    StageRange nvtx_range("gp_sort");
     if (!c || (!in_paths && n_in > 0) || !out_path) return GP_ERR_ARG;
     cudaSetDevice(c->device);
     std::string all, one;
@@ -469,6 +470,7 @@ int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
 
 int gp_match(gp_ctx* c, int order, int compress, int paf, const char* path_a, const char* path_b, const char* out_path,
              int append, int64_t* n_pairs) {
+    StageRange nvtx_range("gp_match");
     if (!c || !path_a || !path_b || !out_path) return GP_ERR_ARG;
     if (compress < 1 || order % compress) return c->fail(GP_ERR_ARG, "order %d not divisible by %d", order, compress);
     cudaSetDevice(c->device);

@@ -441,6 +441,7 @@ int gp_uncompress(gp_ctx* c, int order, int compress, int new_compress, int paf,
 int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
                         const char* out_pairs, const char* work_dir, const char* prefix, int64_t first, int64_t end_line,
                         int64_t step) {
+    StageRange nvtx_range("gp_uncompress");
     if (!c || !in_pairs || !out_pairs) return GP_ERR_ARG;
     if (first < 0 || step < 1) return c->fail(GP_ERR_ARG, "uncompress: bad line range (first %lld, step %lld)",
                                               (long long)first, (long long)step);

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/golaypair_gb300.h"
 #include "gp_internal.h"
@@ -73,6 +74,15 @@ struct HostPinned {
     T* as() const {
         return static_cast<T*>(p);
     }
+};
+
+// An NVTX range over one stage call, named for the entry point: the stages
+// show on a profiler's timeline (no cost without a tool attached).
+struct StageRange {
+    explicit StageRange(const char* name) { nvtxRangePushA(name); }
+    ~StageRange() { nvtxRangePop(); }
+    StageRange(const StageRange&) = delete;
+    StageRange& operator=(const StageRange&) = delete;
 };
 
 // entries of the spectral pruning table (values 0 .. kPruneTab - 1; orders
