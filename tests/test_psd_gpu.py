@@ -36,6 +36,7 @@ def oracle_verdicts(oracle_lib, seqs, order, paf):
 CASES = [  # (order, compress, paf)
     (16, 2, 0), (26, 2, 0), (34, 2, 0), (50, 2, 0), (58, 2, 0), (68, 2, 0), (90, 2, 0), (90, 5, 0),
     (57, 3, -2), (57, 1, -2), (16, 1, 0), (26, 1, 0), (38, 1, 0), (98, 1, 0), (126, 1, 0), (252, 2, 0),
+    (70, 1, 0), (86, 1, 0), (170, 2, 0),  # padded lengths K = 80 and 96
 ]
 
 
