@@ -587,6 +587,9 @@ int tune_batch(gp_ctx* c, const std::vector<JobRun>& jobs, BatchCfg& best, doubl
     BatchCfg v1 = base;
     v1.enum_variant = 1;
     cands.push_back(v1);
+    BatchCfg v2 = base;
+    v2.enum_variant = 2;
+    cands.push_back(v2);
     BatchCfg w4 = base;
     w4.windows_per_thread = 4;
     cands.push_back(w4);
@@ -927,7 +930,7 @@ extern "C" int gp_generate_batch(gp_ctx* c, const gp_gen_job* jobs, int njobs, i
         int rc = tune_batch(c, run, bc, &tune_s);
         if (rc) return rc;
     } else if (cfg) {
-        if (cfg->enum_variant == 1) bc.enum_variant = 1;
+        if (cfg->enum_variant == 1 || cfg->enum_variant == 2) bc.enum_variant = cfg->enum_variant;
         if (cfg->windows_per_thread > 0) bc.windows_per_thread = cfg->windows_per_thread;
         if (cfg->cand_cap > 0) bc.cand_cap = cfg->cand_cap;
         if (cfg->tc_ctas_per_sm > 0) bc.tc_ctas_per_sm = cfg->tc_ctas_per_sm;

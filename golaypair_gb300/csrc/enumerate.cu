@@ -178,6 +178,7 @@ __device__ __forceinline__ bool job_full(const EnumJob& j) {
 // Each thread takes windows from a global counter.  A window whose job
 // has reached its soft capacity is left (position saved) and the thread goes
 // on with its next window, so one full job does not idle the others.
+// MINB = 3: 72 registers, no spills (3 CTAs of 256 per SM);
 // MINB = 4: at most 64 registers (4 CTAs of 256 per SM); MINB = 8: capped
 // at 32 registers for full occupancy (some spills).  The tuner picks.
 //
@@ -344,19 +345,22 @@ cudaError_t launch_enumerate(const EnumArgs& a, int num_sms, cudaStream_t st, in
     if (a.nwin <= 0) return cudaSuccess;
     if (a.njobs < 1 || a.njobs > kMaxEnumJobs) return cudaErrorInvalidValue;
     // one wave of resident blocks: windows are handed out dynamically
-    static int resident[2] = {0, 0};
-    int& per_sm = resident[variant == 1 ? 1 : 0];
+    static int resident[3] = {0, 0, 0};
+    const int vi = variant == 1 ? 1 : variant == 2 ? 2 : 0;
+    int& per_sm = resident[vi];
     if (per_sm == 0) {
-        cudaError_t e = variant == 1
-                            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<8>, 256, 0)
-                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<4>, 256, 0);
+        cudaError_t e = vi == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<8>, 256, 0)
+                        : vi == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<3>, 256, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<4>, 256, 0);
         if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     }
     int64_t blocks = (a.nwin + 255) / 256;
     const int64_t maxb = (int64_t)num_sms * per_sm;
     if (blocks > maxb) blocks = maxb;
-    if (variant == 1)
+    if (vi == 1)
         enumerate_kernel<8><<<(unsigned)blocks, 256, 0, st>>>(a);
+    else if (vi == 2)
+        enumerate_kernel<3><<<(unsigned)blocks, 256, 0, st>>>(a);
     else
         enumerate_kernel<4><<<(unsigned)blocks, 256, 0, st>>>(a);
     return cudaGetLastError();

@@ -228,7 +228,8 @@ typedef struct gp_gen_job {
 
 /* Settings of the batched generation engine; zero fields take defaults. */
 typedef struct gp_batch_config {
-    int enum_variant;        /* enumerator kernel: 0 = registers as needed, 1 = full occupancy */
+    int enum_variant;        /* enumerator kernel: 0 = 64 registers (4 CTAs per SM), 1 = full
+                                occupancy (32 registers), 2 = 72 registers, no spills (3 CTAs) */
     int windows_per_thread;  /* rank windows per enumerator thread (0: 1) */
     int64_t cand_cap;        /* candidates per job per pipeline iteration (0: 2^22) */
     int tc_ctas_per_sm;      /* tensor-core filter CTAs per SM (0: as many as fit) */

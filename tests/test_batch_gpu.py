@@ -83,6 +83,7 @@ def test_batch_equals_single_windows(default_run, tmp_path):
     {"cand_cap": 1 << 16},                   # many iterations: windows left and resumed
     {"cand_cap": 5000, "no_graph": 1},
     {"enum_variant": 1},
+    {"enum_variant": 2},
     {"windows_per_thread": 4},
     {"tc_ctas_per_sm": 1},
 ])
@@ -102,7 +103,7 @@ def test_batch_autotune_is_cached_and_exact(default_run, tmp_path):
     with gp.Context(0) as ctx:
         got, _, cfg = run_batch(ctx, tmp_path, "t", autotune=True)
         assert got == files
-        assert cfg.enum_variant in (0, 1) and cfg.windows_per_thread in (1, 4)
+        assert cfg.enum_variant in (0, 1, 2) and cfg.windows_per_thread in (1, 4)
         assert cfg.tc_ctas_per_sm in (0, 1) and cfg.no_graph == 0
         assert cfg.tune_seconds > 0
         got2, _, cfg2 = run_batch(ctx, tmp_path, "u", autotune=True)
