@@ -137,3 +137,28 @@ def test_spectral_identity_on_reference_pairs(name, order, fn, L):
         assert np.allclose(pa[1:] + pb[1:], bound, atol=1e-6)
         sa, sb = int(a @ sign), int(b @ sign)
         assert sa * sa + sb * sb == bound
+
+
+def test_export_two_byte_signatures(tmp_path):
+    """Order 140 at compression 4 (length 35, five letters in 3-bit digits):
+    the bound 280 needs 2-byte signature fields.  Records with arbitrary
+    values; the expected lines are written here from the line format."""
+    order, compress, paf, role = 140, 4, 0, 1
+    L, alpha, b = 35, [-4, -2, 0, 2, 4], 3
+    rng = np.random.default_rng(11)
+    recs = [(rng.integers(0, 5, size=L), rng.integers(0, 281, size=L - 1)) for _ in range(500)]
+    word_bytes = (b * L + 7) // 8
+    hdr = MAGIC + struct.pack("<I9iQ", 1, order, compress, paf, L, len(alpha), b, role, 2, word_bytes, len(recs))
+    hdr += struct.pack("<16b", *(alpha + [0] * 11)) + bytes(8)
+    body, want = bytearray(), []
+    for digits, sig in recs:
+        word = 0
+        for d in digits:
+            word = (word << b) | int(d)
+        body += word.to_bytes(word_bytes, "little")
+        for v in sig:
+            body += int(v).to_bytes(2, "little")
+        want.append("PSD" + "".join(str(int(v)) for v in sig) + " " + "".join(f"{alpha[d]} " for d in digits) + "\n")
+    (tmp_path / "s.bin").write_bytes(hdr + bytes(body))
+    gp.export_text(tmp_path / "s.bin", tmp_path / "s.txt")
+    assert (tmp_path / "s.txt").read_text() == "".join(want)
