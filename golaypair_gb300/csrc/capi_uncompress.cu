@@ -32,9 +32,10 @@
 namespace {
 
 constexpr int kMaxPos = 128;
-// context scratch buffers of the two sides' expansions (c->ux[slot .. slot+8];
-// join.cu and the gather below use ux[8 .. 28])
-constexpr int kSlotA = 30, kSlotB = 39;
+// context scratch buffers of the two sides' expansions (c->ux[slot .. slot+8]),
+// two sets so that one pair expands while the previous one is joined (join.cu
+// and the gather below use ux[8 .. 28])
+constexpr int kSlotA[2] = {30, 48}, kSlotB[2] = {39, 57};
 
 struct ExpandArgs {
     int L;          // compressed length
@@ -473,9 +474,35 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
     const char* end = p + text.size();
     long line_no = 0;
     int rc = GP_OK;
-    Side side_a, side_b;
-    side_a.nrec = c->h_ux.as<unsigned long long>();
-    side_b.nrec = c->h_ux.as<unsigned long long>() + 1;
+    // Pairs alternate between two sets of sides, scratch and streams: pair
+    // i+1 expands on the device while pair i is joined and formatted.  The
+    // join leaves no device work behind, so a set is free again once its
+    // pair is written; output stays in input-pair order.
+    struct PairSet {
+        Side a, b;
+        cudaStream_t sa, sb;
+        bool busy = false;
+    };
+    PairSet set[2];
+    for (int k = 0; k < 2; ++k) {
+        set[k].sa = c->s_jobs[2 * k];
+        set[k].sb = c->s_jobs[2 * k + 1];
+        set[k].a.nrec = c->h_ux.as<unsigned long long>() + 2 * k;
+        set[k].b.nrec = c->h_ux.as<unsigned long long>() + 2 * k + 1;
+    }
+    auto retire = [&](PairSet& ps) -> int {
+        if (!ps.busy) return GP_OK;
+        ps.busy = false;
+        int r = finish_side(c, ps.a, ps.sa);
+        if (r) return r;
+        r = finish_side(c, ps.b, ps.sb);
+        if (r) return r;
+        std::string pairs;
+        r = join_sides(c, ps.a, ps.b, order / new_compress, new_compress, paf, pairs);
+        if (!r && !pairs.empty()) fwrite(pairs.data(), 1, pairs.size(), out);
+        return r;
+    };
+    int cur = 0;
     while (p < end && rc == GP_OK) {
         const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
         if (!nl) nl = end;
@@ -500,28 +527,32 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
             q = e2;
         }
         p = nl + 1;
-        // io.cpp:52-55: a line of the wrong length is an error
+        // io.cpp:52-55: a line of the wrong length is an error (the pairs
+        // before it are still written)
         if ((int)vals.size() != 2 * L) {
-            rc = c->fail(GP_ERR_FORMAT, "PairReader: input line %ld: length is %zu. Expected %d", line_no, vals.size(),
-                         2 * L);
+            rc = retire(set[cur ^ 1]);
+            if (!rc)
+                rc = c->fail(GP_ERR_FORMAT, "PairReader: input line %ld: length is %zu. Expected %d", line_no,
+                             vals.size(), 2 * L);
             break;
         }
         ++line_no;
         std::vector<int> a(vals.begin(), vals.begin() + L), b(vals.begin() + L, vals.end());
-        std::string pairs;
         int64_t na = 0, nb = 0;
+        PairSet& ps = set[cur];
+        ps.busy = true;
         // the two sides expand on two streams, each with its own scratch
-        rc = expand_side(c, a, order, compress, new_compress, paf, true, side_a, &na, c->s_comp, kSlotA);
+        rc = expand_side(c, a, order, compress, new_compress, paf, true, ps.a, &na, ps.sa, kSlotA[cur]);
         if (rc) break;
-        rc = expand_side(c, b, order, compress, new_compress, paf, false, side_b, &nb, c->s_jobs[0], kSlotB);
+        rc = expand_side(c, b, order, compress, new_compress, paf, false, ps.b, &nb, ps.sb, kSlotB[cur]);
         if (rc) break;
-        rc = finish_side(c, side_a, c->s_comp);
-        if (rc) break;
-        rc = finish_side(c, side_b, c->s_jobs[0]);
-        if (rc) break;
-        rc = join_sides(c, side_a, side_b, order / new_compress, new_compress, paf, pairs);
-        if (rc) break;
-        fwrite(pairs.data(), 1, pairs.size(), out);
+        rc = retire(set[cur ^ 1]);  // the previous pair, while this one expands
+        cur ^= 1;
+    }
+    if (rc == GP_OK) rc = retire(set[cur ^ 1]);
+    for (auto& ps : set) {  // nothing of this call stays in flight, also after an error
+        cudaStreamSynchronize(ps.sa);
+        cudaStreamSynchronize(ps.sb);
     }
     fclose(out);
     return rc;

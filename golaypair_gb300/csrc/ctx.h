@@ -135,7 +135,7 @@ struct gp_ctx {
     DevBuf scratch[16];
     // grow-only scratch of the uncompression stage (kept across pairs: a
     // cudaFree per pair would synchronise the device every pair)
-    DevBuf ux[48];
+    DevBuf ux[66];
     HostPinned hscratch[4];
     // batched generation: one stream per job branch, fork/join events
     static constexpr int kJobStreams = 8;
