@@ -151,15 +151,39 @@ std::vector<int> unit_generators(int L) {
 // reverse, decimation by generators of the unit group, alternating
 // negation.  Same set, about 15x less work at length 57.
 // Returns the items flat: count x W entries.
-std::vector<int16_t> pair_generators(int L, int compress) {
+//
+// Every generator maps each half affinely (position i takes +-entry
+// u*i + s of one half, one u for both halves up to sign, the sign set by the
+// parity of i), and so does every product of them.  An element is therefore
+// fixed by the entries at positions 0, 1, L and L+1: with by_key the closure
+// compares those 64 bits instead of all 2L entries.  The items are built by
+// applying generators, never inferred, so when that closure reaches the
+// group's known size it is the group; pair_generators checks exactly that
+// and otherwise redoes the closure comparing whole items.
+uint64_t pair_group_size(int L, int compress);
+extern const uint64_t kMaxGroupBytes;
+
+std::vector<int16_t> pair_closure(int L, int compress, bool by_key) {
     const int W = 2 * L;
     const bool use_alt = !(compress > 1 || L % 2 == 1);  // filter.cpp:83-87
     const std::vector<int> units = unit_generators(L);
     std::vector<int16_t> out;            // items, W entries each
     std::vector<uint32_t> slot(1u << 10, UINT32_MAX);  // open addressing: item index per slot
+    std::vector<uint64_t> keys;  // by_key: every item's key
     size_t count = 0;
+    auto key_of = [&](const int16_t* v) {
+        return (uint64_t)(uint16_t)v[0] | (uint64_t)(uint16_t)v[1] << 16 | (uint64_t)(uint16_t)v[L] << 32 |
+               (uint64_t)(uint16_t)v[L + 1] << 48;
+    };
+    auto mix = [](uint64_t h) {  // MurmurHash3's 64-bit finaliser
+        h ^= h >> 33;
+        h *= 0xff51afd7ed558ccdULL;
+        h ^= h >> 33;
+        h *= 0xc4ceb9fe1a85ec53ULL;
+        return h ^ (h >> 33);
+    };
     auto hash = [&](const int16_t* v) {
-        uint64_t h = 1469598103934665603ULL;
+        uint64_t h = 1469598103934665603ULL;  // FNV-1a over the whole item
         for (int i = 0; i < W; ++i) {
             h ^= (uint16_t)v[i];
             h *= 1099511628211ULL;
@@ -170,7 +194,7 @@ std::vector<int16_t> pair_generators(int L, int compress) {
         std::vector<uint32_t> ns(slot.size() * 2, UINT32_MAX);
         const size_t mask = ns.size() - 1;
         for (size_t i = 0; i < count; ++i) {
-            size_t h = hash(out.data() + i * W) & mask;
+            size_t h = (by_key ? mix(keys[i]) : hash(out.data() + i * W)) & mask;
             while (ns[h] != UINT32_MAX) h = (h + 1) & mask;
             ns[h] = (uint32_t)i;
         }
@@ -179,58 +203,95 @@ std::vector<int16_t> pair_generators(int L, int compress) {
     auto add = [&](const int16_t* v) {
         if (2 * (count + 1) > slot.size()) grow();
         const size_t mask = slot.size() - 1;
-        size_t h = hash(v) & mask;
+        const uint64_t k = by_key ? key_of(v) : 0;
+        size_t h = (by_key ? mix(k) : hash(v)) & mask;
         while (slot[h] != UINT32_MAX) {
-            if (std::memcmp(out.data() + (size_t)slot[h] * W, v, (size_t)W * 2) == 0) return;
+            if (by_key ? keys[slot[h]] == k : std::memcmp(out.data() + (size_t)slot[h] * W, v, (size_t)W * 2) == 0)
+                return;
             h = (h + 1) & mask;
         }
         slot[h] = (uint32_t)count++;
         out.insert(out.end(), v, v + W);
+        if (by_key) keys.push_back(k);
     };
+    auto find_key = [&](uint64_t k) {
+        const size_t mask = slot.size() - 1;
+        for (size_t h = mix(k) & mask; slot[h] != UINT32_MAX; h = (h + 1) & mask)
+            if (keys[slot[h]] == k) return true;
+        return false;
+    };
+    // the generators as maps: output position j takes (neg[j] ? -1 : 1) * input[src[j]]
+    struct Gen {
+        std::vector<int> src;
+        std::vector<char> neg;
+    };
+    std::vector<Gen> gens;
+    auto identity = [&]() {
+        Gen g{std::vector<int>(W), std::vector<char>(W, 0)};
+        for (int j = 0; j < W; ++j) g.src[j] = j;
+        return g;
+    };
+    if (L > 1) {  // shift_pair by 1: rotate b left by 1
+        Gen g = identity();
+        for (int i = 0; i < L; ++i) g.src[L + i] = L + (i + 1) % L;
+        gens.push_back(g);
+    }
+    {  // swap_pair
+        Gen g = identity();
+        for (int i = 0; i < L; ++i) {
+            g.src[i] = L + i;
+            g.src[L + i] = i;
+        }
+        gens.push_back(g);
+    }
+    {  // reverse_pair: reverse b
+        Gen g = identity();
+        for (int i = 0; i < L; ++i) g.src[L + i] = L + L - 1 - i;
+        gens.push_back(g);
+    }
+    for (int u : units) {  // decimate_pair: both parts, new[i] = old[i*u mod L]
+        Gen g = identity();
+        for (int i = 0; i < L; ++i) {
+            g.src[i] = (int)(((long long)i * u) % L);
+            g.src[L + i] = L + g.src[i];
+        }
+        gens.push_back(g);
+    }
+    if (use_alt) {  // altnegative_pair: negate odd positions of both
+        Gen g = identity();
+        for (int i = 1; i < L; i += 2) g.neg[i] = g.neg[L + i] = 1;
+        gens.push_back(g);
+    }
+    const uint64_t expect = pair_group_size(L, compress);
+    if (expect * (uint64_t)W * 2 <= kMaxGroupBytes) out.reserve((size_t)expect * W);
     std::vector<int16_t> cur(W), n(W);
+    auto at = [&](const Gen& g, int j) { return g.neg[j] ? (int16_t)-cur[g.src[j]] : cur[g.src[j]]; };
     for (int i = 0; i < L; ++i) {
         cur[i] = (int16_t)(i + 1);
         cur[L + i] = (int16_t)(L + i + 1);
     }
-    // source index of every decimation, and of the shift by 1
-    std::vector<std::vector<int>> dec(units.size(), std::vector<int>(L));
-    for (size_t k = 0; k < units.size(); ++k)
-        for (int i = 0; i < L; ++i) dec[k][i] = (int)(((long long)i * units[k]) % L);
-    std::vector<int> nxt(L);
-    for (int i = 0; i < L; ++i) nxt[i] = (i + 1) % L;
     add(cur.data());
-    for (size_t at = 0; at < count; ++at) {
-        std::memcpy(cur.data(), out.data() + at * W, (size_t)W * 2);
-        if (L > 1) {  // shift_pair by 1: rotate b left by 1
-            n = cur;
-            for (int i = 0; i < L; ++i) n[L + i] = cur[L + nxt[i]];
-            add(n.data());
-        }
-        for (int i = 0; i < L; ++i) {  // swap_pair
-            n[i] = cur[L + i];
-            n[L + i] = cur[i];
-        }
-        add(n.data());
-        n = cur;  // reverse_pair: reverse b
-        for (int i = 0; i < L; ++i) n[L + i] = cur[L + L - 1 - i];
-        add(n.data());
-        for (const auto& d : dec) {  // decimate_pair: both parts, new[i] = old[i*u mod L]
-            for (int i = 0; i < L; ++i) {
-                n[i] = cur[d[i]];
-                n[L + i] = cur[L + d[i]];
+    for (size_t item = 0; item < count; ++item) {
+        std::memcpy(cur.data(), out.data() + item * W, (size_t)W * 2);
+        for (const Gen& g : gens) {
+            if (by_key) {  // look the image up by its key; write it out only when new
+                const uint64_t k = (uint64_t)(uint16_t)at(g, 0) | (uint64_t)(uint16_t)at(g, 1) << 16 |
+                                   (uint64_t)(uint16_t)at(g, L) << 32 | (uint64_t)(uint16_t)at(g, L + 1) << 48;
+                if (find_key(k)) continue;
             }
-            add(n.data());
-        }
-        if (use_alt) {  // altnegative_pair: negate odd positions of both
-            n = cur;
-            for (int i = 1; i < L; i += 2) {
-                n[i] = (int16_t)-n[i];
-                n[L + i] = (int16_t)-n[L + i];
-            }
+            for (int j = 0; j < W; ++j) n[j] = at(g, j);
             add(n.data());
         }
     }
     return out;
+}
+
+std::vector<int16_t> pair_generators(int L, int compress) {
+    if (L >= 3) {
+        std::vector<int16_t> g = pair_closure(L, compress, true);
+        if (g.size() == pair_group_size(L, compress) * (uint64_t)(2 * L)) return g;
+    }
+    return pair_closure(L, compress, false);
 }
 
 // Rewrites a generator item as "output position o takes +-input[src]" over
@@ -265,7 +326,7 @@ uint64_t pair_group_size(int L, int compress) {
 }
 
 // The group's items take 2L int16 each on the host and again on the device.
-constexpr uint64_t kMaxGroupBytes = uint64_t(1) << 32;
+extern const uint64_t kMaxGroupBytes = uint64_t(1) << 32;
 
 }  // namespace
 
