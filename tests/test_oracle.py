@@ -160,3 +160,13 @@ def test_notes_order72_compression6_candidate_is_a_pair(oracle_lib):
     assert [int((a * np.roll(a, -s)).sum() + (b * np.roll(b, -s)).sum()) for s in range(1, 7)] == [0] * 6
     psd = np.abs(np.fft.fft(a)) ** 2 + np.abs(np.fft.fft(b)) ** 2
     assert np.allclose(psd[1:], 144)
+
+
+@pytest.mark.parametrize("L,compress", [(26, 1), (30, 1), (27, 2)])
+def test_keyed_group_matches_oracle_closure(oracle_lib, L, compress):
+    """The library builds the pair group by 64-bit keys of its elements; the
+    oracle closes the reference's operations comparing whole items.  Sizes at
+    lengths past the range above, with and without the alternating
+    negation."""
+    import golaypair_gb300 as gp
+    assert gp.lib().gp_debug_pair_generator_count(L, compress) == oracle_lib.gpo_pair_generator_count(L, compress)
