@@ -113,6 +113,7 @@ _STAGE_SIGS = {
     "gp_set_spectral_prune": [_P, _i32],
     "gp_job_ranges": [_i32, _i32, _i32, _i32, _i32, _P, _i64],
     "gp_debug_wait_timeout": [_P, _i64],
+    "gp_check": [_P, _P],
     "gp_debug_pair_generator_count": [_i32, _i32],
 }
 
@@ -203,6 +204,11 @@ class Context:
                                                   stream_ptr, ctypes.byref(st) if st is not None else None),
                    "gp_psd_filter_device")
         return st
+
+    def check_stream(self, stream_ptr=None):
+        """gp_check: waits for the stream and raises on a device-side error
+        recorded by the context's kernels (timeout, overflow)."""
+        self.check(self._lib.gp_check(self._h, stream_ptr), "gp_check")
 
     def psd_filter_host_raw(self, seqs_ptr, n, L, order, paf, mode, mask_ptr):
         """Host-buffer filter on raw pointers (e.g. pinned memory)."""

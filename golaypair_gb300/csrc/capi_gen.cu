@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <stdexcept>
 #include <string>
 #include <thread>
 #include <vector>
@@ -735,6 +736,15 @@ int save_checkpoint(gp_ctx* c, const char* path, const GenPlan& p, const std::st
 int load_checkpoint(gp_ctx* c, const char* path, const GenPlan& p, const std::string& spec, JobRun& j) {
     FILE* f = fopen(path, "rb");
     if (!f) return c->fail(GP_ERR_IO, "cannot read checkpoint %s", path);
+    // counts read from the file are checked against the bytes left before
+    // anything is sized by them: a damaged file is GP_ERR_FORMAT
+    fseek(f, 0, SEEK_END);
+    const long fsize = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    auto left = [&]() -> uint64_t {
+        const long pos = ftell(f);
+        return pos < 0 || fsize < pos ? 0 : (uint64_t)(fsize - pos);
+    };
     char magic[8];
     int32_t order = 0, compress = 0, paf = 0, L = 0;
     uint32_t n = 0;
@@ -748,7 +758,7 @@ int load_checkpoint(gp_ctx* c, const char* path, const GenPlan& p, const std::st
     }
     ok = ok && get(f, j.st.necklaces) && get(f, j.st.candidates) && get(f, j.st.psd_pass) && get(f, j.st.unsure);
     uint64_t nr = 0;
-    ok = ok && get(f, nr);
+    ok = ok && get(f, nr) && nr <= left() / 32;
     j.ranges.clear();
     for (uint64_t i = 0; ok && i < nr; ++i) {
         gp::u128 lo = 0, hi = 0;
@@ -757,7 +767,7 @@ int load_checkpoint(gp_ctx* c, const char* path, const GenPlan& p, const std::st
     }
     for (RecordSet* rs : {&j.ra, &j.rb}) {
         uint64_t m = 0;
-        ok = ok && get(f, m);
+        ok = ok && get(f, m) && m <= left() / (16 + 2 * (uint64_t)(p.L - 1));
         if (!ok) break;
         rs->words.resize(m);
         for (uint64_t i = 0; ok && i < m; ++i) ok = get_u128(f, rs->words[i]);
@@ -975,8 +985,12 @@ extern "C" int gp_generate_resumable(gp_ctx* c, int order, int compress, int paf
     if (rc) return rc;
     if (p.dec.empty()) return c->fail(GP_NO_DECOMPOSITION, "Order %d cannot be decomposed", order);
     const std::string spec = "shard " + std::to_string(proc_id) + " " + std::to_string(proc_num);
-    return generate_resumable(c, p, spec, shard_ranges(p, proc_id, proc_num), path_a, path_b, checkpoint_path,
-                              max_iterations, max_seconds, done, stats);
+    try {  // no C++ exception crosses the C ABI
+        return generate_resumable(c, p, spec, shard_ranges(p, proc_id, proc_num), path_a, path_b, checkpoint_path,
+                                  max_iterations, max_seconds, done, stats);
+    } catch (const std::exception& e) {
+        return c->fail(GP_ERR_NOMEM, "checkpointed generation: %s", e.what());
+    }
 }
 
 extern "C" int gp_generate_window_resumable(gp_ctx* c, int order, int compress, int paf, uint64_t begin_hi,
@@ -996,6 +1010,10 @@ extern "C" int gp_generate_window_resumable(gp_ctx* c, int order, int compress, 
     std::vector<std::pair<gp::u128, gp::u128>> ranges;
     if (lo < hi) ranges.emplace_back(lo, hi);
     const std::string spec = "window " + u128_dec(lo) + " " + u128_dec(hi);
-    return generate_resumable(c, p, spec, ranges, path_a, path_b, checkpoint_path, max_iterations, max_seconds, done,
-                              stats);
+    try {  // no C++ exception crosses the C ABI
+        return generate_resumable(c, p, spec, ranges, path_a, path_b, checkpoint_path, max_iterations, max_seconds,
+                                  done, stats);
+    } catch (const std::exception& e) {
+        return c->fail(GP_ERR_NOMEM, "checkpointed generation: %s", e.what());
+    }
 }

@@ -448,6 +448,14 @@ int gp_psd_filter_device(gp_ctx* c, const int8_t* d_seqs, int64_t n, int L, int 
     return GP_OK;
 }
 
+int gp_check(gp_ctx* c, void* stream) {
+    if (!c) return GP_ERR_ARG;
+    cudaSetDevice(c->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->s_comp;
+    GP_CUDA_TRY(c, cudaStreamSynchronize(st));
+    return c->check_status("gp_check");
+}
+
 int gp_psd_tc_values(gp_ctx* c, const int8_t* seqs, int64_t n, int L, float* out) {
     int rc = check_args(c, n, L, GP_PSD_TC_GUARDED);
     if (rc) return rc;

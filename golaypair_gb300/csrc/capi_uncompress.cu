@@ -3,99 +3,541 @@
 // Replaces uncompress_pipeline / uncompress_recursive
 // (src/core/uncompression/uncompression.cpp:32-210) and the GPU stub it can
 // dispatch to (src/core/uncompression/gpu/uncompress_gpu.cpp:17-92, whose
-// kernel computes nothing).  For every compressed pair (a, b):
-//   host    partition table per letter, the reference's rotation of the
-//           sequence, the first entry's partitions reduced to their
-//           rotation/reversal minima (uncompression.cpp:88-142);
-//   device  expand_kernel: mixed-radix rank -> uncompressed word (entry i's
-//           partition fills positions i, i+L, i+2L, ...; uncompression.cpp:
-//           144-165), then the tensor-core PSD filter at the new length,
-//           then finalize_kernel (exact FP64 PSD and signatures: a-side
-//           inverted, b-side plain, uncompression.cpp:195-207);
-//   device  the signature join of the two candidate sets (join.cu) with
-//           exact PAF verification; only the matched pairs come back to
-//           the host, where they are put in the reference's line order
-//           (sorted a-line, then b-line) and appended in input-pair order.
+// kernel computes nothing).  The reference, per compressed pair (a, b):
+// expands each side to every sequence of the new compression (entry i's
+// partition fills positions i, i+L, i+2L, ...), keeps the expansions whose
+// PSD passes the filter, writes them with their signatures to two scratch
+// files, sorts both and merge-joins them on the signature string with an
+// exact PAF check.  Here many pairs are uncompressed per launch sequence:
+//
+// 1. Host plan (uncompression.cpp:88-142): one partition table per letter,
+//    the reference's rotation of each side, its first entry's partitions
+//    reduced to rotation/reversal minima.  A side is a mixed-radix number
+//    over its positions; the expansion of rank t has digit d_i at position i.
+//
+// 2. ux_scan_kernel (fused expansion + PSD filter).  The DFT of an expansion
+//    is a sum of per-position terms, X_k = sum_i C_i(d_i, k) with
+//    C_i(d, k) = sum_q v_q(d) w^((i + L q) k), w = exp(-2 pi i / L').  Bins
+//    k that are multiples of the ratio r = c / c' do not depend on the
+//    expansion (they are the compressed sequence's DFT) and are checked once
+//    per side on the host.  For the other bins a thread adds the terms of the
+//    side's leading free positions once (its "prefix"), then walks a table of
+//    precomputed sums over the trailing free positions (the "suffix", up to a
+//    few hundred combinations in shared memory): one packed fp32 add per bin
+//    and |X|^2 per expansion.  A rigorous bound of the fp32 rounding error
+//    sorts every expansion into sure pass, sure reject, or unsure.
+// 3. ux_recheck_kernel: unsure expansions in FP64 (one warp per expansion,
+//    lanes over bins), the reference's filter psd[k] <= 2n - paf + 0.001.
+// 4. The join.  For a complementary pair, PAF_a(s) + PAF_b(s) = paf * c'
+//    (src/utils/golay.cpp:27-44) implies psd_a(k) + psd_b(k) = 2n - paf at
+//    every k != 0, so the a-side's inverted signature equals the b-side's
+//    plain one: every pair the reference writes joins on the exact integer
+//    PAF vectors (a: paf*c' - PAF_a, b: PAF_b).  ux_key_kernel hashes those
+//    vectors and buckets the survivors by (pair, hash bits);
+//    ux_join_kernel matches each bucket in a shared-memory hash table and
+//    verifies the PAF sums exactly.  No signature is computed on the device.
+// 5. Host: the few matched pairs get their FP64 signatures; a pair is kept
+//    when the two signature strings are equal (the reference's join key),
+//    and the pairs of each input pair are written in the order of the
+//    reference's sorted files (a line, then b line), input pairs in order.
 #include <algorithm>
+#include <array>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <set>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ctx.h"
-#include "finalize.h"
 #include "host_math.h"
-#include "join.h"
+#include "prims.h"
 
 namespace {
 
-constexpr int kMaxPos = 128;
-// context scratch buffers of the two sides' expansions (c->ux[slot .. slot+8]),
-// two sets so that one pair expands while the previous one is joined (join.cu
-// and the gather below use ux[8 .. 28])
-constexpr int kSlotA[2] = {30, 48}, kSlotB[2] = {39, 57};
+constexpr int kMaxL = 64;          // compressed length
+constexpr int kMaxLnew = 128;      // uncompressed length
+constexpr int kMaxRows = 32;       // letters + first-entry lists
+constexpr int kScanThreads = 256;  // prefixes per scan unit
+constexpr int kRankBits = 40;      // survivor word: side << 40 | rank
+constexpr uint64_t kRankMask = (uint64_t(1) << kRankBits) - 1;
+constexpr int kMaxSidesPerBatch = 1 << 23;
+constexpr int kBucketTarget = 512;  // survivors per join bucket (mean)
+constexpr int kJoinTab = 4096;      // shared hash slots of the join kernel
+constexpr int kJoinMaxB = kJoinTab / 2;
+constexpr size_t kScanSmemBudget = 96 * 1024;
 
-struct ExpandArgs {
-    int L;          // compressed length
-    int r;          // parts per entry
-    int Lnew;       // L * r
-    int b;          // bits per new digit
-    int cnew;       // new alphabet offset: digit = (value + cnew) / 2
-    uint64_t rank0;
-    int64_t n;          // ranks rank0 .. rank0 + n - 1, n <= 2^24
-    int d0[kMaxPos];    // mixed-radix digits of rank0 (position L-1 least significant)
-    const uint64_t* inv;  // ceil(2^40 / cnt[i]): t / cnt[i] = t * inv[i] >> 40 for t < 2^24
-    const int* cnt;     // choices per position
-    const int* off;     // offset of position i's table in vals (entries)
-    const int8_t* vals; // choice values, r per choice
-    uint4* words;
+// ------------------------------------------------------------ device side
+
+struct LevelDev {
+    int L, r, Lnew, H, nrows, dmax, np;  // np: bin pairs of the scan's template
+    int nb;                               // varying bins
+    int one_bit;                          // new alphabet is {-1, 1} and Lnew <= 64
+    int target;                           // paf * c'
+    const int* cnt;                       // [nrows] choices per row
+    const int8_t* vals;                   // [nrows][dmax][r] values of each choice
+    const float4* ctab;                   // [L][nrows][dmax][np]: (re 2p, re 2p+1, im 2p, im 2p+1)
+    const double2* ctab64;                // [L][nrows][dmax][2 np]
+    const uint8_t* side_rows;             // [sides][L] row of each position
 };
 
-__global__ void expand_kernel(ExpandArgs a) {
-    __shared__ int s_cnt[kMaxPos], s_off[kMaxPos];
-    for (int i = threadIdx.x; i < a.L; i += blockDim.x) {
-        s_cnt[i] = a.cnt[i];
-        s_off[i] = a.off[i];
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// digits of a rank: position L-1 least significant, positions with one
+// choice contribute nothing
+__device__ __forceinline__ void decode_rank(uint64_t rank, const uint8_t* rows, const int* cnt, int L, uint8_t* d) {
+    for (int i = L - 1; i >= 0; --i) {
+        const uint32_t c = (uint32_t)cnt[rows[i]];
+        if (c == 1) {
+            d[i] = 0;
+        } else if (rank >> 32) {
+            d[i] = (uint8_t)(rank % c);
+            rank /= c;
+        } else {
+            const uint32_t q = (uint32_t)rank / c;
+            d[i] = (uint8_t)((uint32_t)rank - q * c);
+            rank = q;
+        }
     }
-    __syncthreads();
-    __shared__ uint64_t s_inv[kMaxPos];
-    __shared__ int s_d0[kMaxPos];
-    for (int i = threadIdx.x; i < a.L; i += blockDim.x) {
-        s_inv[i] = a.inv[i];
-        s_d0[i] = a.d0[i];
-    }
-    __syncthreads();
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.n; t += (int64_t)gridDim.x * blockDim.x) {
-        // digits of rank0 + t: the digits of t (exact reciprocal division,
-        // t < 2^24) added to those of rank0 with carry
-        uint32_t rest = (uint32_t)t;
-        int carry = 0;
-        uint64_t lo = 0, hi = 0;
-        for (int i = a.L - 1; i >= 0; --i) {
-            const int c = s_cnt[i];
-            const uint32_t q = (uint32_t)(((uint64_t)rest * s_inv[i]) >> 40);
-            int d = (int)(rest - q * (uint32_t)c) + s_d0[i] + carry;
-            rest = q;
-            carry = d >= c;
-            if (carry) d -= c;
-            const int8_t* v = a.vals + (int64_t)(s_off[i] + d) * a.r;
-            for (int q = 0; q < a.r; ++q) {
-                const int p = i + a.L * q;
-                const uint64_t digit = (uint64_t)((v[q] + a.cnew) >> 1);
-                const int pos = a.b * (a.Lnew - 1 - p);
-                if (pos >= 64)
-                    hi |= digit << (pos - 64);
-                else {
-                    lo |= digit << pos;
-                    if (pos + a.b > 64 && pos > 0) hi |= digit >> (64 - pos);
+}
+
+struct ScanArgs {
+    LevelDev lv;
+    const uint64_t* unit_begin;    // [sides + 1]
+    const uint64_t* prefix_count;  // [sides]
+    const uint32_t* nsuf;          // [sides] free positions in the suffix table
+    int n_sides;
+    uint64_t n_units;
+    float thr_lo, thr_hi;          // sure pass below, sure reject above
+    uint64_t* surv;
+    uint64_t surv_cap;
+    uint64_t* unsure;
+    uint64_t unsure_cap;
+    unsigned long long* counters;  // [0] survivors [1] unsure [2] matches
+    uint32_t* side_count;          // survivors per side
+    int* status;
+};
+
+__device__ __forceinline__ void flag_overflow(int* status) { atomicCAS(status, 0, GP_KSTATUS_OVERFLOW); }
+
+template <int NP>
+__global__ void __launch_bounds__(kScanThreads) ux_scan_kernel(ScanArgs a) {
+    extern __shared__ float4 smem[];
+    __shared__ int s_side, s_nfree, s_npre;
+    __shared__ uint32_t s_scount;
+    __shared__ int s_pos[kMaxL], s_cnt[kMaxL], s_coff[kMaxL], s_dig0[kMaxL];
+    __shared__ float4 s_F[NP];
+    const LevelDev& lv = a.lv;
+    float4* s_S = smem;  // [scount][NP] suffix sums, then the free positions' terms
+    float4* s_C = smem;  // placed after the suffix table when a side starts
+    const int tid = threadIdx.x, lane = tid & 31;
+    int cur_side = -1;
+    uint32_t scount = 1;
+    for (uint64_t u = blockIdx.x; u < a.n_units; u += gridDim.x) {
+        __syncthreads();
+        if (tid == 0) {  // last side whose first unit is <= u
+            int lo = 0, hi = a.n_sides - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (a.unit_begin[mid] <= u)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            s_side = lo;
+        }
+        __syncthreads();
+        const int side = s_side;
+        const uint8_t* rows = lv.side_rows + (size_t)side * lv.L;
+        if (side != cur_side) {
+            cur_side = side;
+            if (tid == 0) {
+                int nfree = 0, off = 0;
+                for (int i = 0; i < lv.L; ++i) {
+                    const int c = lv.cnt[rows[i]];
+                    if (c > 1) {
+                        s_pos[nfree] = i;
+                        s_cnt[nfree] = c;
+                        s_coff[nfree] = off;
+                        off += c * NP;
+                        ++nfree;
+                    }
+                }
+                const int nsuf = (int)a.nsuf[side];
+                uint32_t sc = 1;
+                for (int f = nfree - nsuf; f < nfree; ++f) sc *= (uint32_t)s_cnt[f];
+                s_nfree = nfree;
+                s_npre = nfree - nsuf;
+                s_scount = sc;
+            }
+            __syncthreads();
+            scount = s_scount;
+            s_C = smem + (size_t)scount * NP;
+            const int nfree = s_nfree, npre = s_npre;
+            // the free positions' terms, then the fixed positions' sum
+            for (int f = 0; f < nfree; ++f) {
+                const int i = s_pos[f], c = s_cnt[f];
+                const float4* src = lv.ctab + ((size_t)(i * lv.nrows + rows[i]) * lv.dmax) * NP;
+                for (int k = tid; k < c * NP; k += kScanThreads) s_C[s_coff[f] + k] = src[k];
+            }
+            if (tid < NP) {
+                float4 F = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int i = 0; i < lv.L; ++i) {
+                    if (lv.cnt[rows[i]] != 1) continue;
+                    const float4 t = lv.ctab[((size_t)(i * lv.nrows + rows[i]) * lv.dmax) * NP + tid];
+                    F.x += t.x;
+                    F.y += t.y;
+                    F.z += t.z;
+                    F.w += t.w;
+                }
+                s_F[tid] = F;
+            }
+            __syncthreads();
+            // suffix table: every combination of the trailing free positions
+            for (uint32_t k = tid; k < scount * NP; k += kScanThreads) {
+                const uint32_t j = k / NP, p = k - j * NP;
+                uint32_t rem = j;
+                float4 S = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int f = nfree - 1; f >= npre; --f) {
+                    const uint32_t c = (uint32_t)s_cnt[f];
+                    const uint32_t q = rem / c;
+                    const uint32_t d = rem - q * c;
+                    rem = q;
+                    const float4 t = s_C[s_coff[f] + d * NP + p];
+                    S.x += t.x;
+                    S.y += t.y;
+                    S.z += t.z;
+                    S.w += t.w;
+                }
+                s_S[j * NP + p] = S;
+            }
+        }
+        // digits of the unit's first prefix index (prefix positions only)
+        const uint64_t pre0 = (u - a.unit_begin[side]) * (uint64_t)kScanThreads;
+        if (tid == 0) {
+            uint64_t rem = pre0;
+            for (int f = s_npre - 1; f >= 0; --f) {
+                const uint64_t c = (uint64_t)s_cnt[f];
+                s_dig0[f] = (int)(rem % c);
+                rem /= c;
+            }
+        }
+        __syncthreads();
+        const uint64_t pidx = pre0 + (uint64_t)tid;
+        const bool active = pidx < a.prefix_count[side];
+        float2 Pr[NP], Pi[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const float4 F = s_F[p];
+            Pr[p] = make_float2(F.x, F.y);
+            Pi[p] = make_float2(F.z, F.w);
+        }
+        {
+            uint32_t t = (uint32_t)tid;
+            int carry = 0;
+            for (int f = s_npre - 1; f >= 0; --f) {
+                const uint32_t c = (uint32_t)s_cnt[f];
+                const uint32_t q = t / c;
+                int d = (int)(t - q * c) + s_dig0[f] + carry;
+                t = q;
+                carry = d >= (int)c;
+                if (carry) d -= (int)c;
+                const float4* tp = s_C + s_coff[f] + d * NP;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    const float4 v = tp[p];
+                    Pr[p] = __fadd2_rn(Pr[p], make_float2(v.x, v.y));
+                    Pi[p] = __fadd2_rn(Pi[p], make_float2(v.z, v.w));
                 }
             }
         }
-        a.words[t] = make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+        const uint64_t rank0 = pidx * (uint64_t)scount;
+        const float inf = __int_as_float(0x7f800000);
+        for (uint32_t j = 0; j < scount; ++j) {
+            const float4* S = s_S + j * NP;
+            float m0 = active ? 0.f : inf, m1 = m0;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const float4 s = S[p];
+                const float2 xr = __fadd2_rn(Pr[p], make_float2(s.x, s.y));
+                const float2 xi = __fadd2_rn(Pi[p], make_float2(s.z, s.w));
+                const float2 q = __ffma2_rn(xr, xr, __fmul2_rn(xi, xi));
+                if (p & 1)
+                    m1 = max3f(m1, q.x, q.y);
+                else
+                    m0 = max3f(m0, q.x, q.y);
+            }
+            const float m = fmaxf(m0, m1);
+            const bool cand = m <= a.thr_hi;
+            const unsigned bal = __ballot_sync(0xFFFFFFFFu, cand);
+            if (bal) {
+                const bool sure = cand && m < a.thr_lo;
+                const unsigned bs = __ballot_sync(0xFFFFFFFFu, sure);
+                const unsigned bu = bal & ~bs;
+                unsigned long long base_s = 0, base_u = 0;
+                if (lane == 0) {
+                    if (bs) {
+                        base_s = atomicAdd(&a.counters[0], (unsigned long long)__popc(bs));
+                        atomicAdd(&a.side_count[side], (uint32_t)__popc(bs));
+                    }
+                    if (bu) base_u = atomicAdd(&a.counters[1], (unsigned long long)__popc(bu));
+                }
+                base_s = __shfl_sync(0xFFFFFFFFu, base_s, 0);
+                base_u = __shfl_sync(0xFFFFFFFFu, base_u, 0);
+                if (cand) {
+                    const unsigned lt = (1u << lane) - 1u;
+                    const uint64_t val = ((uint64_t)side << kRankBits) | (rank0 + j);
+                    if (sure) {
+                        const unsigned long long pos = base_s + __popc(bs & lt);
+                        if (pos < a.surv_cap)
+                            a.surv[pos] = val;
+                        else
+                            flag_overflow(a.status);
+                    } else {
+                        const unsigned long long pos = base_u + __popc(bu & lt);
+                        if (pos < a.unsure_cap)
+                            a.unsure[pos] = val;
+                        else
+                            flag_overflow(a.status);
+                    }
+                }
+            }
+        }
     }
 }
+
+// The unsure expansions in FP64: each lane decodes one expansion's digits
+// into shared memory, then the warp takes its 32 expansions in turn with
+// lanes over the bins (the reference's filter, fourier.cpp:45-52).
+struct RecheckArgs {
+    LevelDev lv;
+    double thr;
+    const uint64_t* unsure;
+    uint64_t unsure_cap;
+    uint64_t* surv;
+    uint64_t surv_cap;
+    unsigned long long* counters;
+    uint32_t* side_count;
+    int* status;
+};
+
+constexpr int kRecheckWarps = 4;
+
+__global__ void __launch_bounds__(kRecheckWarps * 32) ux_recheck_kernel(RecheckArgs a) {
+    __shared__ uint8_t s_dig[kRecheckWarps][32][kMaxL];
+    const LevelDev& lv = a.lv;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t n = min((uint64_t)a.counters[1], a.unsure_cap);
+    const uint64_t gw = (uint64_t)blockIdx.x * kRecheckWarps + warp, nw = (uint64_t)gridDim.x * kRecheckWarps;
+    for (uint64_t base = gw * 32; base < n; base += nw * 32) {
+        uint64_t val = 0;
+        if (base + lane < n) {
+            val = a.unsure[base + lane];
+            decode_rank(val & kRankMask, lv.side_rows + (size_t)(val >> kRankBits) * lv.L, lv.cnt, lv.L,
+                        s_dig[warp][lane]);
+        }
+        __syncwarp();
+        const int m = (int)min((uint64_t)32, n - base);
+        for (int e = 0; e < m; ++e) {
+            const uint64_t v = __shfl_sync(0xFFFFFFFFu, val, e);
+            const int side = (int)(v >> kRankBits);
+            const uint8_t* rows = lv.side_rows + (size_t)side * lv.L;
+            double pmax = 0.0;
+            for (int b = lane; b < lv.nb; b += 32) {
+                double re = 0.0, im = 0.0;
+                for (int i = 0; i < lv.L; ++i) {
+                    const double2 t =
+                        lv.ctab64[((size_t)(i * lv.nrows + rows[i]) * lv.dmax + s_dig[warp][e][i]) * (2 * lv.np) + b];
+                    re += t.x;
+                    im += t.y;
+                }
+                pmax = fmax(pmax, re * re + im * im);
+            }
+            for (int o = 16; o; o >>= 1) pmax = fmax(pmax, __shfl_xor_sync(0xFFFFFFFFu, pmax, o));
+            if (lane == 0 && pmax <= a.thr) {
+                const unsigned long long pos = atomicAdd(&a.counters[0], 1ull);
+                atomicAdd(&a.side_count[side], 1u);
+                if (pos < a.surv_cap)
+                    a.surv[pos] = v;
+                else
+                    flag_overflow(a.status);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Values of an expansion at its Lnew positions.
+__device__ __forceinline__ void expand_values(const LevelDev& lv, uint64_t val, int8_t* x) {
+    uint8_t d[kMaxL];
+    const uint8_t* rows = lv.side_rows + (size_t)(val >> kRankBits) * lv.L;
+    decode_rank(val & kRankMask, rows, lv.cnt, lv.L, d);
+    for (int i = 0; i < lv.L; ++i) {
+        const int8_t* v = lv.vals + ((size_t)rows[i] * lv.dmax + d[i]) * lv.r;
+        for (int q = 0; q < lv.r; ++q) x[i + lv.L * q] = v[q];
+    }
+}
+
+// PAF(s), s = 1 .. H, of an expansion (src/utils/golay.cpp:27-33).
+__device__ __forceinline__ void expansion_paf(const LevelDev& lv, uint64_t val, int* paf) {
+    int8_t x[kMaxLnew];
+    expand_values(lv, val, x);
+    const int N = lv.Lnew;
+    if (lv.one_bit) {
+        uint64_t w = 0;
+        for (int j = 0; j < N; ++j) w |= (uint64_t)(x[j] > 0) << j;
+        const uint64_t mask = N == 64 ? ~0ull : ((1ull << N) - 1ull);
+        for (int s = 1; s <= lv.H; ++s) {
+            const uint64_t rot = ((w >> s) | (w << (N - s))) & mask;  // bit j = bit j + s of w
+            paf[s - 1] = N - 2 * __popcll(w ^ rot);
+        }
+        return;
+    }
+    for (int s = 1; s <= lv.H; ++s) {
+        int acc = 0, j2 = s;
+        for (int j = 0; j < N; ++j) {
+            acc += (int)x[j] * (int)x[j2];
+            if (++j2 == N) j2 = 0;
+        }
+        paf[s - 1] = acc;
+    }
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t h) {
+    h ^= h >> 33;
+    h *= 0xff51afd7ed558ccdull;
+    h ^= h >> 33;
+    h *= 0xc4ceb9fe1a85ec53ull;
+    h ^= h >> 33;
+    return h;
+}
+
+// join key of a survivor: a-sides (even side index) hash paf*c' - PAF_a(s),
+// b-sides PAF_b(s); complementary pairs have equal keys
+__device__ __forceinline__ uint64_t join_key(const LevelDev& lv, uint64_t val) {
+    int paf[kMaxLnew / 2];
+    expansion_paf(lv, val, paf);
+    const bool is_a = ((val >> kRankBits) & 1) == 0;
+    uint64_t h = 0x243f6a8885a308d3ull;
+    for (int s = 0; s < lv.H; ++s) {
+        const int v = is_a ? lv.target - paf[s] : paf[s];
+        h = (h ^ (uint64_t)(uint32_t)v) * 0x100000001b3ull;
+    }
+    return mix64(h);
+}
+
+struct KeyArgs {
+    LevelDev lv;
+    const uint64_t* surv;
+    uint64_t n;
+    const uint8_t* pair_lg;     // [pairs] log2 buckets of the pair (255: pair skipped)
+    const uint32_t* pair_base;  // [pairs] first bucket of the pair
+    uint64_t* keys;
+    uint32_t* bucket;
+    uint32_t* bcount;
+};
+
+__global__ void ux_key_kernel(KeyArgs a) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = a.surv[i];
+        const uint32_t pair = (uint32_t)(v >> (kRankBits + 1));
+        const int lg = a.pair_lg[pair];
+        if (lg == 255) {
+            a.bucket[i] = 0xFFFFFFFFu;
+            continue;
+        }
+        const uint64_t h = join_key(a.lv, v);
+        const uint32_t b = a.pair_base[pair] + (lg ? (uint32_t)(h >> (64 - lg)) : 0u);
+        a.keys[i] = h;
+        a.bucket[i] = b;
+        atomicAdd(&a.bcount[b], 1u);
+    }
+}
+
+__global__ void ux_scatter_kernel(const uint64_t* surv, const uint64_t* keys, const uint32_t* bucket, uint64_t n,
+                                  const uint32_t* boff, uint32_t* bcur, uint64_t* ent_h, uint32_t* ent_i) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = bucket[i];
+        if (b == 0xFFFFFFFFu) continue;
+        const uint32_t pos = boff[b] + atomicAdd(&bcur[b], 1u);
+        ent_h[pos] = keys[i];
+        ent_i[pos] = (uint32_t)i | ((uint32_t)((surv[i] >> kRankBits) & 1) << 31);  // bit 31: b-side
+    }
+}
+
+struct JoinArgs {
+    LevelDev lv;
+    const uint64_t* surv;
+    const uint64_t* ent_h;
+    const uint32_t* ent_i;
+    const uint32_t* boff;
+    const uint32_t* bcount;
+    uint32_t n_buckets;
+    uint64_t* matches;  // (a survivor word, b survivor word)
+    uint64_t match_cap;
+    unsigned long long* counters;
+    int* status;
+};
+
+__device__ __forceinline__ void verify_and_emit(const JoinArgs& a, uint32_t ia, uint32_t ib) {
+    int pa[kMaxLnew / 2], pb[kMaxLnew / 2];
+    const uint64_t va = a.surv[ia], vb = a.surv[ib];
+    expansion_paf(a.lv, va, pa);
+    expansion_paf(a.lv, vb, pb);
+    for (int s = 0; s < a.lv.H; ++s)
+        if (pa[s] + pb[s] != a.lv.target) return;
+    const unsigned long long pos = atomicAdd(&a.counters[2], 1ull);
+    if (pos < a.match_cap) {
+        a.matches[2 * pos] = va;
+        a.matches[2 * pos + 1] = vb;
+    } else {
+        flag_overflow(a.status);
+    }
+}
+
+// One bucket per block iteration: b-side entries into a shared hash table
+// keyed by the low hash bits (the bucket came from the high ones), a-side
+// entries probe it.  A bucket too large for the table is joined pairwise.
+__global__ void __launch_bounds__(256) ux_join_kernel(JoinArgs a) {
+    __shared__ uint32_t tab[kJoinTab];
+    for (uint32_t bk = blockIdx.x; bk < a.n_buckets; bk += gridDim.x) {
+        const uint32_t n = a.bcount[bk], base = a.boff[bk];
+        __syncthreads();
+        if (n > kJoinMaxB) {  // rare: quadratic over the bucket
+            for (uint64_t w = threadIdx.x; w < (uint64_t)n * n; w += blockDim.x) {
+                const uint32_t e = (uint32_t)(w / n), f = (uint32_t)(w % n);
+                const uint32_t ie = a.ent_i[base + e], jf = a.ent_i[base + f];
+                if ((ie >> 31) || !(jf >> 31) || a.ent_h[base + e] != a.ent_h[base + f]) continue;
+                verify_and_emit(a, ie & 0x7FFFFFFFu, jf & 0x7FFFFFFFu);
+            }
+            continue;
+        }
+        for (int k = threadIdx.x; k < kJoinTab; k += blockDim.x) tab[k] = 0;
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+            if (!(a.ent_i[base + e] >> 31)) continue;
+            uint32_t slot = (uint32_t)a.ent_h[base + e] & (kJoinTab - 1);
+            while (atomicCAS(&tab[slot], 0u, e + 1) != 0u) slot = (slot + 1) & (kJoinTab - 1);
+        }
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+            const uint32_t ie = a.ent_i[base + e];
+            if (ie >> 31) continue;
+            const uint64_t h = a.ent_h[base + e];
+            uint32_t slot = (uint32_t)h & (kJoinTab - 1);
+            for (uint32_t t; (t = tab[slot]) != 0u; slot = (slot + 1) & (kJoinTab - 1))
+                if (a.ent_h[base + t - 1] == h) verify_and_emit(a, ie, a.ent_i[base + t - 1] & 0x7FFFFFFFu);
+        }
+    }
+}
+
+// ------------------------------------------------------------ host side
 
 // src/utils/array.cpp:131-160: non-decreasing sequences of length len
 void combinations(int len, const std::vector<int>& alpha, std::vector<std::vector<int>>& out) {
@@ -113,21 +555,46 @@ void combinations(int len, const std::vector<int>& alpha, std::vector<std::vecto
     }
 }
 
-struct Expansion {
-    std::vector<int> cnt, off;
-    std::vector<int8_t> vals;
-    uint64_t total = 1;
-    bool overflow = false;
+// One uncompression level (order, c -> c') with its tables.
+struct Level {
+    int order = 0, c = 0, cn = 0, paf = 0, L = 0, r = 0, Lnew = 0, H = 0, nb = 0, np = 0;
+    int A = 0, nrows = 0, dmax = 0, smax = 0;
+    std::vector<int> alpha, nalpha;
+    std::map<int, int> letter_index;
+    std::vector<std::vector<std::vector<int>>> rowparts;  // [row][choice] -> r values
+    std::vector<int> bins;     // varying bins
+    std::vector<int> cbins;    // bins that are multiples of r (constant per side)
+    double thr = 0;            // 2n - paf + 0.001
+    float thr_lo = 0, thr_hi = 0;
+    std::vector<double> cs, sn;  // cos / sin (2 pi m / Lnew)
 };
 
-// src/core/uncompression/uncompression.cpp:88-142 (orig is rotated in place)
-Expansion plan_expansion(std::vector<int>& orig, int compress, int new_compress) {
-    const std::vector<int> alpha = gp::alphabet(compress), nalpha = gp::alphabet(new_compress);
-    const int r = compress / new_compress;
+// The reference's partition table and first-entry reduction
+// (uncompression.cpp:88-142): rows 0..A-1 hold every ordered partition of
+// letter a into r new letters (next_permutation order of each sorted
+// combination); rows A..2A-1 the rotation/reversal minima of those
+// partitions, the choices of a side's first entry.
+int build_level(gp_ctx* c, Level& lv, int order, int compress, int new_compress, int paf) {
+    lv.order = order;
+    lv.c = compress;
+    lv.cn = new_compress;
+    lv.paf = paf;
+    lv.L = order / compress;
+    lv.r = compress / new_compress;
+    lv.Lnew = lv.L * lv.r;
+    lv.H = lv.Lnew / 2;
+    lv.alpha = gp::alphabet(compress);
+    lv.nalpha = gp::alphabet(new_compress);
+    lv.A = (int)lv.alpha.size();
+    if (lv.L > kMaxL || lv.Lnew > kMaxLnew || 2 * lv.A > kMaxRows)
+        return c->fail(GP_ERR_UNSUPPORTED, "uncompress: length %d -> %d over %d letters", lv.L, lv.Lnew, lv.A);
+    const int r = lv.r;
     std::vector<std::vector<int>> parts;
-    combinations(r, nalpha, parts);
-    std::map<int, std::vector<std::vector<int>>> partitions;
-    for (int letter : alpha) {
+    combinations(r, lv.nalpha, parts);
+    lv.rowparts.assign(2 * lv.A, {});
+    for (int a = 0; a < lv.A; ++a) {
+        const int letter = lv.alpha[a];
+        lv.letter_index[letter] = a;
         std::vector<std::vector<int>> list;
         for (auto part : parts) {
             int sum = 0;
@@ -137,57 +604,191 @@ Expansion plan_expansion(std::vector<int>& orig, int compress, int new_compress)
                 list.push_back(part);
             } while (std::next_permutation(part.begin(), part.end()));
         }
-        partitions[letter] = list;
+        std::set<std::vector<int>> first;
+        for (auto& perm : list) {
+            std::vector<int> mn = perm;
+            for (int rev = 0; rev < 2; ++rev)
+                for (int s = 0; s < r; ++s) {
+                    std::vector<int> cand(r);
+                    for (int i = 0; i < r; ++i) {
+                        const int src = (i + s) % r;
+                        cand[i] = rev ? perm[r - 1 - src] : perm[src];
+                    }
+                    if (cand < mn) mn = cand;
+                }
+            first.insert(mn);
+        }
+        lv.rowparts[a] = list;
+        lv.rowparts[lv.A + a] = std::vector<std::vector<int>>(first.begin(), first.end());
     }
+    lv.nrows = 2 * lv.A;
+    lv.dmax = 1;
+    for (auto& row : lv.rowparts) lv.dmax = std::max<int>(lv.dmax, (int)row.size());
+    for (int k = 1; k <= lv.H; ++k) (k % r ? lv.bins : lv.cbins).push_back(k);
+    lv.nb = (int)lv.bins.size();
+    // bin pairs of the scan kernel's template
+    const int want = (lv.nb + 1) / 2;
+    static const int kNp[] = {2, 4, 6, 8, 10, 12, 16, 24, 32};
+    lv.np = 0;
+    for (int p : kNp)
+        if (p >= want) {
+            lv.np = p;
+            break;
+        }
+    if (!lv.np) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %d varying bins", lv.nb);
+    const size_t ctab_bytes = (size_t)lv.L * lv.dmax * lv.np * 16;
+    if (ctab_bytes + 16 * lv.np > kScanSmemBudget / 2)
+        return c->fail(GP_ERR_UNSUPPORTED, "uncompress: partition tables too large (%zu bytes)", ctab_bytes);
+    lv.smax = (int)std::min<size_t>(729, (kScanSmemBudget - ctab_bytes) / ((size_t)lv.np * 16));
+    lv.thr = 2.0 * order - paf + 0.001;
+    // rigorous fp32 error of |X_k|^2: terms and partial sums per component are
+    // at most L r max|v|; table rounding and at most L + 1 additions each add
+    // a relative 2^-24 of that; the square and sum two more roundings
+    const double u = std::ldexp(1.0, -24);
+    const double comp = (double)lv.L * r * new_compress;
+    const double eps = std::sqrt(2.0) * (2.0 * lv.L + 2.0) * u * comp;
+    const double delta = 2.0 * (2.0 * std::sqrt(lv.thr + 1.0) * eps + 3.0 * eps * eps + 4.0 * u * (lv.thr + 1.0));
+    lv.thr_lo = std::nextafter((float)(lv.thr - delta), 0.f);
+    lv.thr_hi = std::nextafter((float)(lv.thr + delta), 1e30f);
+    lv.cs.resize(lv.Lnew);
+    lv.sn.resize(lv.Lnew);
+    for (int m = 0; m < lv.Lnew; ++m) {  // the FP64 DFT's table: angle 2 pi m / L' in double
+        const double ang = 6.283185307179586476925286766559 * (double)m / (double)lv.Lnew;
+        lv.cs[m] = std::cos(ang);
+        lv.sn[m] = std::sin(ang);
+    }
+    return GP_OK;
+}
+
+// Device copies of a level's tables (context scratch ux[0..3]).
+int upload_level(gp_ctx* c, const Level& lv, LevelDev& d, cudaStream_t s) {
+    const int np = lv.np, NB = 2 * np;
+    std::vector<int> cnt(lv.nrows);
+    std::vector<int8_t> vals((size_t)lv.nrows * lv.dmax * lv.r, 0);
+    std::vector<float4> ct((size_t)lv.L * lv.nrows * lv.dmax * np, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<double2> ct64((size_t)lv.L * lv.nrows * lv.dmax * NB, make_double2(0.0, 0.0));
+    for (int row = 0; row < lv.nrows; ++row) {
+        cnt[row] = (int)lv.rowparts[row].size();
+        for (int d = 0; d < cnt[row]; ++d)
+            for (int q = 0; q < lv.r; ++q) vals[((size_t)row * lv.dmax + d) * lv.r + q] = (int8_t)lv.rowparts[row][d][q];
+    }
+    for (int i = 0; i < lv.L; ++i)
+        for (int row = 0; row < lv.nrows; ++row)
+            for (int d = 0; d < cnt[row]; ++d) {
+                const size_t at = ((size_t)i * lv.nrows + row) * lv.dmax + d;
+                for (int b = 0; b < lv.nb; ++b) {
+                    const int k = lv.bins[b];
+                    long double re = 0, im = 0;
+                    for (int q = 0; q < lv.r; ++q) {
+                        const int m = (int)(((long long)(i + lv.L * q) * k) % lv.Lnew);
+                        const long double ang = 6.283185307179586476925286766559L * (long double)m / (long double)lv.Lnew;
+                        re += (long double)lv.rowparts[row][d][q] * cosl(ang);
+                        im -= (long double)lv.rowparts[row][d][q] * sinl(ang);
+                    }
+                    ct64[at * NB + b] = make_double2((double)re, (double)im);
+                    float4& f = ct[at * np + b / 2];
+                    if (b & 1) {
+                        f.y = (float)re;
+                        f.w = (float)im;
+                    } else {
+                        f.x = (float)re;
+                        f.z = (float)im;
+                    }
+                }
+            }
+    DevBuf &dcnt = c->ux[0], &dvals = c->ux[1], &dct = c->ux[2], &dct64 = c->ux[3];
+    if (!dcnt.ensure(cnt.size() * 4) || !dvals.ensure(vals.size() + 16) || !dct.ensure(ct.size() * 16) ||
+        !dct64.ensure(ct64.size() * 16))
+        return c->fail(GP_ERR_NOMEM, "uncompress: level tables");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dcnt.p, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dvals.p, vals.data(), vals.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dct.p, ct.data(), ct.size() * 16, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dct64.p, ct64.data(), ct64.size() * 16, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));  // the host vectors go out of scope
+    d.L = lv.L;
+    d.r = lv.r;
+    d.Lnew = lv.Lnew;
+    d.H = lv.H;
+    d.nrows = lv.nrows;
+    d.dmax = lv.dmax;
+    d.np = np;
+    d.nb = lv.nb;
+    d.one_bit = lv.cn == 1 && lv.Lnew <= 64;
+    d.target = lv.paf * lv.cn;
+    d.cnt = dcnt.as<int>();
+    d.vals = dvals.as<int8_t>();
+    d.ctab = dct.as<float4>();
+    d.ctab64 = dct64.as<double2>();
+    return GP_OK;
+}
+
+// One side of a compressed pair, planned.
+struct Side {
+    std::vector<uint8_t> rows;  // row of each position
+    uint64_t total = 0;         // expansions (0: none can pass)
+    uint64_t prefix_count = 0;
+    uint32_t nsuf = 0;
+};
+
+// src/core/uncompression/uncompression.cpp:107-142: rotation, rows, sizes.
+int plan_side(gp_ctx* c, const Level& lv, std::vector<int> orig, Side& sd) {
+    const int L = lv.L;
+    for (int v : orig)
+        if (!lv.letter_index.count(v))
+            return c->fail(GP_ERR_FORMAT, "uncompress: value %d is not a letter of compression %d", v, lv.c);
     // first distinct element (ascending) with the most partitions
     std::set<int> distinct(orig.begin(), orig.end());
     size_t best_n = 0;
     int best = orig[0];
     for (int e : distinct) {
-        auto it = partitions.find(e);
-        const size_t n = it == partitions.end() ? 0 : it->second.size();
+        const size_t n = lv.rowparts[lv.letter_index.at(e)].size();
         if (n > best_n) {
             best_n = n;
             best = e;
         }
     }
     // rotate left by i whenever orig[i] == best, on the already rotated sequence
-    for (size_t i = 0; i < orig.size(); ++i)
+    for (int i = 0; i < L; ++i)
         if (orig[i] == best) std::rotate(orig.begin(), orig.begin() + i, orig.end());
-    // first entry: minima of each partition under rotation and reversal
-    std::set<std::vector<int>> first;
-    for (auto& perm : partitions[orig[0]]) {
-        std::vector<int> mn = perm;
-        for (int rev = 0; rev < 2; ++rev)
-            for (int s = 0; s < r; ++s) {
-                std::vector<int> cand(r);
-                for (int i = 0; i < r; ++i) {
-                    const int src = (i + s) % r;
-                    cand[i] = rev ? perm[r - 1 - src] : perm[src];
-                }
-                if (cand < mn) mn = cand;
-            }
-        first.insert(mn);
-    }
-    Expansion e;
-    const int L = (int)orig.size();
-    auto add = [&](const std::vector<std::vector<int>>& list) {
-        e.off.push_back((int)(e.vals.size() / r));
-        e.cnt.push_back((int)list.size());
-        for (auto& v : list)
-            for (int x : v) e.vals.push_back((int8_t)x);
-        const uint64_t c = list.size();
-        if (c == 0) {
-            e.total = 0;
-        } else if (e.total > (uint64_t(1) << 62) / c) {
-            e.overflow = true;
-        } else {
-            e.total *= c;
+    sd.rows.resize(L);
+    for (int i = 0; i < L; ++i) sd.rows[i] = (uint8_t)(lv.letter_index.at(orig[i]) + (i == 0 ? lv.A : 0));
+    // bins that are multiples of r equal the compressed sequence's DFT:
+    // the same for every expansion, checked here in FP64
+    for (int k : lv.cbins) {
+        double re = 0, im = 0;
+        for (int i = 0; i < L; ++i) {
+            const int m = (int)(((long long)i * k) % lv.Lnew);
+            re += orig[i] * lv.cs[m];
+            im -= orig[i] * lv.sn[m];
         }
-    };
-    add(std::vector<std::vector<int>>(first.begin(), first.end()));
-    for (int i = 1; i < L; ++i) add(partitions[orig[i]]);
-    return e;
+        if (re * re + im * im > lv.thr) {
+            sd.total = 0;
+            return GP_OK;
+        }
+    }
+    uint64_t total = 1;
+    std::vector<int> free_cnt;
+    for (int i = 0; i < L; ++i) {
+        const uint64_t n = lv.rowparts[sd.rows[i]].size();
+        if (n == 0) {
+            sd.total = 0;
+            return GP_OK;
+        }
+        if (total > (kRankMask >> 1) / n) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: more than 2^39 expansions of one side");
+        total *= n;
+        if (n > 1) free_cnt.push_back((int)n);
+    }
+    sd.total = total;
+    // suffix table: the trailing free positions whose combinations fit
+    uint32_t sc = 1, nsuf = 0;
+    for (int f = (int)free_cnt.size() - 1; f >= 0; --f) {
+        if ((uint64_t)sc * (uint64_t)free_cnt[f] > (uint64_t)lv.smax) break;
+        sc *= (uint32_t)free_cnt[f];
+        ++nsuf;
+    }
+    sd.nsuf = nsuf;
+    sd.prefix_count = total / sc;
+    return GP_OK;
 }
 
 void put_uint(std::string& s, unsigned v) {
@@ -200,221 +801,52 @@ void put_uint(std::string& s, unsigned v) {
     while (n) s.push_back(tmp[--n]);
 }
 
-// Device records of one side: packed words and signatures.
-struct Side {
-    DevBuf words, sig;
-    int64_t n = 0, cap = 0;
-    unsigned long long* nrec = nullptr;  // pinned: record count, copied back by the expansion's stream
-    bool pending = false;                // enqueued, count not read yet
-};
-
-__global__ void gather_records_kernel(const uint4* words, const uint16_t* sig, int S, const uint32_t* rows, int64_t n,
-                                      uint4* ow, uint16_t* os) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t r = rows[i];
-        ow[i] = words[r];
-        for (int k = 0; k < S; ++k) os[i * S + k] = sig[(int64_t)r * S + k];
+void put_int(std::string& s, int v) {
+    if (v < 0) {
+        s.push_back('-');
+        put_uint(s, (unsigned)(-v));
+    } else {
+        put_uint(s, (unsigned)v);
     }
 }
 
-// Enqueues on stream s the expansion of one compressed sequence, keeping in
-// `side` every expansion that passes the PSD filter, with its signature
-// (uncompression.cpp:195-207; invert selects bound - rint(psd)).  Device
-// scratch: the nine context buffers from c->ux[slot].  finish_side reads the
-// record count once the stream is done.
-int expand_side(gp_ctx* c, std::vector<int> orig, int order, int compress, int new_compress, int paf, bool invert,
-                Side& side, int64_t* n_exp, cudaStream_t s, int slot) {
-    const int L = (int)orig.size();
-    Expansion e = plan_expansion(orig, compress, new_compress);
-    if (e.overflow) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: more than 2^62 expansions");
-    const int r = compress / new_compress;
-    const int Lnew = L * r;
-    const std::vector<int> nalpha = gp::alphabet(new_compress);
-    const int b = gp::bits_for((int)nalpha.size());
-    if (L > kMaxPos || b * Lnew > 128 || !gp::tc_packed_supported(Lnew, b))
-        return c->fail(GP_ERR_UNSUPPORTED, "uncompress: length %d over %d letters", Lnew, (int)nalpha.size());
-    *n_exp += (int64_t)e.total;
-    side.n = 0;
-    side.pending = false;
-    if (e.total == 0) return GP_OK;
-    DevBuf* ux = c->ux + slot;
-    DevBuf &dcnt = ux[0], &doff = ux[1], &dvals = ux[2], &dwords = ux[3], &dmask = ux[4], &dunsure = ux[5],
-           &didx = ux[6], &dmisc = ux[7], &dinv = ux[8];
-    const int64_t chunk = (int64_t)std::min<uint64_t>(e.total, uint64_t(1) << 24);
-    if (!dcnt.ensure(L * 4) || !doff.ensure(L * 4) || !dvals.ensure(e.vals.size() + 16) || !dwords.ensure(chunk * 16) ||
-        !dmask.ensure((chunk + 31) / 32 * 4) || !dunsure.ensure(chunk * 4) || !didx.ensure(chunk * 4) ||
-        !dmisc.ensure(64))
-        return c->fail(GP_ERR_NOMEM, "uncompress: device allocation");
-    // record arena: every expansion could pass; capped at 2^26 records
-    side.cap = (int64_t)std::min<uint64_t>(e.total, uint64_t(1) << 26);
-    if (!side.words.ensure((size_t)side.cap * 16) || !side.sig.ensure((size_t)side.cap * 2 * (Lnew - 1) + 16))
-        return c->fail(GP_ERR_NOMEM, "uncompress: record arena");
-    // exact for offsets below 2^24 while every count is at most 2^16
-    for (int i = 0; i < L; ++i)
-        if (e.cnt[i] > (1 << 16)) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %d choices for one entry", e.cnt[i]);
-    std::vector<uint64_t> inv(L);
-    for (int i = 0; i < L; ++i) inv[i] = ((uint64_t(1) << 40) + (uint64_t)e.cnt[i] - 1) / (uint64_t)e.cnt[i];
-    if (!dinv.ensure(L * 8)) return c->fail(GP_ERR_NOMEM, "uncompress: device allocation");
-    GP_CUDA_TRY(c, cudaMemcpyAsync(dinv.p, inv.data(), L * 8, cudaMemcpyHostToDevice, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(dcnt.p, e.cnt.data(), L * 4, cudaMemcpyHostToDevice, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(doff.p, e.off.data(), L * 4, cudaMemcpyHostToDevice, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(dvals.p, e.vals.data(), e.vals.size(), cudaMemcpyHostToDevice, s));
-    unsigned long long* misc = dmisc.as<unsigned long long>();  // [0] unsure [1] survivors [2] records [3] passes
-    GP_CUDA_TRY(c, cudaMemsetAsync(misc, 0, 64, s));
-    const gp::RowSrc src{nullptr, dwords.as<uint4>(), Lnew, b, new_compress};
-    const double* tw = c->twiddle64(Lnew);
-    if (!tw) return c->fail(GP_ERR_NOMEM, "twiddles");
-    for (uint64_t r0 = 0; r0 < e.total; r0 += (uint64_t)chunk) {
-        const int64_t n = (int64_t)std::min<uint64_t>((uint64_t)chunk, e.total - r0);
-        ExpandArgs ea{};
-        ea.L = L;
-        ea.r = r;
-        ea.Lnew = Lnew;
-        ea.b = b;
-        ea.cnew = new_compress;
-        ea.rank0 = r0;
-        ea.n = n;
-        {
-            uint64_t q = r0;  // digits of r0, position L-1 least significant
-            for (int i = L - 1; i >= 0; --i) {
-                ea.d0[i] = (int)(q % (uint64_t)e.cnt[i]);
-                q /= (uint64_t)e.cnt[i];
-            }
+// The expansion of a survivor word, on the host.
+void host_expand(const Level& lv, const Side& sd, uint64_t rank, std::vector<int>& x) {
+    std::vector<int> d(lv.L, 0);
+    for (int i = lv.L - 1; i >= 0; --i) {
+        const uint64_t c = lv.rowparts[sd.rows[i]].size();
+        d[i] = (int)(rank % c);
+        rank /= c;
+    }
+    x.assign(lv.Lnew, 0);
+    for (int i = 0; i < lv.L; ++i)
+        for (int q = 0; q < lv.r; ++q) x[i + lv.L * q] = lv.rowparts[sd.rows[i]][d[i]][q];
+}
+
+// "PSD" + signature + " " + sequence (src/utils/io.cpp:14-36; the a-side
+// writes bound - rint(psd)), the line the reference's scratch files hold.
+void candidate_line(const Level& lv, const std::vector<int>& x, bool invert, std::string& line, std::string& seq) {
+    const int N = lv.Lnew, bound = 2 * lv.order - lv.paf;
+    line = "PSD";
+    for (int k = 1; k < N; ++k) {
+        double re = 0, im = 0;
+        for (int j = 0, m = 0; j < N; ++j, m += k, m -= m >= N ? N : 0) {
+            re += x[j] * lv.cs[m];
+            im -= x[j] * lv.sn[m];
         }
-        ea.inv = dinv.as<uint64_t>();
-        ea.cnt = dcnt.as<int>();
-        ea.off = doff.as<int>();
-        ea.vals = dvals.as<int8_t>();
-        ea.words = dwords.as<uint4>();
-        int64_t blocks = (n + 255) / 256;
-        if (blocks > (int64_t)c->num_sms * 16) blocks = (int64_t)c->num_sms * 16;
-        expand_kernel<<<(unsigned)blocks, 256, 0, s>>>(ea);
-        GP_CUDA_TRY(c, cudaGetLastError());
-        GP_CUDA_TRY(c, cudaMemsetAsync(misc + 1, 0, 8, s));
-        int rc = c->enqueue_filter(src, n, order, paf, GP_PSD_TC_GUARDED, dmask.as<uint32_t>(), dunsure.as<uint32_t>(),
-                                   misc + 0, s);
-        if (rc) return rc;
-        GP_CUDA_TRY(c, gp::launch_mask_to_list(dmask.as<uint32_t>(), n, didx.as<uint32_t>(), misc + 1, n,
-                                               c->status.as<int>(), c->num_sms, s));
-        gp::FinalizeArgs fa;
-        fa.src = src;
-        fa.roles = nullptr;
-        fa.fixed_role = 1;
-        fa.idx = didx.as<uint32_t>();
-        fa.n_idx = misc + 1;
-        fa.idx_cap = n;
-        fa.tw = tw;
-        fa.thr = 2.0 * order - paf + 0.001;
-        fa.bound = 2 * order - paf;
-        fa.invert_roles = invert ? 1 : 0;
-        fa.check_canonical = 0;
-        fa.units = nullptr;
-        fa.n_units = 0;
-        fa.rec_words = side.words.as<uint4>();
-        fa.rec_role = nullptr;
-        fa.rec_sig = side.sig.as<uint16_t>();
-        fa.rec_src = nullptr;
-        fa.rec_count = misc + 2;  // accumulates over chunks
-        fa.rec_cap = side.cap;
-        fa.psd_pass = misc + 3;
-        fa.status = c->status.as<int>();
-        GP_CUDA_TRY(c, gp::launch_finalize(fa, n, c->num_sms, s));
+        const int p = (int)std::nearbyint(re * re + im * im);
+        put_int(line, invert ? bound - p : p);
     }
-    GP_CUDA_TRY(c, cudaMemcpyAsync(side.nrec, misc + 2, 8, cudaMemcpyDeviceToHost, s));
-    side.pending = true;
-    return GP_OK;
+    seq.clear();
+    for (int v : x) {
+        put_int(seq, v);
+        seq.push_back(' ');
+    }
+    line.push_back(' ');
+    line += seq;
 }
 
-// Waits for a side's expansion on stream s and takes its record count.
-int finish_side(gp_ctx* c, Side& side, cudaStream_t s) {
-    if (!side.pending) return GP_OK;
-    side.pending = false;
-    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
-    int rc = c->check_status("uncompress");
-    if (rc) return rc;
-    side.n = (int64_t)std::min<unsigned long long>(*side.nrec, (unsigned long long)side.cap);
-    return GP_OK;
-}
-
-void put_seq(std::string& t, const std::vector<int>& alpha, gp::u128 word, int b, int L) {
-    for (int j = 0; j < L; ++j) {
-        const int v = alpha[gp::word_digit_h(word, b, L, j)];
-        if (v < 0) {
-            t.push_back('-');
-            put_uint(t, (unsigned)(-v));
-        } else {
-            put_uint(t, (unsigned)v);
-        }
-        t.push_back(' ');
-    }
-}
-
-// Joins the two sides and appends the matched pairs, in the reference's
-// order, to `out`.
-int join_sides(gp_ctx* c, Side& A, Side& B, int Lnew, int new_compress, int paf, std::string& out) {
-    const std::vector<int> nalpha = gp::alphabet(new_compress);
-    const int b = gp::bits_for((int)nalpha.size());
-    std::vector<std::pair<uint32_t, uint32_t>> m;
-    int rc = gp::device_join(c, gp::JoinSide{A.words.as<uint4>(), A.sig.as<uint16_t>(), A.n},
-                             gp::JoinSide{B.words.as<uint4>(), B.sig.as<uint16_t>(), B.n}, Lnew, b, new_compress,
-                             paf * new_compress, m);
-    if (rc || m.empty()) return rc;
-    const int S = Lnew - 1;
-    const int64_t nm = (int64_t)m.size();
-    std::vector<uint32_t> ra(nm), rb(nm);
-    for (int64_t i = 0; i < nm; ++i) {
-        ra[i] = m[i].first;
-        rb[i] = m[i].second;
-    }
-    cudaStream_t s = c->s_comp;
-    DevBuf &dra = c->ux[8], &drb = c->ux[9], &wa = c->ux[10], &wb = c->ux[11], &sa = c->ux[12], &sb = c->ux[13];
-    if (!dra.ensure(nm * 4) || !drb.ensure(nm * 4) || !wa.ensure(nm * 16) || !wb.ensure(nm * 16) ||
-        !sa.ensure(nm * S * 2 + 16) || !sb.ensure(nm * S * 2 + 16))
-        return c->fail(GP_ERR_NOMEM, "uncompress: gather");
-    GP_CUDA_TRY(c, cudaMemcpyAsync(dra.p, ra.data(), nm * 4, cudaMemcpyHostToDevice, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(drb.p, rb.data(), nm * 4, cudaMemcpyHostToDevice, s));
-    const unsigned g = (unsigned)std::min<int64_t>((nm + 255) / 256, 4096);
-    gather_records_kernel<<<g, 256, 0, s>>>(A.words.as<uint4>(), A.sig.as<uint16_t>(), S, dra.as<uint32_t>(), nm,
-                                            wa.as<uint4>(), sa.as<uint16_t>());
-    gather_records_kernel<<<g, 256, 0, s>>>(B.words.as<uint4>(), B.sig.as<uint16_t>(), S, drb.as<uint32_t>(), nm,
-                                            wb.as<uint4>(), sb.as<uint16_t>());
-    GP_CUDA_TRY(c, cudaGetLastError());
-    std::vector<uint4> hwa(nm), hwb(nm);
-    std::vector<uint16_t> hsa((size_t)nm * S), hsb((size_t)nm * S);
-    GP_CUDA_TRY(c, cudaMemcpyAsync(hwa.data(), wa.p, nm * 16, cudaMemcpyDeviceToHost, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(hwb.data(), wb.p, nm * 16, cudaMemcpyDeviceToHost, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(hsa.data(), sa.p, hsa.size() * 2, cudaMemcpyDeviceToHost, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(hsb.data(), sb.p, hsb.size() * 2, cudaMemcpyDeviceToHost, s));
-    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
-    auto word_of = [](const uint4& w) {
-        return ((gp::u128)w.w << 96) | ((gp::u128)w.z << 64) | ((gp::u128)w.y << 32) | w.x;
-    };
-    struct Item {
-        std::string a_line, b_line, pair_line;
-    };
-    std::vector<Item> items(nm);
-    for (int64_t i = 0; i < nm; ++i) {
-        Item& it = items[i];
-        const gp::u128 x = word_of(hwa[i]), y = word_of(hwb[i]);
-        std::string sa_txt, sb_txt;
-        put_seq(sa_txt, nalpha, x, b, Lnew);
-        put_seq(sb_txt, nalpha, y, b, Lnew);
-        it.a_line = "PSD";
-        for (int k = 0; k < S; ++k) put_uint(it.a_line, hsa[i * S + k]);
-        it.a_line.push_back(' ');
-        it.a_line += sa_txt;
-        it.b_line = "PSD";
-        for (int k = 0; k < S; ++k) put_uint(it.b_line, hsb[i * S + k]);
-        it.b_line.push_back(' ');
-        it.b_line += sb_txt;
-        it.pair_line = sa_txt + " " + sb_txt + "\n";
-    }
-    std::sort(items.begin(), items.end(), [](const Item& p, const Item& q) {
-        return p.a_line != q.a_line ? p.a_line < q.a_line : p.b_line < q.b_line;
-    });
-    for (auto& it : items) out += it.pair_line;
-    return GP_OK;
-}
+std::string signature_token(const std::string& line) { return line.substr(0, line.find(' ')); }
 
 bool slurp(const char* path, std::string& out) {
     FILE* f = fopen(path, "rb");
@@ -427,6 +859,240 @@ bool slurp(const char* path, std::string& out) {
     fclose(f);
     out.resize(got);
     return true;
+}
+
+using ScanKernel = void (*)(ScanArgs);
+
+ScanKernel scan_kernel_for(int np) {
+    switch (np) {
+        case 2: return ux_scan_kernel<2>;
+        case 4: return ux_scan_kernel<4>;
+        case 6: return ux_scan_kernel<6>;
+        case 8: return ux_scan_kernel<8>;
+        case 10: return ux_scan_kernel<10>;
+        case 12: return ux_scan_kernel<12>;
+        case 16: return ux_scan_kernel<16>;
+        case 24: return ux_scan_kernel<24>;
+        case 32: return ux_scan_kernel<32>;
+    }
+    return nullptr;
+}
+
+unsigned grid_for(uint64_t n, unsigned cap) {
+    uint64_t g = (n + 255) / 256;
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(g, cap));
+}
+
+// The engine over consecutive pairs [p0, p1): device scratch in ux[4..].
+struct Batcher {
+    gp_ctx* c;
+    const Level& lv;
+    const LevelDev& ld;
+    const std::vector<Side>& sides;  // 2 per pair: a, b
+    cudaStream_t s;
+    ScanKernel scan;
+    int scan_blocks = 0;
+    size_t smem = 0;
+    // matched (a line, b line, pair line) per pair of the batch
+    std::vector<std::vector<std::array<std::string, 3>>> out;
+
+    // Runs the batch; on overflow of a device list returns GP_ERR_OVERFLOW
+    // with *split_hint set, so the caller can halve the batch.
+    int run(int64_t p0, int64_t p1, bool* overflowed);
+};
+
+int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
+    *overflowed = false;
+    const int L = lv.L;
+    const int64_t np_ = p1 - p0, ns = 2 * np_;
+    std::vector<uint8_t> rows((size_t)ns * L);
+    std::vector<uint64_t> ubeg(ns + 1), pcnt(ns);
+    std::vector<uint32_t> nsuf(ns);
+    uint64_t units = 0, total = 0;
+    for (int64_t k = 0; k < ns; ++k) {
+        const Side& sd = sides[2 * p0 + k];
+        memcpy(&rows[(size_t)k * L], sd.rows.data(), L);
+        ubeg[k] = units;
+        pcnt[k] = sd.total ? sd.prefix_count : 0;
+        nsuf[k] = sd.nsuf;
+        if (sd.total) {
+            units += (sd.prefix_count + kScanThreads - 1) / kScanThreads;
+            total += sd.total;
+        }
+    }
+    ubeg[ns] = units;
+    out.assign(np_, {});
+    if (units == 0) return GP_OK;
+    // capacities: every expansion could pass at small sizes; at large ones
+    // a pass rate of 1/8 (order 57: under 1 %); unsure 1/64 of that
+    const uint64_t surv_cap = std::max<uint64_t>(1024, std::min<uint64_t>(total, std::max<uint64_t>(total / 8, 1 << 20)));
+    const uint64_t unsure_cap = std::max<uint64_t>(1024, surv_cap / 64);
+    DevBuf &drows = c->ux[4], &dubeg = c->ux[5], &dpcnt = c->ux[6], &dnsuf = c->ux[7], &dcnt = c->ux[8],
+           &dsurv = c->ux[9], &duns = c->ux[10], &dside = c->ux[11];
+    if (!drows.ensure(rows.size()) || !dubeg.ensure(ubeg.size() * 8) || !dpcnt.ensure(pcnt.size() * 8) ||
+        !dnsuf.ensure(nsuf.size() * 4) || !dcnt.ensure(64) || !dsurv.ensure(surv_cap * 8) ||
+        !duns.ensure(unsure_cap * 8) || !dside.ensure((size_t)ns * 4))
+        return c->fail(GP_ERR_NOMEM, "uncompress: batch buffers");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(drows.p, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dubeg.p, ubeg.data(), ubeg.size() * 8, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dpcnt.p, pcnt.data(), pcnt.size() * 8, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dnsuf.p, nsuf.data(), nsuf.size() * 4, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemsetAsync(dcnt.p, 0, 64, s));
+    GP_CUDA_TRY(c, cudaMemsetAsync(dside.p, 0, (size_t)ns * 4, s));
+    unsigned long long* counters = dcnt.as<unsigned long long>();
+    LevelDev d = ld;
+    d.side_rows = drows.as<uint8_t>();
+    ScanArgs sa{};
+    sa.lv = d;
+    sa.unit_begin = dubeg.as<uint64_t>();
+    sa.prefix_count = dpcnt.as<uint64_t>();
+    sa.nsuf = dnsuf.as<uint32_t>();
+    sa.n_sides = (int)ns;
+    sa.n_units = units;
+    sa.thr_lo = lv.thr_lo;
+    sa.thr_hi = lv.thr_hi;
+    sa.surv = dsurv.as<uint64_t>();
+    sa.surv_cap = surv_cap;
+    sa.unsure = duns.as<uint64_t>();
+    sa.unsure_cap = unsure_cap;
+    sa.counters = counters;
+    sa.side_count = dside.as<uint32_t>();
+    sa.status = c->status.as<int>();
+    const unsigned sgrid = (unsigned)std::min<uint64_t>(units, (uint64_t)scan_blocks);
+    scan<<<sgrid, kScanThreads, smem, s>>>(sa);
+    GP_CUDA_TRY(c, cudaGetLastError());
+    RecheckArgs ra{};
+    ra.lv = d;
+    ra.thr = lv.thr;
+    ra.unsure = sa.unsure;
+    ra.unsure_cap = unsure_cap;
+    ra.surv = sa.surv;
+    ra.surv_cap = surv_cap;
+    ra.counters = counters;
+    ra.side_count = sa.side_count;
+    ra.status = sa.status;
+    ux_recheck_kernel<<<(unsigned)c->num_sms * 8, kRecheckWarps * 32, 0, s>>>(ra);
+    GP_CUDA_TRY(c, cudaGetLastError());
+    std::vector<unsigned long long> hc(8);
+    std::vector<uint32_t> side_count(ns);
+    GP_CUDA_TRY(c, cudaMemcpyAsync(hc.data(), counters, 64, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(side_count.data(), sa.side_count, (size_t)ns * 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    if (hc[0] > surv_cap || hc[1] > unsure_cap) {
+        cudaMemset(c->status.p, 0, sizeof(int));
+        *overflowed = true;
+        return GP_ERR_OVERFLOW;
+    }
+    int rc = c->check_status("uncompress");
+    if (rc) return rc;
+    const uint64_t nsurv = hc[0];
+    // buckets: a pair with no survivor on one side cannot match
+    std::vector<uint8_t> lg(np_, 255);
+    std::vector<uint32_t> pbase(np_, 0);
+    uint64_t nbk = 0;
+    for (int64_t p = 0; p < np_; ++p) {
+        const uint64_t na = side_count[2 * p], nbb = side_count[2 * p + 1];
+        if (!na || !nbb) continue;
+        int l = 0;
+        while (((uint64_t)kBucketTarget << l) < na + nbb && l < 30) ++l;
+        lg[p] = (uint8_t)l;
+        pbase[p] = (uint32_t)nbk;
+        nbk += uint64_t(1) << l;
+    }
+    if (nbk == 0 || nsurv == 0) return GP_OK;
+    if (nbk >= (uint64_t(1) << 31)) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %llu join buckets", (unsigned long long)nbk);
+    DevBuf &dlg = c->ux[12], &dpb = c->ux[13], &dkeys = c->ux[14], &dbkt = c->ux[15], &dbc = c->ux[16],
+           &dbo = c->ux[17], &dbcur = c->ux[18], &dscan = c->ux[19], &deh = c->ux[20], &dei = c->ux[21],
+           &dm = c->ux[22];
+    const uint64_t match_cap = std::max<uint64_t>(1 << 16, nsurv / 16);
+    if (!dlg.ensure(np_) || !dpb.ensure((size_t)np_ * 4) || !dkeys.ensure(nsurv * 8) || !dbkt.ensure(nsurv * 4) ||
+        !dbc.ensure(nbk * 4) || !dbo.ensure(nbk * 4 + 4) || !dbcur.ensure(nbk * 4) ||
+        !dscan.ensure(gp::scan_tmp_bytes((int64_t)nbk)) || !deh.ensure(nsurv * 8) || !dei.ensure(nsurv * 4) ||
+        !dm.ensure(match_cap * 16))
+        return c->fail(GP_ERR_NOMEM, "uncompress: join buffers");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dlg.p, lg.data(), np_, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dpb.p, pbase.data(), (size_t)np_ * 4, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemsetAsync(dbc.p, 0, nbk * 4, s));
+    GP_CUDA_TRY(c, cudaMemsetAsync(dbcur.p, 0, nbk * 4, s));
+    KeyArgs ka{};
+    ka.lv = d;
+    ka.surv = sa.surv;
+    ka.n = nsurv;
+    ka.pair_lg = dlg.as<uint8_t>();
+    ka.pair_base = dpb.as<uint32_t>();
+    ka.keys = dkeys.as<uint64_t>();
+    ka.bucket = dbkt.as<uint32_t>();
+    ka.bcount = dbc.as<uint32_t>();
+    ux_key_kernel<<<grid_for(nsurv, (unsigned)c->num_sms * 16), 256, 0, s>>>(ka);
+    GP_CUDA_TRY(c, cudaGetLastError());
+    GP_CUDA_TRY(c, gp::exclusive_scan_u32(dbc.as<uint32_t>(), dbo.as<uint32_t>(), (int64_t)nbk, dscan.as<uint32_t>(), s));
+    ux_scatter_kernel<<<grid_for(nsurv, (unsigned)c->num_sms * 16), 256, 0, s>>>(
+        sa.surv, ka.keys, ka.bucket, nsurv, dbo.as<uint32_t>(), dbcur.as<uint32_t>(), deh.as<uint64_t>(),
+        dei.as<uint32_t>());
+    GP_CUDA_TRY(c, cudaGetLastError());
+    JoinArgs ja{};
+    ja.lv = d;
+    ja.surv = sa.surv;
+    ja.ent_h = deh.as<uint64_t>();
+    ja.ent_i = dei.as<uint32_t>();
+    ja.boff = dbo.as<uint32_t>();
+    ja.bcount = dbc.as<uint32_t>();
+    ja.n_buckets = (uint32_t)nbk;
+    ja.matches = dm.as<uint64_t>();
+    ja.match_cap = match_cap;
+    ja.counters = counters;
+    ja.status = sa.status;
+    ux_join_kernel<<<(unsigned)std::min<uint64_t>(nbk, (uint64_t)c->num_sms * 8), 256, 0, s>>>(ja);
+    GP_CUDA_TRY(c, cudaGetLastError());
+    GP_CUDA_TRY(c, cudaMemcpyAsync(hc.data(), counters, 64, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    if (hc[2] > match_cap) {
+        cudaMemset(c->status.p, 0, sizeof(int));
+        *overflowed = true;
+        return GP_ERR_OVERFLOW;
+    }
+    rc = c->check_status("uncompress join");
+    if (rc) return rc;
+    const uint64_t nm = hc[2];
+    if (nm == 0) return GP_OK;
+    std::vector<uint64_t> hm(nm * 2);
+    GP_CUDA_TRY(c, cudaMemcpy(hm.data(), dm.p, nm * 16, cudaMemcpyDeviceToHost));
+    // signatures of the matched expansions; the reference joins on the
+    // signature string, which the PAF condition implies up to FP64 rounding
+    std::vector<std::array<std::string, 3>> items(nm);
+    std::vector<char> keep(nm, 0);
+    std::vector<int64_t> pair_of(nm);
+    auto work = [&](uint64_t lo, uint64_t hi) {
+        std::vector<int> xa, xb;
+        std::string la, sa_, lb, sb_;
+        for (uint64_t m = lo; m < hi; ++m) {
+            const uint64_t va = hm[2 * m], vb = hm[2 * m + 1];
+            const int64_t side_a = (int64_t)(va >> kRankBits), side_b = (int64_t)(vb >> kRankBits);
+            host_expand(lv, sides[2 * p0 + side_a], va & kRankMask, xa);
+            host_expand(lv, sides[2 * p0 + side_b], vb & kRankMask, xb);
+            candidate_line(lv, xa, true, la, sa_);
+            candidate_line(lv, xb, false, lb, sb_);
+            pair_of[m] = side_a >> 1;
+            if (signature_token(la) != signature_token(lb)) continue;
+            keep[m] = 1;
+            items[m] = {la, lb, sa_ + " " + sb_ + "\n"};
+        }
+    };
+    const unsigned nt = (unsigned)std::min<uint64_t>(16, (nm + 63) / 64);
+    if (nt <= 1) {
+        work(0, nm);
+    } else {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; ++t) th.emplace_back(work, nm * t / nt, nm * (t + 1) / nt);
+        for (auto& t : th) t.join();
+    }
+    for (uint64_t m = 0; m < nm; ++m)
+        if (keep[m]) out[pair_of[m]].push_back(std::move(items[m]));
+    for (auto& v : out)
+        std::sort(v.begin(), v.end(), [](const std::array<std::string, 3>& p, const std::array<std::string, 3>& q) {
+            return p[0] != q[0] ? p[0] < q[0] : p[1] < q[1];
+        });
+    return GP_OK;
 }
 
 }  // namespace
@@ -449,8 +1115,6 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
     (void)work_dir;
     (void)prefix;
     cudaSetDevice(c->device);
-    if (!c->ensure_job_streams() || !c->h_ux.ensure(64))
-        return c->fail(GP_ERR_CUDA, "uncompress: streams / pinned counts");
     // the reference constructs its PairReader / PairWriter before the
     // pipeline runs (src/main.cpp:122-123): the output is truncated even
     // when nothing is uncompressed
@@ -469,93 +1133,118 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
         fclose(out);
         return GP_OK;  // an unreadable input yields no pairs (the reader is simply not good)
     }
-    const int L = order / compress;
-    const char* p = text.data();
-    const char* end = p + text.size();
-    long line_no = 0;
-    int rc = GP_OK;
-    // Pairs alternate between two sets of sides, scratch and streams: pair
-    // i+1 expands on the device while pair i is joined and formatted.  The
-    // join leaves no device work behind, so a set is free again once its
-    // pair is written; output stays in input-pair order.
-    struct PairSet {
-        Side a, b;
-        cudaStream_t sa, sb;
-        bool busy = false;
-    };
-    PairSet set[2];
-    for (int k = 0; k < 2; ++k) {
-        set[k].sa = c->s_jobs[2 * k];
-        set[k].sb = c->s_jobs[2 * k + 1];
-        set[k].a.nrec = c->h_ux.as<unsigned long long>() + 2 * k;
-        set[k].b.nrec = c->h_ux.as<unsigned long long>() + 2 * k + 1;
+    Level lv;
+    int rc = build_level(c, lv, order, compress, new_compress, paf);
+    if (rc) {
+        fclose(out);
+        return rc;
     }
-    auto retire = [&](PairSet& ps) -> int {
-        if (!ps.busy) return GP_OK;
-        ps.busy = false;
-        int r = finish_side(c, ps.a, ps.sa);
-        if (r) return r;
-        r = finish_side(c, ps.b, ps.sb);
-        if (r) return r;
-        std::string pairs;
-        r = join_sides(c, ps.a, ps.b, order / new_compress, new_compress, paf, pairs);
-        if (!r && !pairs.empty()) fwrite(pairs.data(), 1, pairs.size(), out);
-        return r;
-    };
-    int cur = 0;
-    while (p < end && rc == GP_OK) {
-        const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
-        if (!nl) nl = end;
-        // lines outside [first, end_line) or off the step are left out
-        const int64_t this_line = line_no;
-        if (this_line < first || this_line >= end_line || (this_line - first) % step != 0) {
-            ++line_no;
+    const int L = lv.L;
+    // parse the selected lines; io.cpp:52-55: a line of the wrong length is
+    // an error, the pairs before it are still written
+    std::vector<Side> sides;
+    int format_rc = GP_OK;
+    {
+        const char* p = text.data();
+        const char* end = p + text.size();
+        int64_t line_no = 0;
+        std::vector<int> vals;
+        while (p < end) {
+            const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
+            if (!nl) nl = end;
+            const int64_t this_line = line_no;
+            if (this_line < first || this_line >= end_line || (this_line - first) % step != 0) {
+                ++line_no;
+                p = nl + 1;
+                if (this_line >= end_line) break;
+                continue;
+            }
+            vals.clear();
+            const char* q = p;
+            while (q < nl) {
+                while (q < nl && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
+                if (q >= nl) break;
+                char* e2;
+                const long v = strtol(q, &e2, 10);
+                if (e2 == q) break;
+                vals.push_back((int)v);
+                q = e2;
+            }
             p = nl + 1;
-            if (this_line >= end_line) break;
+            if ((int)vals.size() != 2 * L) {
+                format_rc = c->fail(GP_ERR_FORMAT, "PairReader: input line %lld: length is %zu. Expected %d",
+                                    (long long)line_no, vals.size(), 2 * L);
+                break;
+            }
+            ++line_no;
+            for (int h = 0; h < 2; ++h) {
+                Side sd;
+                rc = plan_side(c, lv, std::vector<int>(vals.begin() + h * L, vals.begin() + (h + 1) * L), sd);
+                if (rc) break;
+                sides.push_back(std::move(sd));
+            }
+            if (rc) break;
+        }
+    }
+    if (rc) {
+        fclose(out);
+        return rc;
+    }
+    const int64_t npairs = (int64_t)sides.size() / 2;
+    cudaStream_t s = c->s_comp;
+    LevelDev ld{};
+    if (npairs) rc = upload_level(c, lv, ld, s);
+    Batcher bt{c, lv, ld, sides, s, scan_kernel_for(lv.np)};
+    if (!rc && npairs) {
+        const size_t ctab_bytes = (size_t)lv.L * lv.dmax * lv.np * 16;
+        bt.smem = (size_t)lv.smax * lv.np * 16 + ctab_bytes;
+        cudaError_t e = cudaFuncSetAttribute(bt.scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt.smem);
+        int per_sm = 0;
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bt.scan, kScanThreads, bt.smem);
+        if (e != cudaSuccess || per_sm < 1)
+            rc = c->fail(GP_ERR_CUDA, "uncompress: scan kernel occupancy (%s)", cudaGetErrorString(e));
+        bt.scan_blocks = c->num_sms * std::max(1, per_sm);
+    }
+    // batches of consecutive pairs, by expansions; a batch whose device
+    // lists overflow is split in half and run again
+    constexpr uint64_t kBatchExpansions = uint64_t(1) << 35;
+    std::vector<std::pair<int64_t, int64_t>> todo;
+    for (int64_t p = 0; p < npairs && !rc;) {
+        int64_t q = p;
+        uint64_t tot = 0;
+        while (q < npairs && (q == p || (tot + sides[2 * q].total + sides[2 * q + 1].total <= kBatchExpansions &&
+                                         q - p < kMaxSidesPerBatch / 2))) {
+            tot += sides[2 * q].total + sides[2 * q + 1].total;
+            ++q;
+        }
+        todo.emplace_back(p, q);
+        p = q;
+    }
+    std::reverse(todo.begin(), todo.end());
+    std::string buf;
+    while (!rc && !todo.empty()) {
+        const auto [p0, p1] = todo.back();
+        todo.pop_back();
+        bool over = false;
+        rc = bt.run(p0, p1, &over);
+        if (rc == GP_ERR_OVERFLOW && over && p1 - p0 > 1) {
+            const int64_t mid = p0 + (p1 - p0) / 2;
+            todo.emplace_back(mid, p1);
+            todo.emplace_back(p0, mid);
+            rc = GP_OK;
             continue;
         }
-        std::vector<int> vals;
-        std::string line(p, nl);
-        const char* q = line.c_str();
-        while (*q) {
-            while (*q == ' ' || *q == '\t' || *q == '\r') ++q;
-            if (!*q) break;
-            char* e2;
-            const long v = strtol(q, &e2, 10);
-            if (e2 == q) break;
-            vals.push_back((int)v);
-            q = e2;
-        }
-        p = nl + 1;
-        // io.cpp:52-55: a line of the wrong length is an error (the pairs
-        // before it are still written)
-        if ((int)vals.size() != 2 * L) {
-            rc = retire(set[cur ^ 1]);
-            if (!rc)
-                rc = c->fail(GP_ERR_FORMAT, "PairReader: input line %ld: length is %zu. Expected %d", line_no,
-                             vals.size(), 2 * L);
-            break;
-        }
-        ++line_no;
-        std::vector<int> a(vals.begin(), vals.begin() + L), b(vals.begin() + L, vals.end());
-        int64_t na = 0, nb = 0;
-        PairSet& ps = set[cur];
-        ps.busy = true;
-        // the two sides expand on two streams, each with its own scratch
-        rc = expand_side(c, a, order, compress, new_compress, paf, true, ps.a, &na, ps.sa, kSlotA[cur]);
+        if (rc == GP_ERR_OVERFLOW && over) rc = c->fail(GP_ERR_OVERFLOW, "uncompress: one pair overflows the device lists");
         if (rc) break;
-        rc = expand_side(c, b, order, compress, new_compress, paf, false, ps.b, &nb, ps.sb, kSlotB[cur]);
-        if (rc) break;
-        rc = retire(set[cur ^ 1]);  // the previous pair, while this one expands
-        cur ^= 1;
+        buf.clear();
+        for (auto& v : bt.out)
+            for (auto& it : v) buf += it[2];
+        if (!buf.empty()) fwrite(buf.data(), 1, buf.size(), out);
     }
-    if (rc == GP_OK) rc = retire(set[cur ^ 1]);
-    for (auto& ps : set) {  // nothing of this call stays in flight, also after an error
-        cudaStreamSynchronize(ps.sa);
-        cudaStreamSynchronize(ps.sb);
-    }
+    cudaStreamSynchronize(s);
     fclose(out);
-    return rc;
+    return rc ? rc : format_rc;
 }
 
 }  // extern "C"

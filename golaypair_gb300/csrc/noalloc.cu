@@ -16,13 +16,16 @@
 //   * Batches are limited to kNoAllocMaxRows rows (the unsure list must be
 //     able to hold every row); larger n is rejected with GP_ERR_ARG.
 //   * The first call on a device looks up the array's device address there
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
+//     (cudaGetSymbolAddress) with that device current and keeps it for the
+//     life of the process; make that first call before any stream capture.
+//     A device reset (cudaDeviceReset) invalidates the kept address: do not
+//     call the entry point on that device again in the same process.
 //   * Every call shares the array and it keeps the last call's contents;
 //     the call clears the counter and status words it relies on.  Calls that
 //     overlap on the GPU (other streams, other threads) race on it.
-//   * The call is synchronous: it waits for its stream, then reads the
-//     kernel status word (a timed-out device wait returns GP_ERR_TIMEOUT).
+//   * The call is synchronous: it reads the kernel status word on its own
+//     stream and waits for that stream (a timed-out device wait returns
+//     GP_ERR_TIMEOUT); it does not wait on the device's other streams.
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -155,9 +158,12 @@ extern "C" int gp_psd_filter_noalloc(const int8_t* d_seqs, int64_t n, int L, int
     if (launch_psd_recheck(src, reinterpret_cast<const double*>(s + kOffTw64), thr, a.unsure, a.unsure_count, n,
                            d_pass_mask, sms, st) != cudaSuccess)
         return GP_ERR_CUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return GP_ERR_CUDA;
+    // the status word is read on the caller's stream: nothing here waits on
+    // other streams of the device
     int status = 0;
-    if (cudaMemcpy(&status, s + kOffStatus, sizeof status, cudaMemcpyDeviceToHost) != cudaSuccess) return GP_ERR_CUDA;
+    if (cudaMemcpyAsync(&status, s + kOffStatus, sizeof status, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return GP_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return GP_ERR_CUDA;
     if (status >= GP_KSTATUS_TIMEOUT_BASE && status < GP_KSTATUS_OVERFLOW) return GP_ERR_TIMEOUT;
     if (status) return GP_ERR_OVERFLOW;
     return GP_OK;

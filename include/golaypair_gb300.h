@@ -65,10 +65,24 @@ int gp_psd_filter(gp_ctx* ctx, const int8_t* seqs, int64_t n, int L, int order, 
                   uint32_t* pass_mask, gp_psd_stats* stats);
 
 /* Same on DEVICE buffers (seqs, pass_mask), enqueued on `stream`
- * (a cudaStream_t; NULL = the context's stream).  With stats == NULL the call
- * does not synchronise.  n < 2^31. */
+ * (a cudaStream_t; NULL = the context's stream).  n < 2^31.  With stats !=
+ * NULL the call synchronises and returns any device-side error.  With
+ * stats == NULL it only enqueues: the mask is valid once gp_check(ctx,
+ * stream) has returned GP_OK, which reports a bounded device wait that gave
+ * up (GP_ERR_TIMEOUT) or an overflow (GP_ERR_OVERFLOW) of this call; until
+ * then the error stays pending in the context.  The unsure list and counters
+ * of the FP64 recheck belong to the context: calls on one context must not
+ * overlap on the GPU (enqueue them on one stream, or wait in between). */
 int gp_psd_filter_device(gp_ctx* ctx, const int8_t* d_seqs, int64_t n, int L, int order, int paf, int mode,
                          uint32_t* d_pass_mask, void* stream, gp_psd_stats* stats);
+
+/* Waits for `stream` (NULL = the context's stream) and returns the status
+ * the context's kernels recorded: GP_OK, GP_ERR_TIMEOUT (a bounded device
+ * wait gave up) or GP_ERR_OVERFLOW (a device list ran out of room); the
+ * status is cleared.  Asynchronous callers of gp_psd_filter_device call it
+ * before reading the mask.  No counterpart in the reference, whose filter is
+ * a synchronous host function. */
+int gp_check(gp_ctx* ctx, void* stream);
 
 /* Profiling: when enabled, CUDA events bracket every launch of the main
  * filter kernel (tensor-core or FP64) on its stream.  gp_kernel_time waits
@@ -99,9 +113,12 @@ int gp_debug_wait_timeout(gp_ctx* ctx, int64_t limit_ns);
  *   - n <= 2^20 rows (GP_ERR_ARG beyond, with a message on stderr);
  *     2 <= L <= 127 (GP_ERR_UNSUPPORTED otherwise);
  *   - the first call on a device looks up the array's device address there
- *     (with that device current); make it before any stream capture;
+ *     (with that device current) and keeps it; make it before any stream
+ *     capture; after a cudaDeviceReset of that device the kept address is
+ *     stale: do not call the entry point there again in the same process;
  *   - all calls share the array: calls that overlap on the GPU race;
- *   - synchronous: returns after the stream has finished the work.
+ *   - synchronous: returns after `stream` has finished the work (it waits on
+ *     that stream only).
  */
 int gp_psd_filter_noalloc(const int8_t* d_seqs, int64_t n, int L, int order, int paf, uint32_t* d_pass_mask,
                           void* stream);

@@ -63,8 +63,8 @@ static inline void fftw_execute(const fftw_plan p) {
     const double s = (p->sign == FFTW_FORWARD) ? -1.0 : 1.0;
     for (int k = 0; k < n; ++k) {
         double re = 0.0, im = 0.0;
-        for (int j = 0; j < n; ++j) {
-            int m = (int)(((long long)j * k) % n);
+        int m = 0; /* (j*k) mod n, stepped by k: the same index, no division */
+        for (int j = 0; j < n; ++j, m += k, m -= (m >= n) ? n : 0) {
             double c = p->cs[m], sv = s * p->sn[m];
             re += p->in[j][0] * c - p->in[j][1] * sv;
             im += p->in[j][0] * sv + p->in[j][1] * c;

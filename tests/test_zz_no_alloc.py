@@ -36,15 +36,26 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
     torch.cuda.set_device(0)
     fn = _entry()
     rng = np.random.default_rng(2026)
-    cases = [  # (order, compress, paf, rows): two calls in a row, different shapes
-        (90, 2, 0, 300_000),
-        (57, 3, -2, 200_003),
+    # (order, compress, paf, rows), called one after the other: one length in
+    # every padded-K bucket of the tensor-core filter (K = 16 .. 128); the
+    # entry point builds its twiddles on the device, the allocating one on
+    # the host, and the verdicts must agree in every bucket
+    cases = [
+        (26, 2, 0, 100_000),    # L 13, K 16
+        (57, 3, -2, 200_003),   # L 19, K 32
+        (90, 2, 0, 300_000),    # L 45, K 48
+        (57, 1, -2, 100_000),   # L 57, K 64
+        (72, 1, 0, 60_000),     # L 72, K 80
+        (90, 1, 0, 60_000),     # L 90, K 96
+        (98, 1, 0, 50_000),     # L 98, K 112
+        (126, 1, 0, 50_000),    # L 126, K 128
     ]
     with gp.Context(0) as ctx:
         stream = torch.cuda.Stream()
         for order, compress, paf, n in cases:
             L = order // compress
-            alpha = np.array(list(range(-compress, compress + 1, 2)), dtype=np.int8)
+            alpha = np.array([v for v in range(-compress, compress + 1, 2) if compress % 2 == 0 or v != 0],
+                             dtype=np.int8)
             seqs = torch.from_numpy(rng.choice(alpha, size=(n, L))).cuda()
             want = torch.zeros((n + 31) // 32, dtype=torch.int32, device="cuda")
             got = torch.full_like(want, -1)
@@ -55,7 +66,8 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
             assert rc == 0, rc
             torch.cuda.synchronize()
             assert torch.equal(got, want)
-            assert int(want.ne(0).sum()) > 0  # the batch does contain passes
+            if L <= 57:
+                assert int(want.ne(0).sum()) > 0  # the batch does contain passes
 
 
 def test_noalloc_rejects_batches_over_its_limit():
