@@ -55,27 +55,30 @@ def oracle_lib():
     return lib
 
 
-def host_sample(rows, seed=0):
-    """The same distribution as the device batch, generated on the host."""
-    import numpy as np
-    rng = np.random.default_rng(seed + 1000)
-    out, have = [], 0
-    while have < rows:
-        s = rng.choice(np.array([-2, 0, 2], dtype=np.int8), size=(1 << 20, L))
-        rs = s.astype(np.int32).sum(1)
-        s = s[np.isin(rs, [-12, -6, 6, 12])]
-        out.append(s)
-        have += len(s)
-    return np.ascontiguousarray(np.concatenate(out)[:rows])
+def device_batch_to_host(rows, seed=0):
+    """The bench batch itself (make_batch on the GPU with the same seed, so
+    the very rows the GPU arm filters), copied to pinned host memory; the
+    device copy is freed before anything is timed."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    d = make_batch(torch, rows, dev, seed=seed)
+    h = torch.empty((rows, L), dtype=torch.int8, pin_memory=True)
+    h.copy_(d)
+    del d
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return h.numpy()
 
 
-def cpu_baseline(seconds=12.0):
+def cpu_baseline(host_rows, seconds=12.0):
     """The oracle's FP64 PSD filter (restating src/utils/fourier.cpp:25-52)
-    on all host cores, over a bounded sample of the workload."""
+    on all host cores, over a bounded sample of the bench batch: its first
+    rows (host_rows, copied from the device batch), cycled for ~12 s."""
     import numpy as np
     lib = oracle_lib()
     cores = os.cpu_count() or 1
-    sample = host_sample(1 << 21)
+    sample = np.ascontiguousarray(host_rows)
     verdict = np.zeros(len(sample), dtype=np.uint8)
     lib.gpo_psd_filter_batch(sample.ctypes.data, 1 << 16, L, ORDER, PAF, verdict.ctypes.data, cores)  # warm
     done, t0 = 0, time.perf_counter()
@@ -86,34 +89,41 @@ def cpu_baseline(seconds=12.0):
         if el >= seconds:
             break
     return {"value": done / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{done} rows of the workload distribution (2^21 distinct, seeded), FP64 direct DFT of "
+            "sample": f"{done} rows: the first {len(sample)} rows of the bench batch, cycled; FP64 direct DFT of "
                       f"bins 1..L/2 with early exit, {cores} threads, {el:.1f} s"}
 
 
 def run_reference(args):
+    """The reference's filter (the oracle's FP64 restatement of
+    src/utils/fourier.cpp:25-52; the reference's own build needs FFTW and
+    Boost, absent on the GPU machine) on the host cores, over the same rows as
+    the GPU arm (same generator and seed), one pass over all of them per
+    step."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     import numpy as np
     lib = oracle_lib()
     cores = os.cpu_count() or 1
-    per_step = 1 << 22
-    sample = host_sample(per_step)
-    verdict = np.zeros(per_step, dtype=np.uint8)
+    rows = args.rows
+    WORKLOAD["rows"] = rows
+    seqs = device_batch_to_host(rows, seed=0)
+    verdict = np.zeros(rows, dtype=np.uint8)
     for _ in range(args.warmup):
-        lib.gpo_psd_filter_batch(sample.ctypes.data, per_step, L, ORDER, PAF, verdict.ctypes.data, cores)
+        lib.gpo_psd_filter_batch(seqs.ctypes.data, rows, L, ORDER, PAF, verdict.ctypes.data, cores)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        lib.gpo_psd_filter_batch(sample.ctypes.data, per_step, L, ORDER, PAF, verdict.ctypes.data, cores)
+        lib.gpo_psd_filter_batch(seqs.ctypes.data, rows, L, ORDER, PAF, verdict.ctypes.data, cores)
     el = time.perf_counter() - t0
-    v = per_step * args.steps / el
+    v = rows * args.steps / el
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(WORKLOAD, step_rows=per_step),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, generated on device, copied to host before timing)", "config": WORKLOAD,
+            "passes": int(verdict.sum()),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{per_step} rows per step of the workload distribution; the oracle's FP64 "
-                                       f"filter (restating src/utils/fourier.cpp:25-52), {cores} threads"},
+                             "sample": f"the whole batch ({rows} rows) per step; the oracle's FP64 filter "
+                                       f"(restating src/utils/fourier.cpp:25-52), {cores} threads"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -185,15 +195,13 @@ def make_batch(torch, rows, device, seed=0):
 
 
 def read_profile_traffic():
-    """dram bytes per row of the filter kernel from the committed ncu summary."""
-    p = os.path.join(REPO, "profiles", "psd_tc_L45.md")
+    """DRAM bytes per row of the filter kernel, from the machine-readable
+    record of its ncu capture (profiles/psd_tc_L45.json)."""
+    p = os.path.join(REPO, "profiles", "psd_tc_L45.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
-        for line in f:
-            if line.startswith("dram_bytes_per_row:"):
-                return float(line.split(":")[1].split()[0])
-    return None
+        return float(json.load(f)["dram_bytes_per_row"])
 
 
 def run_gpu(args):
@@ -294,6 +302,7 @@ def run_gpu(args):
     # D2H of the pass mask inside the timed region
     hseqs = torch.empty((ROWS, L), dtype=torch.int8, pin_memory=True)
     hseqs.copy_(seqs)
+    cpu_rows = hseqs[:min(ROWS, 1 << 22)].numpy()  # the CPU baseline's sample: the batch's first rows
     hmask = torch.zeros((ROWS + 31) // 32, dtype=torch.int32, pin_memory=True)
     del seqs
     torch.cuda.empty_cache()
@@ -342,12 +351,133 @@ def run_gpu(args):
                     "d2h_bytes_per_step": ROWS // 8, "steps": e_steps},
             "clocks": clk,
         }
-        line["cpu_baseline"] = cpu_baseline()
+        line["cpu_baseline"] = cpu_baseline(cpu_rows)
+        if ws == 1 and not args.no_extras:
+            line["generation"] = generation_extras(gp, ctx, peaks)
         print(json.dumps(line))
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def tc_flops(L):
+    """Algorithmic PSD flops per candidate: 4 L floor(L/2) + 3 floor(L/2)."""
+    return 4 * L * (L // 2) + 3 * (L // 2)
+
+
+class OracleGenStats(ctypes.Structure):
+    """gpo_gen_stats of oracle/golay_oracle.h."""
+    _fields_ = [("necklaces", ctypes.c_int64), ("psd_evals", ctypes.c_int64), ("psd_pass", ctypes.c_int64),
+                ("written_a", ctypes.c_int64), ("written_b", ctypes.c_int64)]
+
+
+def _oracle_gen_job(job):
+    """One generation job through the oracle, in a spawned pool worker: a
+    rank window ("window", order, c, paf, lo, hi) or one job of the
+    reference's -n/-j split ("split", order, c, paf, j, n)."""
+    import tempfile as _t
+    lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_build", "libgolay_oracle.so"))
+    i32, u64, cp, P = ctypes.c_int, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_void_p
+    lib.gpo_generate.argtypes = [i32, i32, i32, cp, cp, i32, i32, P]
+    lib.gpo_generate_window.argtypes = [i32, i32, i32, cp, cp, u64, u64, u64, u64, P]
+    st = OracleGenStats()
+    with _t.TemporaryDirectory() as d:
+        a, b = os.path.join(d, "a").encode(), os.path.join(d, "b").encode()
+        if job[0] == "window":
+            _, order, comp, paf, lo, hi = job
+            m = 2 ** 64 - 1
+            lib.gpo_generate_window(order, comp, paf, a, b, lo >> 64, lo & m, hi >> 64, hi & m, ctypes.byref(st))
+        else:
+            _, order, comp, paf, j, n = job
+            lib.gpo_generate(order, comp, paf, a, b, j, n, ctypes.byref(st))
+    return st.necklaces, st.psd_evals
+
+
+def generation_extras(gp, ctx, peaks):
+    """The generation configurations, measured after the headline (one
+    dict): the uneven batch (orders 34, 50, 58, 68 at compression 2 and 90
+    at compression 5 over 2^32-word windows) in one tuned engine run; order
+    57 (paf -2, compression 3 -> 1) through the golay driver: gen, sort,
+    match over the whole word space, the uncompression of all 196,216 pairs
+    to length 57 and the equivalence filter of the result; and the oracle's
+    generation on the host cores over bounded samples of the same two
+    workloads."""
+    import multiprocessing as mp
+    import tempfile
+
+    from golaypair_gb300.workloads import batch_windows
+    env = dict(os.environ, LC_ALL="C")
+    bf16 = peaks.get("bf16_tflops") or 1887.2
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        wins = batch_windows()
+        spec = [(o, c, p, lo, hi, os.path.join(tmp, f"{o}a"), os.path.join(tmp, f"{o}b")) for (o, c, p, lo, hi) in wins]
+        ctx.generate_batch(spec, autotune=True)  # the tuner runs once; its choice is cached in the context
+        t0 = time.perf_counter()
+        stats, cfg = ctx.generate_batch(spec, autotune=True)
+        el = time.perf_counter() - t0
+        nk = sum(s.necklaces for s in stats)
+        cand = sum(s.candidates for s in stats)
+        flops = sum(s.candidates * tc_flops(o // c) for s, (o, c, _, _, _) in zip(stats, wins))
+        out["uneven_batch"] = {
+            "seconds": el, "necklaces": nk, "candidates": cand, "necklaces_per_s": nk / el,
+            "candidates_per_s": cand / el, "iterations": cfg.iterations,
+            "tuned": {k: getattr(cfg, k) for k in ("enum_variant", "windows_per_thread", "cand_cap", "tc_ctas_per_sm")},
+            "tensor_pipe": {"algorithmic_tflops": flops / el / 1e12, "peak_tflops": bf16,
+                            "frac": flops / el / 1e12 / bf16,
+                            "note": "algorithmic PSD flops of the candidates over the whole engine run; the "
+                                    "enumerator (integer issue) takes most of the device time"}}
+        cli = gp.CLI_PATH
+        d = os.path.join(tmp, "r57")
+        base = [cli, "57", "-c", "3", "1", "--paf", "-2", "--dir", d]
+        times = {}
+        for stage in ("gen", "sort", "match", "uncompress", "filter"):
+            t0 = time.perf_counter()
+            subprocess.run(base + [stage], check=True, env=env, stdout=subprocess.DEVNULL)
+            times[stage] = time.perf_counter() - t0
+        wd = os.path.join(d, "order-57")
+        with open(os.path.join(wd, "57-pairs-3")) as f:
+            p3 = f.read().split("\n")[:-1]
+        nlines = {fn: sum(1 for _ in open(os.path.join(wd, fn)))
+                  for fn in ("57-filtered_sorted-a", "57-filtered_sorted-b", "57-pairs-1", "57-unique")}
+        exps = 0
+        for line in p3:
+            v = line.split()
+            for side in (v[:19], v[19:]):
+                ones = sum(1 for x in side if x in ("1", "-1"))
+                exps += 3 ** (ones - 1) if ones else 1
+        out["order57"] = {
+            "stage_seconds": times, "lines": nlines, "pairs_compression3": len(p3), "expansions": exps,
+            "uncompress_pairs_per_s": len(p3) / times["uncompress"],
+            "uncompress_expansions_per_s": exps / times["uncompress"],
+            "match_pairs_per_s": len(p3) / times["match"],
+            "filter_pairs_per_s": nlines["57-pairs-1"] / times["filter"],
+            "note": "process wall times of the golay driver, context creation and file I/O included"}
+        # the oracle on the host cores: the batch's windows cut to 2^26 words,
+        # and 16 of 1000 jobs of the order-57 split, one process per item
+        cores = os.cpu_count() or 1
+        subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
+        sample = [("window",) + tuple(w) for w in batch_windows(1 << 26)]
+        with mp.get_context("spawn").Pool(min(cores, len(sample))) as pool:
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_gen_job, sample)
+            wel = time.perf_counter() - t0
+        shards = [("split", 57, 3, -2, j, 1000) for j in range(min(cores, 16))]
+        with mp.get_context("spawn").Pool(len(shards)) as pool:
+            t0 = time.perf_counter()
+            res57 = pool.map(_oracle_gen_job, shards)
+            sel = time.perf_counter() - t0
+        out["cpu_pipeline"] = {
+            "kind": "port", "cores": cores,
+            "uneven_batch_2^26_windows": {"seconds": wel, "necklaces_per_s": sum(r[0] for r in res) / wel,
+                                          "candidates_per_s": sum(r[1] for r in res) / wel,
+                                          "processes": len(sample)},
+            "order57_16_of_1000_jobs": {"seconds": sel, "necklaces_per_s": sum(r[0] for r in res57) / sel,
+                                        "candidates_per_s": sum(r[1] for r in res57) / sel,
+                                        "processes": len(shards)},
+            "note": "the oracle's generation (FP64 PSD filter, canonical check, files) on the same host's cores"}
+    return out
 
 
 def run_pipeline(args):
@@ -446,6 +576,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--rows", type=int, default=1 << 28, help="batch rows (profiling runs only)")
     ap.add_argument("--profile", action="store_true", help="time the tensor-core filter only")
+    ap.add_argument("--no-extras", action="store_true", help="skip the generation configurations after the headline")
     ap.add_argument("--trace", action="store_true", help="with --profile: per-role cycle counters")
     ap.add_argument("--pipeline", action="store_true", help="time the generation configurations instead")
     ap.add_argument("--pipeline-pairs", type=int, default=200, help="compressed pairs to uncompress (--pipeline)")

@@ -10,12 +10,29 @@ Boost headers) into oracle/_ref/golay_ref, runs it under LC_ALL=C, and stores:
   shard 7 of 1000);
 * manifest.json "windows" -- the same for the uneven batch's windows
   (golaypair_gb300/workloads.py) at 2^32 and 2^24 words, produced by the
-  reference's own generation functions through oracle/ref_window_driver.cpp.
+  reference's own generation functions through oracle/ref_window_driver.cpp,
+  and the pair file of the reference's `sort` and `match` over each window's
+  candidate files;
+* n21_c31/, n27_c31/ -- the sorted, pair and unique files of
+  `main N -c 3 1 --paf -2 all` (Legendre-type pairs, odd compression 3 -> 1;
+  verbatim), and hashes of the same runs at orders 33 and 39;
+* manifest.json "n57" -- order 57, paf -2, compression 3 -> 1 in full:
+  `gen` over 8 jobs (-n 8 -j 0..7, run in parallel), `sort`, `match`
+  (hashes of the sorted files and of the 196,216-line pair file), then the
+  uncompression and filter of two 200-line subsets of the pair file (its
+  first 200 lines; 200 lines drawn with numpy's default_rng(0), in file
+  order).  The reference never reads its line-range options, so each line
+  is uncompressed in a directory of its own (one process per line, several
+  at a time) and the per-line outputs are concatenated in line order, which
+  is what one run over the subset writes; `filter` then runs on each
+  subset's concatenated pair file.  About 3 hours on 8 cores; resumable:
+  steps whose outputs exist in the work directory are skipped.
 
 Needs the reference sources; run in the build container only:
-    python tests/golden/make_golden.py            # everything
+    python tests/golden/make_golden.py            # everything but n57
     python tests/golden/make_golden.py --windows  # only the window goldens
     python tests/golden/make_golden.py --run=NAME # only the named run (merged)
+    python tests/golden/make_golden.py --n57 --workdir DIR  # the order-57 goldens
 """
 import hashlib
 import json
@@ -46,7 +63,15 @@ RUNS = [
     ("n32_c421", ["32", "-c", "4", "2", "1", "gen", "sort", "match", "uncompress"],
      ["32-filtered-a#0", "32-filtered-b#0", "32-filtered_sorted-a", "32-filtered_sorted-b", "32-pairs-4",
       "32-pairs-2", "32-pairs-1"], False),
+] + [
+    # Legendre-type pairs (paf -2) at the odd compression 3 -> 1
+    (f"n{n}_c31", [str(n), "-c", "3", "1", "--paf", "-2", "all"],
+     [f"{n}-filtered_sorted-a", f"{n}-filtered_sorted-b", f"{n}-pairs-3", f"{n}-pairs-1", f"{n}-unique"], n < 30)
+    for n in (21, 27, 33, 39)
 ]
+N57_ARGV = ["57", "-c", "3", "1", "--paf", "-2"]
+N57_JOBS = 8
+N57_HEADS = 200
 SUBCOMMANDS = {"gen", "sort", "match", "uncompress", "filter", "all"}
 
 
@@ -70,14 +95,28 @@ def window_key(job):
 
 
 def run_window(job, tmp):
+    """The window's candidate files from the reference's own generation
+    functions, then the reference's `sort` and `match` over them (the files
+    placed as job 0's candidate files of a work directory)."""
     o, c, p, lo, hi = job
-    fa, fb = os.path.join(tmp, window_key(job).replace("/", "_") + "a"), os.path.join(tmp, window_key(job).replace("/", "_") + "b")
+    env = dict(os.environ, LC_ALL="C")
+    d = os.path.join(tmp, window_key(job).replace("/", "_"))
+    wd = os.path.join(d, f"order-{o}")
+    os.makedirs(wd)
+    fa, fb = os.path.join(wd, f"{o}-filtered-a#0"), os.path.join(wd, f"{o}-filtered-b#0")
     out = subprocess.run([REF_WINDOW_BIN, str(o), str(c), str(p), str(lo), str(hi), fa, fb], check=True,
-                         capture_output=True, text=True, env=dict(os.environ, LC_ALL="C")).stdout
+                         capture_output=True, text=True, env=env).stdout
     rec = {"job": list(job), "necklaces": int(out.split()[-1])}
     for side, path in (("a", fa), ("b", fb)):
         with open(path, "rb") as f:
             rec[side] = {"lines": f.read().count(b"\n"), "sha256": sha256(path)}
+    # match returns 1 on an empty input (src/core/match/match_pairs.cpp:32-38), after writing an empty pair file
+    r = subprocess.run([REF_BIN, str(o), "-c", str(c), "--paf", str(p), "--dir", d, "sort", "match"], env=env,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    assert r.returncode in (0, 1), (job, r.returncode)
+    pairs = os.path.join(wd, f"{o}-pairs-{c}")
+    with open(pairs, "rb") as f:
+        rec["pairs"] = {"lines": f.read().count(b"\n"), "sha256": sha256(pairs)}
     return rec
 
 
@@ -90,10 +129,102 @@ def make_windows(manifest):
     manifest["windows"] = {window_key(r["job"]): r for r in recs}
 
 
+def n57_subsets(nlines):
+    """The two head subsets of the order-57 pair file: line indices (0-based)."""
+    import numpy as np
+    seeded = sorted(np.random.default_rng(0).choice(nlines, N57_HEADS, replace=False).tolist())
+    return {"head200": list(range(N57_HEADS)), "seed200": seeded}
+
+
+def make_n57(manifest, work, procs):
+    env = dict(os.environ, LC_ALL="C")
+    full = os.path.join(work, "d")
+    wd = os.path.join(full, "order-57")
+    if not os.path.exists(os.path.join(wd, "57-pairs-3")):
+        ps = [subprocess.Popen([REF_BIN] + N57_ARGV + ["-n", str(N57_JOBS), "-j", str(j), "--dir", full, "gen"],
+                               stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env=env)
+              for j in range(N57_JOBS)]
+        for p in ps:
+            assert p.wait() == 0
+        for sub in ("sort", "match"):
+            subprocess.run([REF_BIN] + N57_ARGV + ["-n", str(N57_JOBS), "--dir", full, sub], check=True, env=env,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    rec = {"argv": N57_ARGV + ["-n", str(N57_JOBS), "gen|sort|match"], "files": {}, "subsets": {}}
+    for fn in ("57-filtered_sorted-a", "57-filtered_sorted-b", "57-pairs-3"):
+        with open(os.path.join(wd, fn), "rb") as f:
+            data = f.read()
+        rec["files"][fn] = {"lines": data.count(b"\n"), "sha256": hashlib.sha256(data).hexdigest()}
+    with open(os.path.join(wd, "57-pairs-3")) as f:
+        lines = f.read().split("\n")[:-1]
+    subsets = n57_subsets(len(lines))
+
+    def cost(i):  # expansions of the line's two sides: 3^(entries of magnitude 1, less the first)
+        v = lines[i].split()
+        return sum(3 ** max(0, sum(1 for x in side if x in ("1", "-1")) - 1) for side in (v[:19], v[19:]))
+
+    todo = sorted(set(i for idx in subsets.values() for i in idx), key=lambda i: -cost(i))
+
+    def one_line(i):  # uncompression of one input line
+        d = os.path.join(work, "h", str(i))
+        if os.path.exists(os.path.join(d, "ok")):
+            return
+        os.makedirs(os.path.join(d, "order-57"), exist_ok=True)
+        with open(os.path.join(d, "order-57", "57-pairs-3"), "w") as f:
+            f.write(lines[i] + "\n")
+        subprocess.run([REF_BIN] + N57_ARGV + ["--dir", d, "uncompress"], check=True, env=env,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        for t in ("uncompress_tmp_a", "uncompress_tmp_b", "uncompress_tmp_a.sorted", "uncompress_tmp_b.sorted"):
+            os.remove(os.path.join(d, "order-57", t))
+        open(os.path.join(d, "ok"), "w").close()
+
+    with ThreadPoolExecutor(procs) as ex:  # longest lines first
+        list(ex.map(one_line, todo))
+    for name, idx in subsets.items():
+        d = os.path.join(work, name)
+        os.makedirs(os.path.join(d, "order-57"), exist_ok=True)
+        with open(os.path.join(d, "order-57", "57-pairs-3"), "w") as f:
+            f.write("".join(lines[i] + "\n" for i in idx))
+        with open(os.path.join(d, "order-57", "57-pairs-1"), "wb") as f:
+            for i in idx:
+                with open(os.path.join(work, "h", str(i), "order-57", "57-pairs-1"), "rb") as g:
+                    f.write(g.read())
+        if not os.path.exists(os.path.join(d, "order-57", "57-unique")):
+            subprocess.run([REF_BIN] + N57_ARGV + ["--dir", d, "filter"], check=True, env=env,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        srec = {"indices": idx, "files": {}}
+        for fn in ("57-pairs-1", "57-unique"):
+            with open(os.path.join(d, "order-57", fn), "rb") as f:
+                data = f.read()
+            srec["files"][fn] = {"lines": data.count(b"\n"), "sha256": hashlib.sha256(data).hexdigest()}
+        rec["subsets"][name] = srec
+    manifest["n57"] = rec
+
+
+def arg_value(name, default=None):
+    for i, a in enumerate(sys.argv[1:], 1):
+        if a.startswith(name + "="):
+            return a.split("=", 1)[1]
+        if a == name and i + 1 < len(sys.argv):
+            return sys.argv[i + 1]
+    return default
+
+
 def main():
     subprocess.run(["bash", os.path.join(REPO, "oracle", "build_ref.sh")], check=True)
     if not os.path.exists(REF_BIN):
         sys.exit("reference binary missing (no reference sources here)")
+    if "--n57" in sys.argv[1:]:
+        work = os.path.abspath(arg_value("--workdir") or tempfile.mkdtemp(prefix="golden57_"))
+        procs = int(arg_value("--procs", str(N57_JOBS)))
+        manifest = {}
+        make_n57(manifest, work, procs)
+        with open(os.path.join(HERE, "manifest.json")) as f:  # merged into the current manifest at the end
+            cur = json.load(f)
+        cur["n57"] = manifest["n57"]
+        with open(os.path.join(HERE, "manifest.json"), "w") as f:
+            json.dump(cur, f, indent=1, sort_keys=True)
+        print("order-57 goldens written")
+        return
     if "--windows" in sys.argv[1:]:
         with open(os.path.join(HERE, "manifest.json")) as f:
             manifest = json.load(f)

@@ -9,6 +9,8 @@ capacity, enumerator variant, windows per thread, filter grid, tuner).
 """
 import ctypes
 import hashlib
+import os
+import subprocess
 
 import pytest
 
@@ -132,9 +134,24 @@ def test_uneven_batch_windows_match_reference(golden_manifest, tmp_path, size):
     recs = golden_manifest["windows"]
     with gp.Context(0) as ctx:
         files, stats, _ = run_batch(ctx, tmp_path, "w", jobs=wins, autotune=size > (1 << 24))
-    for w, (a, b), st in zip(wins, files, stats):
+    for i, (w, (a, b), st) in enumerate(zip(wins, files, stats)):
         rec = recs["%d/%d/%d/%d-%d" % tuple(w)]
         assert st.necklaces == rec["necklaces"], w
         assert a.count(b"\n") == rec["a"]["lines"] and b.count(b"\n") == rec["b"]["lines"], w
         assert hashlib.sha256(a).hexdigest() == rec["a"]["sha256"], w
         assert hashlib.sha256(b).hexdigest() == rec["b"]["sha256"], w
+        if "pairs" not in rec:
+            continue
+        # the per-order pair set: sort and match over the batch's files, as the
+        # reference's sort and match ran over its own window files
+        o, c, p = w[0], w[1], w[2]
+        wd = tmp_path / f"pairs{i}" / f"order-{o}"
+        wd.mkdir(parents=True)
+        (wd / f"{o}-filtered-a#0").write_bytes(a)
+        (wd / f"{o}-filtered-b#0").write_bytes(b)
+        r = subprocess.run([gp.CLI_PATH, str(o), "-c", str(c), "--paf", str(p), "--dir", str(wd.parent), "sort",
+                            "match"], capture_output=True, text=True, env=dict(os.environ, LC_ALL="C"))
+        assert r.returncode in (0, 1), r.stderr
+        pairs = read(str(wd / f"{o}-pairs-{c}"))
+        assert pairs.count(b"\n") == rec["pairs"]["lines"], w
+        assert hashlib.sha256(pairs).hexdigest() == rec["pairs"]["sha256"], w
