@@ -7,13 +7,16 @@
 // and (compression 1, even L only) negate the odd positions of both.  It is
 // built on the host, as the reference builds it once per run.
 //
-// class_kernel (several CTAs per pair, each a share of the generators)
-// applies every generator to the pair with the reference's application rule
-// (equivalence.cpp:97-144), counts the distinct images in a per-pair
-// open-addressing table (generator ids; images are recomputed entry by
-// entry, never stored) and looks every distinct image up in the sorted pair
-// set.  The host then replays the reference's in-order erase loop
-// (filter.cpp:117-144) on those class sizes and member lists.
+// class_kernel applies every generator to the pairs with the reference's
+// application rule (equivalence.cpp:97-144).  One pass over the (transposed)
+// generator table hashes the images of several pairs at once, so the table
+// is read once per group of pairs, not once per pair.  Per pair it counts
+// the generators that fix the pair (its stabiliser: the class size is the
+// group order over that count, orbit-stabiliser, the generator set being a
+// group) and looks every image up in a hash set of the input pairs
+// (verified entry by entry on a hash match).  The host then replays the
+// reference's in-order erase loop (filter.cpp:117-144) on those class sizes
+// and member lists.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -36,91 +39,103 @@ __device__ __forceinline__ int image_at(const int16_t* srcT, int64_t ng, int64_t
     return s < 0 ? -v : v;
 }
 
-__device__ __forceinline__ uint32_t image_hash(const int16_t* srcT, int64_t ng, int64_t g, const int8_t* sx, int W) {
-    uint32_t h = 2166136261u;
-    for (int o = 0; o < W; ++o) {
-        h ^= (uint8_t)image_at(srcT, ng, g, sx, o);
-        h *= 16777619u;
-    }
-    return h ^ (h >> 15);
-}
+constexpr int kPairsPerCta = 8;  // pairs whose images one pass over the generator table hashes
 
-__device__ __forceinline__ bool same_image(const int16_t* srcT, int64_t ng, int64_t g1, int64_t g2, const int8_t* sx,
-                                           int W) {
+// FNV-1a over the entries as bytes (value mod 256), folded; the host hashes
+// the input pairs with the same steps
+__host__ __device__ __forceinline__ uint32_t fnv_step(uint32_t h, int v) { return (h ^ (uint8_t)v) * 16777619u; }
+__host__ __device__ __forceinline__ uint32_t fnv_fold(uint32_t h) { return h ^ (h >> 15); }
+constexpr uint32_t kFnvBasis = 2166136261u;
+
+// the image of the pair sx under generator g equals target (W entries)
+__device__ __forceinline__ bool image_equals(const int16_t* srcT, int64_t ng, int64_t g, const int8_t* sx,
+                                             const int8_t* target, int W) {
     for (int o = 0; o < W; ++o)
-        if (image_at(srcT, ng, g1, sx, o) != image_at(srcT, ng, g2, sx, o)) return false;
+        if (image_at(srcT, ng, g, sx, o) != target[o]) return false;
     return true;
 }
 
-// keys: sorted pairs, W bytes each (value + 128, so byte order = int order);
-// the image of generator g is compared entry by entry as it is computed
-__device__ __forceinline__ int64_t find_image(const uint8_t* keys, int64_t np, int W, const int16_t* srcT, int64_t ng,
-                                              int64_t g, const int8_t* sx) {
-    int64_t lo = 0, hi = np - 1;
-    while (lo <= hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        const uint8_t* k = keys + mid * W;
-        int c = 0;
-        for (int i = 0; i < W; ++i) {
-            const int a = k[i], b = image_at(srcT, ng, g, sx, i) + 128;
-            if (a != b) {
-                c = a < b ? -1 : 1;
-                break;
-            }
-        }
-        if (c == 0) return mid;
-        if (c < 0)
-            lo = mid + 1;
-        else
-            hi = mid - 1;
-    }
-    return -1;
-}
+struct ClassArgs {
+    const int16_t* srcT;      // generator table, transposed: srcT[o * ng + g]
+    int64_t ng;
+    int64_t group0;           // first pair group of the launch
+    const int8_t* pairs;      // np x W, sorted (the reference's set order)
+    int64_t np;
+    int W;
+    const uint32_t* set_h;    // hash set of the pairs: folded hash, pair index (EMPTY: 0xFFFFFFFF)
+    const uint32_t* set_i;
+    uint32_t set_mask;
+    uint32_t* stab;           // per pair: generators that fix it
+    uint32_t* members;        // (pair, member) index pairs
+    unsigned long long* nmembers;
+    int64_t mcap;
+    int* status;
+};
 
-// CTA b handles pair p0 + b / splits and the generators of its share
-// (b % splits): the CTAs of one pair share its open-addressing table of
-// generator ids, so each distinct image is counted once.
-__global__ void class_kernel(const int16_t* srcT, int64_t ng, const int8_t* pairs, const uint8_t* keys, int64_t np,
-                             int W, int64_t p0, int splits, int32_t* tables, int64_t tsize,
-                             unsigned long long* class_size, uint32_t* members, unsigned long long* nmembers,
-                             int64_t mcap, int* status) {
-    const int64_t local = blockIdx.x / splits;
+// CTA b: pairs of group b / splits (kPairsPerCta consecutive pairs) and the
+// generators of share b % splits.
+__global__ void __launch_bounds__(256) class_kernel(ClassArgs a, int splits) {
+    constexpr int PG = kPairsPerCta;
+    __shared__ int8_t sx[PG][kMaxW];
+    __shared__ uint32_t self_h[PG];
+    const int64_t group = a.group0 + blockIdx.x / splits;
     const int part = blockIdx.x % splits;
-    const int64_t x = p0 + local;
-    const int8_t* xs = pairs + x * W;
-    int32_t* tab = tables + local * tsize;
-    __shared__ int8_t sx[kMaxW];
-    for (int i = threadIdx.x; i < W; i += blockDim.x) sx[i] = xs[i];
+    const int64_t x0 = group * PG;
+    const int npg = (int)min((int64_t)PG, a.np - x0);
+    const int W = a.W;
+    for (int k = threadIdx.x; k < PG * W; k += blockDim.x) {
+        const int p = k / W, o = k - p * W;
+        sx[p][o] = p < npg ? a.pairs[(x0 + p) * W + o] : 0;
+    }
     __syncthreads();
-    unsigned distinct = 0;
+    if (threadIdx.x < PG) {
+        uint32_t h = kFnvBasis;
+        for (int o = 0; o < W; ++o) h = fnv_step(h, sx[threadIdx.x][o]);
+        self_h[threadIdx.x] = fnv_fold(h);
+    }
+    __syncthreads();
+    uint32_t stab[PG];
+#pragma unroll
+    for (int p = 0; p < PG; ++p) stab[p] = 0;
     const int64_t step = (int64_t)splits * blockDim.x;
-    for (int64_t g = (int64_t)part * blockDim.x + threadIdx.x; g < ng; g += step) {
-        int64_t h = (int64_t)(image_hash(srcT, ng, g, sx, W) & (uint32_t)(tsize - 1));
-        bool inserted = false;
-        for (int64_t probe = 0; probe < tsize; ++probe) {
-            const int32_t old = atomicCAS(&tab[h], -1, (int32_t)g);
-            if (old == -1) {
-                inserted = true;
-                break;
+    for (int64_t g = (int64_t)part * blockDim.x + threadIdx.x; g < a.ng; g += step) {
+        uint32_t h[PG];
+#pragma unroll
+        for (int p = 0; p < PG; ++p) h[p] = kFnvBasis;
+        for (int o = 0; o < W; ++o) {  // one read of the generator's entry serves every pair of the group
+            const int sgn = a.srcT[(int64_t)o * a.ng + g];
+            const int idx = (sgn < 0 ? -sgn : sgn) - 1;
+#pragma unroll
+            for (int p = 0; p < PG; ++p) {
+                const int v = sx[p][idx];
+                h[p] = fnv_step(h[p], sgn < 0 ? -v : v);
             }
-            if (same_image(srcT, ng, g, old, sx, W)) break;
-            h = (h + 1) & (tsize - 1);
         }
-        if (!inserted) continue;
-        ++distinct;
-        const int64_t m = find_image(keys, np, W, srcT, ng, g, sx);
-        if (m >= 0) {
-            const unsigned long long pos = atomicAdd(nmembers, 1ull);
-            if ((int64_t)pos < mcap) {
-                members[2 * pos] = (uint32_t)x;
-                members[2 * pos + 1] = (uint32_t)m;
-            } else {
-                atomicCAS(status, 0, GP_KSTATUS_OVERFLOW);
+#pragma unroll
+        for (int p = 0; p < PG; ++p) {
+            if (p >= npg) continue;
+            const uint32_t hp = fnv_fold(h[p]);
+            if (hp == self_h[p] && image_equals(a.srcT, a.ng, g, sx[p], sx[p], W)) ++stab[p];
+            for (uint32_t slot = hp & a.set_mask;; slot = (slot + 1) & a.set_mask) {
+                const uint32_t m = a.set_i[slot];
+                if (m == 0xFFFFFFFFu) break;
+                if (a.set_h[slot] != hp || !image_equals(a.srcT, a.ng, g, sx[p], a.pairs + (int64_t)m * W, W))
+                    continue;
+                const unsigned long long pos = atomicAdd(a.nmembers, 1ull);
+                if ((int64_t)pos < a.mcap) {
+                    a.members[2 * pos] = (uint32_t)(x0 + p);
+                    a.members[2 * pos + 1] = m;
+                } else {
+                    atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
+                }
             }
         }
     }
-    distinct = __reduce_add_sync(0xFFFFFFFFu, distinct);
-    if ((threadIdx.x & 31) == 0 && distinct) atomicAdd(&class_size[x], (unsigned long long)distinct);
+#pragma unroll
+    for (int p = 0; p < PG; ++p) {
+        const uint32_t t = __reduce_add_sync(0xFFFFFFFFu, stab[p]);
+        if ((threadIdx.x & 31) == 0 && t && p < npg) atomicAdd(&a.stab[x0 + p], t);
+    }
 }
 
 // Units that generate the group of units mod L (greedy: each one added is
@@ -382,50 +397,80 @@ int gp_equiv_filter(gp_ctx* c, int order, int compress, const char* in_path, con
             for (int o = 0; o < W; ++o) items[(size_t)o * ng + g] = s[o];
         }
         std::vector<int8_t> pairs((size_t)np * W);
-        std::vector<uint8_t> keys((size_t)np * W);
         for (int64_t i = 0; i < np; ++i)
-            for (int j = 0; j < W; ++j) {
-                pairs[i * W + j] = P[i][j];
-                keys[i * W + j] = (uint8_t)(P[i][j] + 128);
-            }
-        int64_t tsize = 1;
-        while (tsize < 2 * ng) tsize <<= 1;
-        int64_t batch = std::max<int64_t>(1, std::min<int64_t>(np, (int64_t(1) << 28) / (tsize * 4)));
+            for (int j = 0; j < W; ++j) pairs[i * W + j] = P[i][j];
+        // hash set of the pairs (the image lookup), same hash as the kernel's
+        uint32_t set_size = 1;
+        while (set_size < 2 * (uint64_t)np) set_size <<= 1;
+        std::vector<uint32_t> set_h(set_size, 0), set_i(set_size, 0xFFFFFFFFu);
+        for (int64_t i = 0; i < np; ++i) {
+            uint32_t h = kFnvBasis;
+            for (int j = 0; j < W; ++j) h = fnv_step(h, P[i][j]);
+            h = fnv_fold(h);
+            uint32_t slot = h & (set_size - 1);
+            while (set_i[slot] != 0xFFFFFFFFu) slot = (slot + 1) & (set_size - 1);
+            set_h[slot] = h;
+            set_i[slot] = (uint32_t)i;
+        }
         const int64_t mcap = std::max<int64_t>(np * 64, 1 << 20);
         cudaStream_t s = c->s_comp;
-        DevBuf di, dp, dk, dt, dcs, dm, dmisc;
-        if (!di.ensure(items.size() * 2) || !dp.ensure(pairs.size()) || !dk.ensure(keys.size()) ||
-            !dt.ensure((size_t)batch * tsize * 4) || !dcs.ensure(np * 8) || !dm.ensure((size_t)mcap * 8) ||
+        DevBuf di, dp, dsh, dsi, dst, dm, dmisc;
+        if (!di.ensure(items.size() * 2) || !dp.ensure(pairs.size()) || !dsh.ensure((size_t)set_size * 4) ||
+            !dsi.ensure((size_t)set_size * 4) || !dst.ensure(np * 4) || !dm.ensure((size_t)mcap * 8) ||
             !dmisc.ensure(64))
             return c->fail(GP_ERR_NOMEM, "equivalence filter: device allocation");
         GP_CUDA_TRY(c, cudaMemcpyAsync(di.p, items.data(), items.size() * 2, cudaMemcpyHostToDevice, s));
         GP_CUDA_TRY(c, cudaMemcpyAsync(dp.p, pairs.data(), pairs.size(), cudaMemcpyHostToDevice, s));
-        GP_CUDA_TRY(c, cudaMemcpyAsync(dk.p, keys.data(), keys.size(), cudaMemcpyHostToDevice, s));
-        GP_CUDA_TRY(c, cudaMemsetAsync(dcs.p, 0, np * 8, s));
+        GP_CUDA_TRY(c, cudaMemcpyAsync(dsh.p, set_h.data(), (size_t)set_size * 4, cudaMemcpyHostToDevice, s));
+        GP_CUDA_TRY(c, cudaMemcpyAsync(dsi.p, set_i.data(), (size_t)set_size * 4, cudaMemcpyHostToDevice, s));
+        GP_CUDA_TRY(c, cudaMemsetAsync(dst.p, 0, np * 4, s));
         GP_CUDA_TRY(c, cudaMemsetAsync(dmisc.p, 0, 64, s));
-        for (int64_t p0 = 0; p0 < np; p0 += batch) {
-            const int64_t nb = std::min(batch, np - p0);
-            // CTAs per pair: enough for four CTAs per SM, each with at least
-            // one generator per thread
-            const int64_t want = std::max<int64_t>(1, (4 * (int64_t)c->num_sms + nb - 1) / nb);
-            const int splits = (int)std::max<int64_t>(1, std::min<int64_t>(want, (ng + 255) / 256));
-            GP_CUDA_TRY(c, cudaMemsetAsync(dt.p, 0xFF, (size_t)nb * tsize * 4, s));
-            class_kernel<<<(unsigned)(nb * splits), 256, 0, s>>>(
-                di.as<int16_t>(), ng, dp.as<int8_t>(), dk.as<uint8_t>(), np, W, p0, splits, dt.as<int32_t>(), tsize,
-                dcs.as<unsigned long long>(), dm.as<uint32_t>(), dmisc.as<unsigned long long>(), mcap,
-                c->status.as<int>());
-            GP_CUDA_TRY(c, cudaGetLastError());
+        ClassArgs ca{};
+        ca.srcT = di.as<int16_t>();
+        ca.ng = ng;
+        ca.pairs = dp.as<int8_t>();
+        ca.np = np;
+        ca.W = W;
+        ca.set_h = dsh.as<uint32_t>();
+        ca.set_i = dsi.as<uint32_t>();
+        ca.set_mask = set_size - 1;
+        ca.stab = dst.as<uint32_t>();
+        ca.members = dm.as<uint32_t>();
+        ca.nmembers = dmisc.as<unsigned long long>();
+        ca.mcap = mcap;
+        ca.status = c->status.as<int>();
+        const int64_t groups = (np + kPairsPerCta - 1) / kPairsPerCta;
+        // generator shares per group: enough CTAs for eight per SM, each share
+        // at least one generator per thread
+        const int64_t want = std::max<int64_t>(1, (8 * (int64_t)c->num_sms + groups - 1) / groups);
+        const int splits = (int)std::max<int64_t>(1, std::min<int64_t>(want, (ng + 255) / 256));
+        for (int64_t g0 = 0; g0 < groups; g0 += (int64_t(1) << 20)) {  // grids of at most 2^20 groups
+            const int64_t gn = std::min<int64_t>(groups - g0, int64_t(1) << 20);
+            ClassArgs cb = ca;
+            cb.group0 = g0;
+            class_kernel<<<(unsigned)(gn * splits), 256, 0, s>>>(cb, splits);
         }
+        GP_CUDA_TRY(c, cudaGetLastError());
         GP_CUDA_TRY(c, cudaStreamSynchronize(s));
         int rc = c->check_status("equivalence filter");
         if (rc) {
             if (out) fclose(out);
             return rc;
         }
-        std::vector<unsigned long long> csize(np);
+        std::vector<uint32_t> stab(np);
         unsigned long long nmem = 0;
-        GP_CUDA_TRY(c, cudaMemcpy(csize.data(), dcs.p, np * 8, cudaMemcpyDeviceToHost));
+        GP_CUDA_TRY(c, cudaMemcpy(stab.data(), dst.p, np * 4, cudaMemcpyDeviceToHost));
         GP_CUDA_TRY(c, cudaMemcpy(&nmem, dmisc.p, 8, cudaMemcpyDeviceToHost));
+        // orbit-stabiliser: class size = group order / generators fixing the pair
+        std::vector<unsigned long long> csize(np);
+        for (int64_t i = 0; i < np; ++i) {
+            if (stab[i] == 0 || ng % stab[i] != 0) {
+                if (out) fclose(out);
+                return c->fail(GP_ERR_CUDA, "equivalence filter: stabiliser of pair %lld is %u of %lld generators",
+                               (long long)i, stab[i], (long long)ng);
+            }
+            csize[i] = (unsigned long long)(ng / stab[i]);
+        }
         std::vector<uint32_t> mem((size_t)nmem * 2);
         if (nmem) GP_CUDA_TRY(c, cudaMemcpy(mem.data(), dm.p, mem.size() * 4, cudaMemcpyDeviceToHost));
         std::vector<std::vector<uint32_t>> members(np);

@@ -129,19 +129,26 @@ __device__ __forceinline__ void flag_overflow(int* status) { atomicCAS(status, 0
 template <int NP>
 __global__ void __launch_bounds__(kScanThreads) ux_scan_kernel(ScanArgs a) {
     extern __shared__ float4 smem[];
-    __shared__ int s_side, s_nfree, s_npre;
+    __shared__ int s_nfree, s_npre;
     __shared__ uint32_t s_scount;
-    __shared__ int s_pos[kMaxL], s_cnt[kMaxL], s_coff[kMaxL], s_dig0[kMaxL];
+    __shared__ int s_pos[kMaxL], s_cnt[kMaxL], s_coff[kMaxL];
     __shared__ float4 s_F[NP];
     const LevelDev& lv = a.lv;
     float4* s_S = smem;  // [scount][NP] suffix sums, then the free positions' terms
     float4* s_C = smem;  // placed after the suffix table when a side starts
     const int tid = threadIdx.x, lane = tid & 31;
-    int cur_side = -1;
+    // a contiguous share of the units per CTA: consecutive units mostly
+    // belong to one side, so its tables are built once and no barrier
+    // separates the units of a side
+    const uint64_t u_begin = a.n_units * blockIdx.x / gridDim.x;
+    const uint64_t u_end = a.n_units * (blockIdx.x + 1) / gridDim.x;
+    int side = -1;  // the same in every thread of the CTA
     uint32_t scount = 1;
-    for (uint64_t u = blockIdx.x; u < a.n_units; u += gridDim.x) {
-        __syncthreads();
-        if (tid == 0) {  // last side whose first unit is <= u
+    int npre = 0;
+    for (uint64_t u = u_begin; u < u_end; ++u) {
+        // the side of unit u: the last side whose first unit is <= u
+        int sd = side;
+        if (sd < 0) {
             int lo = 0, hi = a.n_sides - 1;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
@@ -150,13 +157,13 @@ __global__ void __launch_bounds__(kScanThreads) ux_scan_kernel(ScanArgs a) {
                 else
                     hi = mid - 1;
             }
-            s_side = lo;
+            sd = lo;
         }
-        __syncthreads();
-        const int side = s_side;
-        const uint8_t* rows = lv.side_rows + (size_t)side * lv.L;
-        if (side != cur_side) {
-            cur_side = side;
+        while (sd + 1 < a.n_sides && a.unit_begin[sd + 1] <= u) ++sd;
+        const uint8_t* rows = lv.side_rows + (size_t)sd * lv.L;
+        if (sd != side) {
+            __syncthreads();  // every thread is done with the previous side's tables
+            side = sd;
             if (tid == 0) {
                 int nfree = 0, off = 0;
                 for (int i = 0; i < lv.L; ++i) {
@@ -178,8 +185,9 @@ __global__ void __launch_bounds__(kScanThreads) ux_scan_kernel(ScanArgs a) {
             }
             __syncthreads();
             scount = s_scount;
+            npre = s_npre;
             s_C = smem + (size_t)scount * NP;
-            const int nfree = s_nfree, npre = s_npre;
+            const int nfree = s_nfree;
             // the free positions' terms, then the fixed positions' sum
             for (int f = 0; f < nfree; ++f) {
                 const int i = s_pos[f], c = s_cnt[f];
@@ -217,19 +225,9 @@ __global__ void __launch_bounds__(kScanThreads) ux_scan_kernel(ScanArgs a) {
                 }
                 s_S[j * NP + p] = S;
             }
+            __syncthreads();
         }
-        // digits of the unit's first prefix index (prefix positions only)
-        const uint64_t pre0 = (u - a.unit_begin[side]) * (uint64_t)kScanThreads;
-        if (tid == 0) {
-            uint64_t rem = pre0;
-            for (int f = s_npre - 1; f >= 0; --f) {
-                const uint64_t c = (uint64_t)s_cnt[f];
-                s_dig0[f] = (int)(rem % c);
-                rem /= c;
-            }
-        }
-        __syncthreads();
-        const uint64_t pidx = pre0 + (uint64_t)tid;
+        const uint64_t pidx = (u - a.unit_begin[side]) * (uint64_t)kScanThreads + (uint64_t)tid;
         const bool active = pidx < a.prefix_count[side];
         float2 Pr[NP], Pi[NP];
 #pragma unroll
@@ -238,16 +236,19 @@ __global__ void __launch_bounds__(kScanThreads) ux_scan_kernel(ScanArgs a) {
             Pr[p] = make_float2(F.x, F.y);
             Pi[p] = make_float2(F.z, F.w);
         }
-        {
-            uint32_t t = (uint32_t)tid;
-            int carry = 0;
-            for (int f = s_npre - 1; f >= 0; --f) {
+        if (active) {  // the prefix: digits of pidx over the leading free positions
+            uint64_t rem = pidx;
+            for (int f = npre - 1; f >= 0; --f) {
                 const uint32_t c = (uint32_t)s_cnt[f];
-                const uint32_t q = t / c;
-                int d = (int)(t - q * c) + s_dig0[f] + carry;
-                t = q;
-                carry = d >= (int)c;
-                if (carry) d -= (int)c;
+                uint32_t d;
+                if (rem >> 32) {
+                    d = (uint32_t)(rem % c);
+                    rem /= c;
+                } else {
+                    const uint32_t q = (uint32_t)rem / c;
+                    d = (uint32_t)rem - q * c;
+                    rem = q;
+                }
                 const float4* tp = s_C + s_coff[f] + d * NP;
 #pragma unroll
                 for (int p = 0; p < NP; ++p) {
@@ -258,10 +259,11 @@ __global__ void __launch_bounds__(kScanThreads) ux_scan_kernel(ScanArgs a) {
             }
         }
         const uint64_t rank0 = pidx * (uint64_t)scount;
-        const float inf = __int_as_float(0x7f800000);
-        for (uint32_t j = 0; j < scount; ++j) {
+        const float init = active ? 0.f : __int_as_float(0x7f800000);
+        // max p over the varying bins of prefix + suffix j
+        auto eval = [&](uint32_t j) {
             const float4* S = s_S + j * NP;
-            float m0 = active ? 0.f : inf, m1 = m0;
+            float m0 = init, m1 = init;
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
                 const float4 s = S[p];
@@ -273,42 +275,54 @@ __global__ void __launch_bounds__(kScanThreads) ux_scan_kernel(ScanArgs a) {
                 else
                     m0 = max3f(m0, q.x, q.y);
             }
-            const float m = fmaxf(m0, m1);
+            return fmaxf(m0, m1);
+        };
+        // survivors (sure passes) and the band around the bound (unsure),
+        // appended with one atomic per warp and list
+        auto emit = [&](float m, uint32_t j) {
             const bool cand = m <= a.thr_hi;
             const unsigned bal = __ballot_sync(0xFFFFFFFFu, cand);
-            if (bal) {
-                const bool sure = cand && m < a.thr_lo;
-                const unsigned bs = __ballot_sync(0xFFFFFFFFu, sure);
-                const unsigned bu = bal & ~bs;
-                unsigned long long base_s = 0, base_u = 0;
-                if (lane == 0) {
-                    if (bs) {
-                        base_s = atomicAdd(&a.counters[0], (unsigned long long)__popc(bs));
-                        atomicAdd(&a.side_count[side], (uint32_t)__popc(bs));
-                    }
-                    if (bu) base_u = atomicAdd(&a.counters[1], (unsigned long long)__popc(bu));
+            if (!bal) return;
+            const bool sure = cand && m < a.thr_lo;
+            const unsigned bs = __ballot_sync(0xFFFFFFFFu, sure);
+            const unsigned bu = bal & ~bs;
+            unsigned long long base_s = 0, base_u = 0;
+            if (lane == 0) {
+                if (bs) {
+                    base_s = atomicAdd(&a.counters[0], (unsigned long long)__popc(bs));
+                    atomicAdd(&a.side_count[side], (uint32_t)__popc(bs));
                 }
-                base_s = __shfl_sync(0xFFFFFFFFu, base_s, 0);
-                base_u = __shfl_sync(0xFFFFFFFFu, base_u, 0);
-                if (cand) {
-                    const unsigned lt = (1u << lane) - 1u;
-                    const uint64_t val = ((uint64_t)side << kRankBits) | (rank0 + j);
-                    if (sure) {
-                        const unsigned long long pos = base_s + __popc(bs & lt);
-                        if (pos < a.surv_cap)
-                            a.surv[pos] = val;
-                        else
-                            flag_overflow(a.status);
-                    } else {
-                        const unsigned long long pos = base_u + __popc(bu & lt);
-                        if (pos < a.unsure_cap)
-                            a.unsure[pos] = val;
-                        else
-                            flag_overflow(a.status);
-                    }
+                if (bu) base_u = atomicAdd(&a.counters[1], (unsigned long long)__popc(bu));
+            }
+            base_s = __shfl_sync(0xFFFFFFFFu, base_s, 0);
+            base_u = __shfl_sync(0xFFFFFFFFu, base_u, 0);
+            if (cand) {
+                const unsigned lt = (1u << lane) - 1u;
+                const uint64_t val = ((uint64_t)side << kRankBits) | (rank0 + j);
+                if (sure) {
+                    const unsigned long long pos = base_s + __popc(bs & lt);
+                    if (pos < a.surv_cap)
+                        a.surv[pos] = val;
+                    else
+                        flag_overflow(a.status);
+                } else {
+                    const unsigned long long pos = base_u + __popc(bu & lt);
+                    if (pos < a.unsure_cap)
+                        a.unsure[pos] = val;
+                    else
+                        flag_overflow(a.status);
                 }
             }
+        };
+        uint32_t j = 0;
+        for (; j + 2 <= scount; j += 2) {  // two independent suffixes per step
+            const float ma = eval(j), mb = eval(j + 1);
+            if (__any_sync(0xFFFFFFFFu, ma <= a.thr_hi || mb <= a.thr_hi)) {
+                emit(ma, j);
+                emit(mb, j + 1);
+            }
         }
+        if (j < scount) emit(eval(j), j);
     }
 }
 
@@ -728,6 +742,8 @@ struct Side {
     uint64_t total = 0;         // expansions (0: none can pass)
     uint64_t prefix_count = 0;
     uint32_t nsuf = 0;
+    uint32_t suffix_count = 1;  // combinations in the suffix table
+    uint32_t free_choices = 0;  // choices summed over the free positions (the scan's term table)
 };
 
 // src/core/uncompression/uncompression.cpp:107-142: rotation, rows, sizes.
@@ -787,6 +803,8 @@ int plan_side(gp_ctx* c, const Level& lv, std::vector<int> orig, Side& sd) {
         ++nsuf;
     }
     sd.nsuf = nsuf;
+    sd.suffix_count = sc;
+    for (int n : free_cnt) sd.free_choices += (uint32_t)n;
     sd.prefix_count = total / sc;
     return GP_OK;
 }
@@ -1196,8 +1214,15 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
     if (npairs) rc = upload_level(c, lv, ld, s);
     Batcher bt{c, lv, ld, sides, s, scan_kernel_for(lv.np)};
     if (!rc && npairs) {
-        const size_t ctab_bytes = (size_t)lv.L * lv.dmax * lv.np * 16;
-        bt.smem = (size_t)lv.smax * lv.np * 16 + ctab_bytes;
+        // shared memory of the scan: the largest suffix table and term table
+        // any side of this call needs (a few tens of KB: several CTAs per SM)
+        uint64_t max_sc = 1, max_fc = 0;
+        for (const Side& sd : sides) {
+            if (!sd.total) continue;
+            max_sc = std::max<uint64_t>(max_sc, sd.suffix_count);
+            max_fc = std::max<uint64_t>(max_fc, sd.free_choices);
+        }
+        bt.smem = (size_t)(max_sc + max_fc) * lv.np * 16;
         cudaError_t e = cudaFuncSetAttribute(bt.scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt.smem);
         int per_sm = 0;
         if (e == cudaSuccess)
