@@ -458,7 +458,14 @@ def generation_extras(gp, ctx, peaks):
         # and 16 of 1000 jobs of the order-57 split, one process per item
         cores = os.cpu_count() or 1
         subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
-        sample = [("window",) + tuple(w) for w in batch_windows(1 << 26)]
+        # each 2^26-word window cut into `cores` equal rank ranges, so that
+        # every core has work
+        sample = []
+        for (o, c, p, lo, hi) in batch_windows(1 << 26):
+            for k in range(cores):
+                a, b = lo + (hi - lo) * k // cores, lo + (hi - lo) * (k + 1) // cores
+                if a < b:
+                    sample.append(("window", o, c, p, a, b))
         with mp.get_context("spawn").Pool(min(cores, len(sample))) as pool:
             t0 = time.perf_counter()
             res = pool.map(_oracle_gen_job, sample)
@@ -472,7 +479,7 @@ def generation_extras(gp, ctx, peaks):
             "kind": "port", "cores": cores,
             "uneven_batch_2^26_windows": {"seconds": wel, "necklaces_per_s": sum(r[0] for r in res) / wel,
                                           "candidates_per_s": sum(r[1] for r in res) / wel,
-                                          "processes": len(sample)},
+                                          "jobs": len(sample), "processes": min(cores, len(sample))},
             "order57_16_of_1000_jobs": {"seconds": sel, "necklaces_per_s": sum(r[0] for r in res57) / sel,
                                         "candidates_per_s": sum(r[1] for r in res57) / sel,
                                         "processes": len(shards)},
