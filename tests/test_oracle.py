@@ -21,7 +21,7 @@ def run_oracle(oracle_bin, tmp_path, argv):
     return os.path.join(d, f"order-{argv[0]}")
 
 
-@pytest.mark.parametrize("name", ["n16", "n26"])
+@pytest.mark.parametrize("name", ["n16", "n26", "n21_c31", "n27_c31"])
 def test_oracle_full_pipeline_matches_reference(oracle_bin, tmp_path, golden_manifest, name):
     rec = golden_manifest["runs"][name]
     wd = run_oracle(oracle_bin, tmp_path, rec["argv"])
@@ -31,7 +31,7 @@ def test_oracle_full_pipeline_matches_reference(oracle_bin, tmp_path, golden_man
         assert got.count(b"\n") == meta["lines"]
 
 
-@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000"])
+@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000", "n33_c31"])
 def test_oracle_generation_matches_reference_hash(oracle_bin, tmp_path, golden_manifest, name):
     rec = golden_manifest["runs"][name]
     wd = run_oracle(oracle_bin, tmp_path, rec["argv"])

@@ -35,7 +35,7 @@ def golay(args, tmp, check=True):
     return r, os.path.join(d, f"order-{args[0]}")
 
 
-@pytest.mark.parametrize("name", ["n16", "n26"])
+@pytest.mark.parametrize("name", ["n16", "n26", "n21_c31", "n27_c31"])
 def test_all_matches_reference(tmp_path, golden_manifest, name):
     rec = golden_manifest["runs"][name]
     _, wd = golay(rec["argv"], tmp_path)
@@ -45,10 +45,12 @@ def test_all_matches_reference(tmp_path, golden_manifest, name):
         assert got == want, fn
 
 
-@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000", "n32_c421"])
+@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000", "n32_c421", "n33_c31", "n39_c31"])
 def test_gen_matches_reference_hash(tmp_path, golden_manifest, name):
     """Hashes of the reference's own outputs; n32_c421 runs generation at
-    compression 4 and uncompresses 4 -> 2 -> 1 (90,320 pairs at length 32)."""
+    compression 4 and uncompresses 4 -> 2 -> 1 (90,320 pairs at length 32);
+    n33_c31 and n39_c31 run the whole pipeline for Legendre-type pairs at
+    compression 3 -> 1 (9,370 pairs of length 39, 2,318 classes)."""
     rec = golden_manifest["runs"][name]
     r, wd = golay(rec["argv"], tmp_path)
     for fn, meta in rec["files"].items():
@@ -169,6 +171,37 @@ def _filter_gpu_vs_oracle(oracle_lib, tmp_path, order, pairs_file):
     got, want = read(tmp_path / "gpu"), read(tmp_path / "orc")
     assert got == want
     return got
+
+
+N57 = ["57", "-c", "3", "1", "--paf", "-2"]
+
+
+def test_order57_compression3_matches_reference(tmp_path, golden_manifest):
+    """Order 57, paf -2, compression 3 -> 1 (Legendre-type pairs): gen, sort
+    and match over the whole word space give the reference's sorted files
+    (366,602 a / 3,299,242 b lines) and its 196,216-line pair file; the
+    uncompression to length 57 and the equivalence filter of two 200-line
+    subsets of that pair file (its first 200 lines, and 200 lines drawn with
+    a fixed seed) give the reference's compression-1 pairs and unique pairs
+    (the reference's outputs, produced by tests/golden/make_golden.py)."""
+    if "n57" not in golden_manifest:
+        pytest.skip("order-57 goldens not generated yet (tests/golden/make_golden.py --n57)")
+    rec = golden_manifest["n57"]
+    _, wd = golay(N57 + ["gen", "sort", "match"], tmp_path / "full")
+    for fn, meta in rec["files"].items():
+        got = read(os.path.join(wd, fn))
+        assert got.count(b"\n") == meta["lines"], fn
+        assert hashlib.sha256(got).hexdigest() == meta["sha256"], fn
+    lines = read(os.path.join(wd, "57-pairs-3")).splitlines(keepends=True)
+    for name, sub in rec["subsets"].items():
+        d = tmp_path / name / "order-57"
+        d.mkdir(parents=True)
+        (d / "57-pairs-3").write_bytes(b"".join(lines[i] for i in sub["indices"]))
+        _, swd = golay(N57 + ["uncompress", "filter"], tmp_path / name)
+        for fn, meta in sub["files"].items():
+            got = read(os.path.join(swd, fn))
+            assert got.count(b"\n") == meta["lines"], (name, fn)
+            assert hashlib.sha256(got).hexdigest() == meta["sha256"], (name, fn)
 
 
 def test_filter_n32_matches_oracle(oracle_lib, tmp_path, golden_manifest):
