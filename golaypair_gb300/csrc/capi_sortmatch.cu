@@ -425,6 +425,205 @@ int gp_sort_text(gp_ctx* c, const std::string& text, std::string& out) {
     return GP_OK;
 }
 
+// ------------------------------------------------ binary survivor inputs
+// Every input a binary survivor file of one job: the records go to the
+// device as they are, the device formats their lines (the text the
+// generation call would have written, survivors.h), sorts them with the
+// same keys as text input and gathers the kept lines in order; the host
+// only reads the files and writes the sorted text.
+
+struct SurvGeom {
+    int L, bits, k, sig_bytes, word_bytes, rec_bytes;
+    int alpha[16];
+};
+
+__device__ __forceinline__ int ndigits_u(unsigned v) {
+    int n = 1;
+    while (v >= 10) {
+        v /= 10;
+        ++n;
+    }
+    return n;
+}
+
+__device__ __forceinline__ void rec_word(const uint8_t* r, int word_bytes, uint64_t& lo, uint64_t& hi) {
+    lo = hi = 0;
+    for (int i = 0; i < word_bytes; ++i) {
+        const uint64_t b = r[i];
+        if (i < 8)
+            lo |= b << (8 * i);
+        else
+            hi |= b << (8 * (i - 8));
+    }
+}
+
+__device__ __forceinline__ int rec_digit(uint64_t lo, uint64_t hi, int bits, int L, int j) {
+    const int pos = bits * (L - 1 - j);
+    const uint64_t m = (1ull << bits) - 1ull;
+    if (pos >= 64) return (int)((hi >> (pos - 64)) & m);
+    uint64_t v = lo >> pos;
+    if (pos + bits > 64 && pos > 0) v |= hi << (64 - pos);
+    return (int)(v & m);
+}
+
+__device__ __forceinline__ unsigned rec_sig(const uint8_t* r, const SurvGeom& g, int k) {
+    const uint8_t* s = r + g.word_bytes;
+    return g.sig_bytes == 1 ? s[k] : (unsigned)(s[2 * k] | (s[2 * k + 1] << 8));
+}
+
+// line length (newline included) of every record; a digit past the
+// alphabet or bits above the word make the input malformed
+__global__ void surv_len_kernel(const uint8_t* recs, int64_t n, SurvGeom g, uint32_t* len, unsigned* maxlen,
+                                int* bad) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t* r = recs + i * g.rec_bytes;
+        uint64_t lo, hi;
+        rec_word(r, g.word_bytes, lo, hi);
+        const int used = g.bits * g.L;
+        const bool high = used < 64 ? (lo >> used) != 0 || hi != 0 : (used < 128 && (hi >> (used - 64)) != 0);
+        uint32_t l = 3 + 1 + 1;  // "PSD", the space after the signature, the newline
+        for (int k = 0; k < g.L - 1; ++k) l += (uint32_t)ndigits_u(rec_sig(r, g, k));
+        bool ok = !high;
+        for (int j = 0; j < g.L; ++j) {
+            const int d = rec_digit(lo, hi, g.bits, g.L, j);
+            if (d >= g.k) {
+                ok = false;
+                break;
+            }
+            const int v = g.alpha[d];
+            l += (uint32_t)(ndigits_u((unsigned)(v < 0 ? -v : v)) + (v < 0) + 1);
+        }
+        if (!ok) atomicExch(bad, 1);
+        len[i] = l;
+        atomicMax(maxlen, l - 1);
+    }
+}
+
+__device__ __forceinline__ char* put_dec(char* o, unsigned v) {
+    char tmp[10];
+    int n = 0;
+    do {
+        tmp[n++] = (char)('0' + v % 10);
+        v /= 10;
+    } while (v);
+    while (n) *o++ = tmp[--n];
+    return o;
+}
+
+// each record's line (src/utils/io.cpp:14-36) at its offset
+__global__ void surv_format_kernel(const uint8_t* recs, int64_t n, SurvGeom g, const uint32_t* off, char* text,
+                                   uint64_t* start, uint32_t* len) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t* r = recs + i * g.rec_bytes;
+        uint64_t lo, hi;
+        rec_word(r, g.word_bytes, lo, hi);
+        char* o = text + off[i];
+        char* const o0 = o;
+        *o++ = 'P';
+        *o++ = 'S';
+        *o++ = 'D';
+        for (int k = 0; k < g.L - 1; ++k) o = put_dec(o, rec_sig(r, g, k));
+        *o++ = ' ';
+        for (int j = 0; j < g.L; ++j) {
+            const int v = g.alpha[rec_digit(lo, hi, g.bits, g.L, j)];
+            if (v < 0) *o++ = '-';
+            o = put_dec(o, (unsigned)(v < 0 ? -v : v));
+            *o++ = ' ';
+        }
+        *o = '\n';
+        start[i] = off[i];
+        len[i] = (uint32_t)(o - o0);  // without the newline, as the text path's line lengths
+    }
+}
+
+__global__ void gather_len_kernel(const uint32_t* len, const uint32_t* order, int64_t n, uint32_t* out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = len[order[i]] + 1;
+}
+
+// one warp per kept line: its bytes and newline at the line's output offset
+__global__ void gather_lines_kernel(const char* text, const uint64_t* start, const uint32_t* len,
+                                    const uint32_t* order, const uint32_t* out_off, int64_t n, char* out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t k = w0; k < n; k += nw) {
+        const uint32_t i = order[k];
+        const char* src = text + start[i];
+        char* dst = out + out_off[k];
+        const uint32_t l = len[i] + 1;  // the newline follows the line in the formatted text
+        for (uint32_t c = lane; c < l; c += 32) dst[c] = src[c];
+    }
+}
+
+// Sorted, de-duplicated lines of the records (all of one geometry).
+// Returns GP_ERR_FORMAT on a malformed record.
+int gp_sort_records(gp_ctx* c, const SurvGeom& g, const std::vector<uint8_t>& recs, int64_t n, std::string& out) {
+    out.clear();
+    if (n == 0) return GP_OK;
+    cudaStream_t s = c->s_comp;
+    DevBuf dr, dl, dlen2, doff, dscan, dmisc, dt, ds, dk, di, dtmp, dflag, dpos, dord, dooff, dout;
+    if (!dr.ensure(recs.size() + 16) || !dl.ensure(n * 4 + 4) || !doff.ensure(n * 4 + 4) ||
+        !dscan.ensure(gp::scan_tmp_bytes(n)) || !dmisc.ensure(64) || !ds.ensure(n * 8))
+        return c->fail(GP_ERR_NOMEM, "sort: device allocation");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dr.p, recs.data(), recs.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemsetAsync(dmisc.p, 0, 64, s));
+    unsigned* d_maxlen = dmisc.as<unsigned>();
+    int* d_bad = dmisc.as<int>() + 1;
+    surv_len_kernel<<<grid_for(n), 256, 0, s>>>(dr.as<uint8_t>(), n, g, dl.as<uint32_t>(), d_maxlen, d_bad);
+    GP_CUDA_TRY(c, cudaGetLastError());
+    GP_CUDA_TRY(c, gp::exclusive_scan_u32(dl.as<uint32_t>(), doff.as<uint32_t>(), n, dscan.as<uint32_t>(), s));
+    uint32_t last_off = 0, last_len = 0;
+    unsigned hm[2] = {0, 0};
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&last_off, doff.as<uint32_t>() + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&last_len, dl.as<uint32_t>() + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(hm, dmisc.p, 8, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    if (hm[1]) return c->fail(GP_ERR_FORMAT, "sort: malformed survivor record");
+    const uint64_t total = (uint64_t)last_off + last_len;
+    if (total >= (uint64_t(1) << 32)) return c->fail(GP_ERR_UNSUPPORTED, "sort: %llu bytes of lines", (unsigned long long)total);
+    const int Wk = std::max(1, (int)((hm[0] + 7) / 8));
+    if (!dt.ensure(total + 16) || !dk.ensure((size_t)n * Wk * 4) || !di.ensure(n * 4) ||
+        !dtmp.ensure(gp::radix_sort_tmp_bytes(n)) || !dflag.ensure(n * 4) || !dpos.ensure(n * 4) ||
+        !dord.ensure(n * 4 + 4) || !dlen2.ensure(n * 4) || !dooff.ensure(n * 4))
+        return c->fail(GP_ERR_NOMEM, "sort: device allocation");
+    surv_format_kernel<<<grid_for(n), 256, 0, s>>>(dr.as<uint8_t>(), n, g, doff.as<uint32_t>(), dt.as<char>(),
+                                                   ds.as<uint64_t>(), dl.as<uint32_t>());
+    build_keys_kernel<<<grid_for(n), 256, 0, s>>>(dt.as<char>(), ds.as<uint64_t>(), dl.as<uint32_t>(), n, Wk, 1,
+                                                  dk.as<uint32_t>());
+    GP_CUDA_TRY(c, cudaGetLastError());
+    int bits = 8;
+    int rc = sort_radix_bits(c, dk.as<uint32_t>(), Wk, n, di.as<uint32_t>(), dtmp.p, s, &bits);
+    if (rc) return rc;
+    GP_CUDA_TRY(c, gp::iota_u32(di.as<uint32_t>(), n, s));
+    GP_CUDA_TRY(c, gp::radix_sort_keys(dk.as<uint32_t>(), Wk, Wk, di.as<uint32_t>(), n, dtmp.p, s, bits));
+    GP_CUDA_TRY(c, gp::mark_unique(dk.as<uint32_t>(), Wk, di.as<uint32_t>(), n, Wk, dflag.as<uint32_t>(), s));
+    uint32_t* d_cnt = dord.as<uint32_t>() + n;
+    GP_CUDA_TRY(c, gp::compact_flags(dflag.as<uint32_t>(), di.as<uint32_t>(), dord.as<uint32_t>(), n,
+                                     dpos.as<uint32_t>(), dscan.as<uint32_t>(), d_cnt, s));
+    uint32_t nu = 0;
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&nu, d_cnt, 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    if (nu == 0) return GP_OK;
+    gather_len_kernel<<<grid_for(nu), 256, 0, s>>>(dl.as<uint32_t>(), dord.as<uint32_t>(), nu, dlen2.as<uint32_t>());
+    GP_CUDA_TRY(c, cudaGetLastError());
+    GP_CUDA_TRY(c, gp::exclusive_scan_u32(dlen2.as<uint32_t>(), dooff.as<uint32_t>(), nu, dscan.as<uint32_t>(), s));
+    uint32_t o_last = 0, l_last = 0;
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&o_last, dooff.as<uint32_t>() + nu - 1, 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&l_last, dlen2.as<uint32_t>() + nu - 1, 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    const uint64_t out_bytes = (uint64_t)o_last + l_last;
+    if (!dout.ensure(out_bytes + 16)) return c->fail(GP_ERR_NOMEM, "sort: device allocation");
+    gather_lines_kernel<<<(unsigned)std::min<int64_t>((nu + 7) / 8, 65535 * 8), 256, 0, s>>>(
+        dt.as<char>(), ds.as<uint64_t>(), dl.as<uint32_t>(), dord.as<uint32_t>(), dooff.as<uint32_t>(), nu,
+        dout.as<char>());
+    GP_CUDA_TRY(c, cudaGetLastError());
+    out.resize(out_bytes);
+    GP_CUDA_TRY(c, cudaMemcpyAsync(&out[0], dout.p, out_bytes, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    return GP_OK;
+}
+
 extern "C" {
 
 int gp_tuned_settings(const gp_ctx* c, char* buf, int cap) {
@@ -448,6 +647,46 @@ int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
     if (!c || (!in_paths && n_in > 0) || !out_path) return GP_ERR_ARG;
     cudaSetDevice(c->device);
     std::string all, one;
+    {
+        // all inputs binary survivor files of one job: the records are
+        // formatted and sorted on the device
+        std::vector<uint8_t> recs;
+        SurvGeom g{};
+        int64_t n = 0;
+        bool binary = n_in > 0;
+        gp::SurvHeader h0{};
+        for (int i = 0; i < n_in && binary; ++i) {
+            if (!slurp(in_paths[i], one)) return c->fail(GP_ERR_IO, "sort: cannot read %s", in_paths[i]);
+            gp::SurvHeader h;
+            const uint8_t* body = nullptr;
+            const int kind = gp::surv_parse(one, h, &body);
+            if (kind < 0) return c->fail(GP_ERR_FORMAT, "sort: malformed survivor file %s", in_paths[i]);
+            if (kind == 0 || (i > 0 && (h.L != h0.L || h.bits != h0.bits || h.k != h0.k || h.sig_bytes != h0.sig_bytes ||
+                                        std::memcmp(h.alpha, h0.alpha, 16) != 0))) {
+                binary = false;
+                break;
+            }
+            if (i == 0) h0 = h;
+            recs.insert(recs.end(), body, body + h.count * gp::surv_record_bytes(h));
+            n += (int64_t)h.count;
+        }
+        if (binary) {
+            g.L = h0.L;
+            g.bits = h0.bits;
+            g.k = h0.k;
+            g.sig_bytes = h0.sig_bytes;
+            g.word_bytes = h0.word_bytes;
+            g.rec_bytes = (int)gp::surv_record_bytes(h0);
+            for (int a = 0; a < 16; ++a) g.alpha[a] = h0.alpha[a];
+            std::string sorted;
+            int rc = gp_sort_records(c, g, recs, n, sorted);
+            if (rc) return rc;
+            FILE* f = fopen(out_path, "w");
+            if (!f) return c->fail(GP_ERR_IO, "sort: cannot write %s", out_path);
+            fwrite(sorted.data(), 1, sorted.size(), f);
+            return fclose(f) == 0 ? GP_OK : c->fail(GP_ERR_IO, "sort: write failed");
+        }
+    }
     for (int i = 0; i < n_in; ++i) {
         if (!slurp(in_paths[i], one)) return c->fail(GP_ERR_IO, "sort: cannot read %s", in_paths[i]);
         gp::SurvHeader h;
