@@ -194,6 +194,15 @@ def make_batch(torch, rows, device, seed=0):
     return out
 
 
+def read_profile_record(name):
+    """A machine-readable ncu record under profiles/ (None when absent)."""
+    p = os.path.join(REPO, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
+
+
 def read_profile_traffic():
     """DRAM bytes per row of the filter kernel, from the machine-readable
     record of its ncu capture (profiles/psd_tc_L45.json)."""
@@ -427,7 +436,8 @@ def generation_extras(gp, ctx, peaks):
             "tensor_pipe": {"algorithmic_tflops": flops / el / 1e12, "peak_tflops": bf16,
                             "frac": flops / el / 1e12 / bf16,
                             "note": "algorithmic PSD flops of the candidates over the whole engine run; the "
-                                    "enumerator (integer issue) takes most of the device time"}}
+                                    "enumerator (integer issue) takes most of the device time"},
+            "enumerator_issue": read_profile_record("enumerate_batch.json")}
         cli = gp.CLI_PATH
         d = os.path.join(tmp, "r57")
         base = [cli, "57", "-c", "3", "1", "--paf", "-2", "--dir", d]
