@@ -947,8 +947,11 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     out.assign(np_, {});
     if (units == 0) return GP_OK;
     // capacities: every expansion could pass at small sizes; at large ones
-    // a pass rate of 1/8 (order 57: under 1 %); unsure 1/64 of that
-    const uint64_t surv_cap = std::max<uint64_t>(1024, std::min<uint64_t>(total, std::max<uint64_t>(total / 8, 1 << 20)));
+    // a pass rate of 1/8 (order 57: under 1 %), at most 2^30 survivors (8 GB;
+    // the join packs survivor indices into 31 bits); unsure 1/64 of that.
+    // A batch that overflows is split in two and run again.
+    const uint64_t surv_cap = std::max<uint64_t>(
+        1024, std::min<uint64_t>(uint64_t(1) << 30, std::min<uint64_t>(total, std::max<uint64_t>(total / 8, 1 << 20))));
     const uint64_t unsure_cap = std::max<uint64_t>(1024, surv_cap / 64);
     DevBuf &drows = c->ux[4], &dubeg = c->ux[5], &dpcnt = c->ux[6], &dnsuf = c->ux[7], &dcnt = c->ux[8],
            &dsurv = c->ux[9], &duns = c->ux[10], &dside = c->ux[11];
