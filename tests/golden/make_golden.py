@@ -16,6 +16,7 @@ Boost headers) into oracle/_ref/golay_ref, runs it under LC_ALL=C, and stores:
 * n21_c31/, n27_c31/ -- the sorted, pair and unique files of
   `main N -c 3 1 --paf -2 all` (Legendre-type pairs, odd compression 3 -> 1;
   verbatim), and hashes of the same runs at orders 33 and 39;
+* hashes of order 36 at compression 6: the chain 6 -> 3 -> 1 and 6 -> 1;
 * manifest.json "n57" -- order 57, paf -2, compression 3 -> 1 in full:
   `gen` over 8 jobs (-n 8 -j 0..7, run in parallel), `sort`, `match`
   (hashes of the sorted files and of the 196,216-line pair file), then the
@@ -68,6 +69,11 @@ RUNS = [
     (f"n{n}_c31", [str(n), "-c", "3", "1", "--paf", "-2", "all"],
      [f"{n}-filtered_sorted-a", f"{n}-filtered_sorted-b", f"{n}-pairs-3", f"{n}-pairs-1", f"{n}-unique"], n < 30)
     for n in (21, 27, 33, 39)
+] + [
+    # compression 6: the chain 6 -> 3 -> 1 (ratio 2 into the odd alphabet, then 3) and 6 -> 1 directly
+    ("n36_c631", ["36", "-c", "6", "3", "1", "gen", "sort", "match", "uncompress"],
+     ["36-filtered_sorted-a", "36-filtered_sorted-b", "36-pairs-6", "36-pairs-3", "36-pairs-1"], False),
+    ("n36_c61", ["36", "-c", "6", "1", "gen", "sort", "match", "uncompress"], ["36-pairs-6", "36-pairs-1"], False),
 ]
 N57_ARGV = ["57", "-c", "3", "1", "--paf", "-2"]
 N57_JOBS = 8

@@ -45,12 +45,15 @@ def test_all_matches_reference(tmp_path, golden_manifest, name):
         assert got == want, fn
 
 
-@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000", "n32_c421", "n33_c31", "n39_c31"])
+@pytest.mark.parametrize("name", ["n34", "n57_shard7of1000", "n32_c421", "n33_c31", "n39_c31", "n36_c631", "n36_c61"])
 def test_gen_matches_reference_hash(tmp_path, golden_manifest, name):
     """Hashes of the reference's own outputs; n32_c421 runs generation at
     compression 4 and uncompresses 4 -> 2 -> 1 (90,320 pairs at length 32);
     n33_c31 and n39_c31 run the whole pipeline for Legendre-type pairs at
-    compression 3 -> 1 (9,370 pairs of length 39, 2,318 classes)."""
+    compression 3 -> 1 (9,370 pairs of length 39, 2,318 classes); n36_c631
+    uncompresses order 36 from compression 6 to 3 (2,309 pairs over the
+    alphabet +-1, +-3) and on to 1, n36_c61 from 6 to 1 directly (up to 20
+    partitions per entry)."""
     rec = golden_manifest["runs"][name]
     r, wd = golay(rec["argv"], tmp_path)
     for fn, meta in rec["files"].items():
