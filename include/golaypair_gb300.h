@@ -303,11 +303,13 @@ int gp_match(gp_ctx* ctx, int order, int compress, int paf, const char* path_a, 
  * const std::string& prefix, DeviceType) (src/core/uncompression/
  * uncompression.h:19-29, uncompression.cpp:32-79) for both of its devices:
  * every pair of in_pairs (compression c) is expanded to compression c_new,
- * PSD-filtered, sorted and matched; the pairs are written to out_pairs in
- * input order.  Candidate files of each pair stay in device memory (the
- * reference's uncompress_tmp_* scratch files are not written; work_dir and
- * prefix are accepted for interface parity).  A line with the wrong number
- * of values is GP_ERR_FORMAT (the reference throws, io.cpp:52-55).
+ * PSD-filtered and matched; the pairs are written to out_pairs in input
+ * order, in the order the reference's sorted scratch files give them.
+ * Many pairs are processed per batch on the device; the candidates never
+ * leave it (the reference's uncompress_tmp_* scratch files are not written;
+ * work_dir and prefix are accepted for interface parity).  A line with the
+ * wrong number of values is GP_ERR_FORMAT (the reference throws,
+ * io.cpp:52-55); the pairs of the lines before it are still written.
  */
 int gp_uncompress(gp_ctx* ctx, int order, int compress, int new_compress, int paf, const char* in_pairs,
                   const char* out_pairs, const char* work_dir, const char* prefix);
