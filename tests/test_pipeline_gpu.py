@@ -187,8 +187,6 @@ def test_order57_compression3_matches_reference(tmp_path, golden_manifest):
     subsets of that pair file (its first 200 lines, and 200 lines drawn with
     a fixed seed) give the reference's compression-1 pairs and unique pairs
     (the reference's outputs, produced by tests/golden/make_golden.py)."""
-    if "n57" not in golden_manifest:
-        pytest.skip("order-57 goldens not generated yet (tests/golden/make_golden.py --n57)")
     rec = golden_manifest["n57"]
     _, wd = golay(N57 + ["gen", "sort", "match"], tmp_path / "full")
     for fn, meta in rec["files"].items():
