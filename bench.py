@@ -362,7 +362,10 @@ def run_gpu(args):
         }
         line["cpu_baseline"] = cpu_baseline(cpu_rows)
         if ws == 1 and not args.no_extras:
-            line["generation"] = generation_extras(gp, ctx, peaks)
+            try:  # the headline stands even if a generation figure cannot be taken
+                line["generation"] = generation_extras(gp, ctx, peaks)
+            except Exception as e:  # noqa: BLE001 -- reported in the line, not raised
+                line["generation"] = {"error": f"{type(e).__name__}: {e}"}
         print(json.dumps(line))
     ctx.close()
     if ws > 1:
