@@ -471,10 +471,10 @@ def generation_extras(gp, ctx, peaks):
         # and 16 of 1000 jobs of the order-57 split, one process per item
         cores = os.cpu_count() or 1
         subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
-        # each 2^26-word window cut into `cores` equal rank ranges, so that
+        # each 2^28-word window cut into `cores` equal rank ranges, so that
         # every core has work
         sample = []
-        for (o, c, p, lo, hi) in batch_windows(1 << 26):
+        for (o, c, p, lo, hi) in batch_windows(1 << 28):
             for k in range(cores):
                 a, b = lo + (hi - lo) * k // cores, lo + (hi - lo) * (k + 1) // cores
                 if a < b:
@@ -490,7 +490,7 @@ def generation_extras(gp, ctx, peaks):
             sel = time.perf_counter() - t0
         out["cpu_pipeline"] = {
             "kind": "port", "cores": cores,
-            "uneven_batch_2^26_windows": {"seconds": wel, "necklaces_per_s": sum(r[0] for r in res) / wel,
+            "uneven_batch_2^28_windows": {"seconds": wel, "necklaces_per_s": sum(r[0] for r in res) / wel,
                                           "candidates_per_s": sum(r[1] for r in res) / wel,
                                           "jobs": len(sample), "processes": min(cores, len(sample))},
             "order57_16_of_1000_jobs": {"seconds": sel, "necklaces_per_s": sum(r[0] for r in res57) / sel,
