@@ -467,7 +467,7 @@ def generation_extras(gp, ctx, peaks):
             "match_pairs_per_s": len(p3) / times["match"],
             "filter_pairs_per_s": nlines["57-pairs-1"] / times["filter"],
             "note": "process wall times of the golay driver, context creation and file I/O included"}
-        # the oracle on the host cores: the batch's windows cut to 2^26 words,
+        # the oracle on the host cores: the batch's windows cut to 2^28 words,
         # and 16 of 1000 jobs of the order-57 split, one process per item
         cores = os.cpu_count() or 1
         subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
