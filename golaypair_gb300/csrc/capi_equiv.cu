@@ -18,6 +18,7 @@
 // reference's in-order erase loop (filter.cpp:117-144) on those class sizes
 // and member lists.
 #include <algorithm>
+#include <stdexcept>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -353,7 +354,7 @@ int64_t gp_debug_pair_generator_count(int L, int compress) {
     return (int64_t)(pair_generators(L, compress).size() / (size_t)(2 * L));
 }
 
-int gp_equiv_filter(gp_ctx* c, int order, int compress, const char* in_path, const char* out_path) {
+static int gp_equiv_filter_impl(gp_ctx* c, int order, int compress, const char* in_path, const char* out_path) {
     StageRange nvtx_range("gp_equiv_filter");
     if (!c || !in_path || !out_path) return GP_ERR_ARG;
     if (compress < 1 || order % compress) return c->fail(GP_ERR_ARG, "order %d not divisible by %d", order, compress);
@@ -509,6 +510,15 @@ int gp_equiv_filter(gp_ctx* c, int order, int compress, const char* in_path, con
         fclose(out);
     }
     return GP_OK;
+}
+
+// No C++ exception (an allocation failure on a huge input) crosses the C ABI.
+int gp_equiv_filter(gp_ctx* c, int order, int compress, const char* in_path, const char* out_path) {
+    try {
+        return gp_equiv_filter_impl(c, order, compress, in_path, out_path);
+    } catch (const std::exception& e) {
+        return c ? c->fail(GP_ERR_NOMEM, "equivalence filter: %s", e.what()) : GP_ERR_NOMEM;
+    }
 }
 
 }  // extern "C"

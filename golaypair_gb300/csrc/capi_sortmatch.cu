@@ -15,6 +15,7 @@
 // vectors.  Pairs are written in the reference's order: token order, then A
 // line order, then B line order.
 #include <algorithm>
+#include <stdexcept>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -642,7 +643,7 @@ int gp_tuned_settings(const gp_ctx* c, char* buf, int cap) {
     return (int)t.size() + 1;
 }
 
-int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
+static int gp_sort_impl(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
     StageRange nvtx_range("gp_sort");
     if (!c || (!in_paths && n_in > 0) || !out_path) return GP_ERR_ARG;
     cudaSetDevice(c->device);
@@ -707,7 +708,16 @@ int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
     return fclose(f) == 0 ? GP_OK : c->fail(GP_ERR_IO, "sort: write failed");
 }
 
-int gp_match(gp_ctx* c, int order, int compress, int paf, const char* path_a, const char* path_b, const char* out_path,
+// No C++ exception (an allocation failure on a huge input) crosses the C ABI.
+int gp_sort(gp_ctx* c, const char** in_paths, int n_in, const char* out_path) {
+    try {
+        return gp_sort_impl(c, in_paths, n_in, out_path);
+    } catch (const std::exception& e) {
+        return c ? c->fail(GP_ERR_NOMEM, "sort: %s", e.what()) : GP_ERR_NOMEM;
+    }
+}
+
+static int gp_match_impl(gp_ctx* c, int order, int compress, int paf, const char* path_a, const char* path_b, const char* out_path,
              int append, int64_t* n_pairs) {
     StageRange nvtx_range("gp_match");
     if (!c || !path_a || !path_b || !out_path) return GP_ERR_ARG;
@@ -728,6 +738,16 @@ int gp_match(gp_ctx* c, int order, int compress, int paf, const char* path_a, co
     fwrite(out.data(), 1, out.size(), f);
     fclose(f);
     return rc;
+}
+
+// No C++ exception (an allocation failure on a huge input) crosses the C ABI.
+int gp_match(gp_ctx* c, int order, int compress, int paf, const char* path_a, const char* path_b, const char* out_path,
+             int append, int64_t* n_pairs) {
+    try {
+        return gp_match_impl(c, order, compress, paf, path_a, path_b, out_path, append, n_pairs);
+    } catch (const std::exception& e) {
+        return c ? c->fail(GP_ERR_NOMEM, "match: %s", e.what()) : GP_ERR_NOMEM;
+    }
 }
 
 }  // extern "C"

@@ -41,6 +41,7 @@
 //    and the pairs of each input pair are written in the order of the
 //    reference's sorted files (a line, then b line), input pairs in order.
 #include <algorithm>
+#include <stdexcept>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -1131,7 +1132,7 @@ int gp_uncompress(gp_ctx* c, int order, int compress, int new_compress, int paf,
                                INT64_MAX, 1);
 }
 
-int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
+static int gp_uncompress_lines_impl(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
                         const char* out_pairs, const char* work_dir, const char* prefix, int64_t first, int64_t end_line,
                         int64_t step) {
     StageRange nvtx_range("gp_uncompress");
@@ -1278,6 +1279,16 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
     cudaStreamSynchronize(s);
     fclose(out);
     return rc ? rc : format_rc;
+}
+
+// No C++ exception (an allocation failure on a huge input) crosses the C ABI.
+int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs, const char* out_pairs,
+                        const char* work_dir, const char* prefix, int64_t first, int64_t end_line, int64_t step) {
+    try {
+        return gp_uncompress_lines_impl(c, order, compress, new_compress, paf, in_pairs, out_pairs, work_dir, prefix, first, end_line, step);
+    } catch (const std::exception& e) {
+        return c ? c->fail(GP_ERR_NOMEM, "uncompress: %s", e.what()) : GP_ERR_NOMEM;
+    }
 }
 
 }  // extern "C"
