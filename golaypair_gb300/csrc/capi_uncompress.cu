@@ -921,7 +921,7 @@ struct Batcher {
     std::vector<std::vector<std::array<std::string, 3>>> out;
 
     // Runs the batch; on overflow of a device list returns GP_ERR_OVERFLOW
-    // with *split_hint set, so the caller can halve the batch.
+    // with *overflowed set, so the caller can halve the batch.
     int run(int64_t p0, int64_t p1, bool* overflowed);
 };
 
