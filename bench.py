@@ -435,7 +435,8 @@ def generation_extras(gp, ctx, peaks):
         out["uneven_batch"] = {
             "seconds": el, "necklaces": nk, "candidates": cand, "necklaces_per_s": nk / el,
             "candidates_per_s": cand / el, "iterations": cfg.iterations,
-            "tuned": {k: getattr(cfg, k) for k in ("enum_variant", "windows_per_thread", "cand_cap", "tc_ctas_per_sm")},
+            "tuned": {k: getattr(cfg, k) for k in ("enum_variant", "windows_per_thread", "cand_cap", "tc_ctas_per_sm",
+                                                   "multi_launch")},
             "tensor_pipe": {"algorithmic_tflops": flops / el / 1e12, "peak_tflops": bf16,
                             "frac": flops / el / 1e12 / bf16,
                             "note": "algorithmic PSD flops of the candidates over the whole engine run; the "
@@ -531,8 +532,9 @@ def run_pipeline(args):
         # --pipeline-no-graph: default settings with direct launches (for
         # per-kernel profiling, which does not follow graph replays)
         direct = gp.BatchConfig()
-        direct.no_graph = 1
-        tune = not args.pipeline_no_graph
+        direct.no_graph = 1 if args.pipeline_no_graph else 0
+        direct.multi_launch = 1 if args.pipeline_multi_launch else 0
+        tune = not (args.pipeline_no_graph or args.pipeline_multi_launch)
         t0 = time.perf_counter()
         _, cfg = ctx.generate_batch(spec, autotune=tune, config=None if tune else direct)
         tune_el = time.perf_counter() - t0
@@ -545,7 +547,7 @@ def run_pipeline(args):
                           "necklaces_per_s": tot_n / el, "candidates_per_s": tot_c / el,
                           "necklaces": tot_n, "candidates": tot_c, "iterations": cfg.iterations,
                           "tuned": {k: getattr(cfg, k) for k in ("enum_variant", "windows_per_thread", "cand_cap",
-                                                                 "tc_ctas_per_sm")},
+                                                                 "tc_ctas_per_sm", "multi_launch")},
                           "tune_run_seconds": tune_el, "tuner_seconds": cfg.tune_seconds,
                           "per_job": [dict(order=w[0], compress=w[1], written=s.written_a + s.written_b,
                                            necklaces=s.necklaces, candidates=s.candidates, psd_pass=s.psd_pass,
@@ -604,6 +606,8 @@ def main():
                     help="--pipeline: everything, or only the uneven batch in one engine run")
     ap.add_argument("--pipeline-no-graph", action="store_true",
                     help="--pipeline: run the batch engine with direct launches and default settings")
+    ap.add_argument("--pipeline-multi-launch", action="store_true",
+                    help="--pipeline: run the batch engine untuned with one launch per kernel over all jobs")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

@@ -51,7 +51,7 @@ class GenJob(ctypes.Structure):
 class BatchConfig(ctypes.Structure):
     _fields_ = [("enum_variant", ctypes.c_int), ("windows_per_thread", ctypes.c_int), ("cand_cap", ctypes.c_int64),
                 ("tc_ctas_per_sm", ctypes.c_int), ("no_graph", ctypes.c_int), ("iterations", ctypes.c_int),
-                ("tune_seconds", ctypes.c_double)]
+                ("tune_seconds", ctypes.c_double), ("multi_launch", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -163,7 +163,12 @@ struct BatchCfg {
     int64_t cand_cap = int64_t(1) << 22;  // candidates per job per iteration (soft)
     int tc_ctas_per_sm = 0;      // tensor-core filter CTAs per SM (0 = as many as fit)
     int use_graph = 1;
+    // 1: one launch per kernel and iteration over every job (filter,
+    // recheck, listing, finalize); 0: per-job launches on the jobs' own
+    // streams
+    int multi_launch = 0;
 };
+
 
 struct JobRun {
     GenPlan p;
@@ -176,6 +181,13 @@ struct JobRun {
     // set when the engine stopped early: the word ranks still to search
     std::vector<std::pair<gp::u128, gp::u128>> remaining;
 };
+
+// True when one filter launch takes every job (lengths up to 63).
+bool multi_launch_ok(const std::vector<JobRun>& jobs) {
+    for (auto& j : jobs)
+        if (!gp::tc_multi_supported(j.p.L, j.p.b)) return false;
+    return (int)jobs.size() <= gp::kMaxTcJobs;
+}
 
 // Early stop of the engine (checkpointed searches): after an iteration that
 // reaches max_iterations (> 0) or max_seconds (> 0) with windows left, the
@@ -357,6 +369,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
                 if (rs == d.second) r |= 2;
             }
         }
+        // (built before any graph capture: the tables are copied synchronously)
         if (!c->twiddle_image(p.L) || !c->twiddle64(p.L))
             return c->fail(GP_ERR_NOMEM, "batch generation: twiddle tables for length %d", p.L);
         GP_CUDA_TRY(c, cudaMemcpyAsync(A + j.off_units, j.units.data(), j.units.size() * 2, cudaMemcpyHostToDevice, s));
@@ -381,10 +394,85 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     ea.next_win = ctr + kNextWin;
     ea.status = c->status.as<int>();
 
-    // ---- one iteration of the pipeline on stream s (branches per job)
+    // ---- one iteration of the pipeline on stream s
+    const bool multi = cfg.multi_launch && multi_launch_ok(jobs);
+    auto row_src = [&](int ji) {
+        const JobRun& j = jobs[ji];
+        return gp::RowSrc{nullptr, reinterpret_cast<const uint4*>(A + j.off_words), j.p.L, j.p.b, j.p.compress};
+    };
+    auto finalize_args = [&](int ji) {
+        JobRun& j = jobs[ji];
+        const GenPlan& p = j.p;
+        unsigned long long* it = ctr + ji * kIterSlots;
+        uint8_t* rb = A + j.off_rec;
+        gp::FinalizeArgs fa;
+        fa.src = row_src(ji);
+        fa.roles = A + j.off_roles;
+        fa.fixed_role = 0;
+        fa.idx = reinterpret_cast<uint32_t*>(A + j.off_idx);
+        fa.n_idx = it + 2;
+        fa.idx_cap = j.hard;
+        fa.tw = c->twiddle64(p.L);
+        fa.thr = 2.0 * p.order - p.paf + 0.001;
+        fa.bound = 2 * p.order - p.paf;
+        fa.invert_roles = 2;  // B lines carry bound - rint(psd) (io.cpp:26-36)
+        fa.check_canonical = 1;
+        fa.units = reinterpret_cast<const int16_t*>(A + j.off_units);
+        fa.n_units = (int)j.units.size();
+        fa.rec_words = reinterpret_cast<uint4*>(rb);
+        fa.rec_role = rb + (size_t)j.rcap * 16;
+        fa.rec_sig = reinterpret_cast<uint16_t*>(rb + align_up((size_t)j.rcap * 17, 16));
+        fa.rec_src = nullptr;
+        fa.rec_count = ctr + kCumBase + ji * kCumSlots + 1;
+        fa.rec_cap = j.rcap;
+        fa.psd_pass = ctr + kCumBase + ji * kCumSlots + 2;
+        fa.status = c->status.as<int>();
+        fa.prune_tab = c->spectral_prune && fa.bound < kPruneTab ? c->prune_tab.as<uint8_t>() : nullptr;
+        return fa;
+    };
+    // every job in one launch per kernel, all on s
+    auto enqueue_multi = [&]() -> int {
+        gp::RowSrc src[gp::kMaxTcJobs];
+        int64_t cap[gp::kMaxTcJobs];
+        const unsigned long long* ndev[gp::kMaxTcJobs];
+        int order[gp::kMaxTcJobs], paf[gp::kMaxTcJobs];
+        uint32_t *mask[gp::kMaxTcJobs], *unsure[gp::kMaxTcJobs];
+        unsigned long long* ucount[gp::kMaxTcJobs];
+        gp::ListMultiArgs la{};
+        gp::FinalizeMultiArgs fm{};
+        la.njobs = fm.njobs = nj;
+        la.status = c->status.as<int>();
+        for (int ji = 0; ji < nj; ++ji) {
+            JobRun& j = jobs[ji];
+            unsigned long long* it = ctr + ji * kIterSlots;
+            src[ji] = row_src(ji);
+            cap[ji] = j.hard;
+            ndev[ji] = it + 0;
+            order[ji] = j.p.order;
+            paf[ji] = j.p.paf;
+            mask[ji] = reinterpret_cast<uint32_t*>(A + j.off_mask);
+            unsure[ji] = reinterpret_cast<uint32_t*>(A + j.off_unsure);
+            ucount[ji] = it + 1;
+            la.job[ji] = gp::ListJob{mask[ji], j.hard, it + 0, reinterpret_cast<uint32_t*>(A + j.off_idx), it + 2,
+                                     j.hard};
+            fm.job[ji] = finalize_args(ji);
+        }
+        int rc = c->enqueue_filter_multi(src, cap, ndev, order, paf, mask, unsure, ucount, nj, cfg.tc_ctas_per_sm, s);
+        if (rc) return rc;
+        GP_CUDA_TRY(c, gp::launch_mask_to_list_multi(la, c->num_sms, s));
+        GP_CUDA_TRY(c, gp::launch_finalize_multi(fm, cap, c->num_sms, s));
+        return GP_OK;
+    };
     auto enqueue_iteration = [&]() -> int {
         GP_CUDA_TRY(c, cudaMemsetAsync(ctr, 0, kIterWords * 8, s));
         GP_CUDA_TRY(c, gp::launch_enumerate(ea, c->num_sms, s, cfg.enum_variant));
+        if (multi) {
+            const int rc = enqueue_multi();
+            if (rc) return rc;
+            GP_CUDA_TRY(c, cudaMemcpyAsync(hctr, ctr, kCounterWords * 8, cudaMemcpyDeviceToHost, s));
+            return GP_OK;
+        }
+        // branches per job
         GP_CUDA_TRY(c, cudaEventRecord(c->ev_fork, s));
         for (int ji = 0; ji < nj; ++ji) {
             JobRun& j = jobs[ji];
@@ -392,7 +480,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
             cudaStream_t sj = c->s_jobs[ji];
             GP_CUDA_TRY(c, cudaStreamWaitEvent(sj, c->ev_fork, 0));
             unsigned long long* it = ctr + ji * kIterSlots;
-            const gp::RowSrc src{nullptr, reinterpret_cast<const uint4*>(A + j.off_words), p.L, p.b, p.compress};
+            const gp::RowSrc src = row_src(ji);
             uint32_t* mask = reinterpret_cast<uint32_t*>(A + j.off_mask);
             uint32_t* idx = reinterpret_cast<uint32_t*>(A + j.off_idx);
             int rc = c->enqueue_filter_dev(src, j.hard, it + 0, p.order, p.paf, mask,
@@ -400,30 +488,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
             if (rc) return rc;
             GP_CUDA_TRY(c, gp::launch_mask_to_list(mask, j.hard, idx, it + 2, j.hard, c->status.as<int>(), c->num_sms,
                                                    sj, it + 0));
-            uint8_t* rb = A + j.off_rec;
-            gp::FinalizeArgs fa;
-            fa.src = src;
-            fa.roles = A + j.off_roles;
-            fa.fixed_role = 0;
-            fa.idx = idx;
-            fa.n_idx = it + 2;
-            fa.idx_cap = j.hard;
-            fa.tw = c->twiddle64(p.L);
-            fa.thr = 2.0 * p.order - p.paf + 0.001;
-            fa.bound = 2 * p.order - p.paf;
-            fa.invert_roles = 2;  // B lines carry bound - rint(psd) (io.cpp:26-36)
-            fa.check_canonical = 1;
-            fa.units = reinterpret_cast<const int16_t*>(A + j.off_units);
-            fa.n_units = (int)j.units.size();
-            fa.rec_words = reinterpret_cast<uint4*>(rb);
-            fa.rec_role = rb + (size_t)j.rcap * 16;
-            fa.rec_sig = reinterpret_cast<uint16_t*>(rb + align_up((size_t)j.rcap * 17, 16));
-            fa.rec_src = nullptr;
-            fa.rec_count = ctr + kCumBase + ji * kCumSlots + 1;
-            fa.rec_cap = j.rcap;
-            fa.psd_pass = ctr + kCumBase + ji * kCumSlots + 2;
-            fa.status = c->status.as<int>();
-            fa.prune_tab = c->spectral_prune && fa.bound < kPruneTab ? c->prune_tab.as<uint8_t>() : nullptr;
+            const gp::FinalizeArgs fa = finalize_args(ji);
             GP_CUDA_TRY(c, gp::launch_finalize(fa, j.hard, c->num_sms, sj));
             GP_CUDA_TRY(c, cudaEventRecord(c->ev_join[ji], sj));
             GP_CUDA_TRY(c, cudaStreamWaitEvent(s, c->ev_join[ji], 0));
@@ -556,13 +621,14 @@ int tune_batch(gp_ctx* c, const std::vector<JobRun>& jobs, BatchCfg& best, doubl
     const auto t0 = std::chrono::steady_clock::now();
     const std::string key = "batch:" + batch_key(jobs);
     auto hit = c->tuned.find(key);
-    if (hit != c->tuned.end() && hit->second.size() == 5) {
+    if (hit != c->tuned.end() && hit->second.size() == 6) {
         const auto& v = hit->second;
         best.enum_variant = (int)v[0];
         best.windows_per_thread = (int)v[1];
         best.cand_cap = v[2];
         best.tc_ctas_per_sm = (int)v[3];
         best.use_graph = (int)v[4];
+        best.multi_launch = (int)v[5];
         *seconds = 0;
         return GP_OK;
     }
@@ -600,6 +666,15 @@ int tune_batch(gp_ctx* c, const std::vector<JobRun>& jobs, BatchCfg& best, doubl
     BatchCfg one = base;
     one.tc_ctas_per_sm = 1;
     cands.push_back(one);
+    if (multi_launch_ok(jobs)) {
+        // one launch per kernel over every job
+        BatchCfg ml = base;
+        ml.multi_launch = 1;
+        cands.push_back(ml);
+        BatchCfg ml1 = ml;
+        ml1.tc_ctas_per_sm = 1;
+        cands.push_back(ml1);
+    }
     double best_t = 1e300;
     for (size_t ci = 0; ci <= cands.size(); ++ci) {
         // candidate 0 runs twice; its first run (module loading) is not scored
@@ -614,7 +689,8 @@ int tune_batch(gp_ctx* c, const std::vector<JobRun>& jobs, BatchCfg& best, doubl
             best = cfg;
         }
     }
-    c->tuned[key] = {best.enum_variant, best.windows_per_thread, best.cand_cap, best.tc_ctas_per_sm, best.use_graph};
+    c->tuned[key] = {best.enum_variant, best.windows_per_thread, best.cand_cap, best.tc_ctas_per_sm, best.use_graph,
+                     best.multi_launch};
     *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return GP_OK;
 }
@@ -945,6 +1021,11 @@ extern "C" int gp_generate_batch(gp_ctx* c, const gp_gen_job* jobs, int njobs, i
         if (cfg->cand_cap > 0) bc.cand_cap = cfg->cand_cap;
         if (cfg->tc_ctas_per_sm > 0) bc.tc_ctas_per_sm = cfg->tc_ctas_per_sm;
         bc.use_graph = cfg->no_graph ? 0 : 1;
+        if (cfg->multi_launch == 1) {
+            if (!multi_launch_ok(run))
+                return c->fail(GP_ERR_UNSUPPORTED, "batch generation: these jobs do not fit one filter launch");
+            bc.multi_launch = 1;
+        }
     }
     int iters = 0;
     int rc = run_batch(c, run, bc, &iters);
@@ -967,6 +1048,7 @@ extern "C" int gp_generate_batch(gp_ctx* c, const gp_gen_job* jobs, int njobs, i
         cfg->cand_cap = bc.cand_cap;
         cfg->tc_ctas_per_sm = bc.tc_ctas_per_sm;
         cfg->no_graph = bc.use_graph ? 0 : 1;
+        cfg->multi_launch = bc.multi_launch;
         cfg->iterations = iters;
         cfg->tune_seconds = tune_s;
     }

@@ -160,6 +160,13 @@ struct gp_ctx {
     }
     // device twiddle image for length L (tensor-core filter)
     const void* twiddle_image(int L);
+    // Multi-job tensor-core filter of device batches (packed words) followed
+    // by the FP64 recheck of every job's unsure rows: two launches on st for
+    // up to eight jobs, each job's tiles at its own padded K.  Per job as
+    // enqueue_filter_dev; unsure counts must be zero.
+    int enqueue_filter_multi(const gp::RowSrc* src, const int64_t* cap, const unsigned long long* const* n_dev,
+                             const int* order, const int* paf, uint32_t* const* d_mask, uint32_t* const* d_unsure,
+                             unsigned long long* const* d_ucount, int njobs, int grid_per_sm, cudaStream_t st);
     // device FP64 twiddle table for length L
     const double* twiddle64(int L);
     // Enqueues the PSD filter of a device batch (int8 rows or packed words)

@@ -21,8 +21,8 @@ namespace {
 
 constexpr int kWarps = 8;
 
-__global__ void mask_to_list_kernel(const uint32_t* mask, int64_t n, const unsigned long long* n_dev, uint32_t* out,
-                                    unsigned long long* count, int64_t cap, int* status) {
+__device__ __forceinline__ void list_bits(const uint32_t* mask, int64_t n, const unsigned long long* n_dev,
+                                          uint32_t* out, unsigned long long* count, int64_t cap, int* status) {
     const int lane = threadIdx.x & 31;
     if (n_dev && (int64_t)*n_dev < n) n = (int64_t)*n_dev;
     const int64_t nwords = (n + 31) / 32;
@@ -45,8 +45,18 @@ __global__ void mask_to_list_kernel(const uint32_t* mask, int64_t n, const unsig
     }
 }
 
-__global__ void __launch_bounds__(kWarps * 32) finalize_kernel(FinalizeArgs a) {
-    extern __shared__ double2 sh_tw[];
+__global__ void mask_to_list_kernel(const uint32_t* mask, int64_t n, const unsigned long long* n_dev, uint32_t* out,
+                                    unsigned long long* count, int64_t cap, int* status) {
+    list_bits(mask, n, n_dev, out, count, cap, status);
+}
+
+// every job's mask in one launch: grid row y serves job y
+__global__ void mask_to_list_multi_kernel(ListMultiArgs a) {
+    const ListJob& j = a.job[blockIdx.y];
+    list_bits(j.mask, j.n, j.n_dev, j.out, j.count, j.cap, a.status);
+}
+
+__device__ __forceinline__ void finalize_rows(const FinalizeArgs& a, double2* sh_tw) {
     const int L = a.src.L;
     double* psd_all = reinterpret_cast<double*>(sh_tw + L);
     int8_t* xs_all = reinterpret_cast<int8_t*>(psd_all + kWarps * L);
@@ -145,6 +155,21 @@ __global__ void __launch_bounds__(kWarps * 32) finalize_kernel(FinalizeArgs a) {
     }
 }
 
+__global__ void __launch_bounds__(kWarps * 32) finalize_kernel(FinalizeArgs a) {
+    extern __shared__ double2 sh_tw[];
+    finalize_rows(a, sh_tw);
+}
+
+// every job's survivors in one launch: grid row y serves job y
+__global__ void __launch_bounds__(kWarps * 32) finalize_multi_kernel(FinalizeMultiArgs m) {
+    extern __shared__ double2 sh_tw[];
+    finalize_rows(m.job[blockIdx.y], sh_tw);
+}
+
+size_t finalize_smem(int L) {
+    return sizeof(double2) * L + sizeof(double) * kWarps * L + (size_t)kWarps * kMaxLen;
+}
+
 }  // namespace
 
 cudaError_t launch_mask_to_list(const uint32_t* mask, int64_t n, uint32_t* out, unsigned long long* count,
@@ -161,10 +186,45 @@ cudaError_t launch_finalize(const FinalizeArgs& a, int64_t max_rows, int num_sms
     if (max_rows <= 0) return cudaSuccess;
     int64_t blocks = (max_rows + kWarps - 1) / kWarps;
     if (blocks > (int64_t)num_sms * 16) blocks = (int64_t)num_sms * 16;
-    const size_t smem = sizeof(double2) * a.src.L + sizeof(double) * kWarps * a.src.L + (size_t)kWarps * kMaxLen;
+    const size_t smem = finalize_smem(a.src.L);
     cudaError_t e = cudaFuncSetAttribute(finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     finalize_kernel<<<(unsigned)blocks, kWarps * 32, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mask_to_list_multi(const ListMultiArgs& a, int num_sms, cudaStream_t st) {
+    if (a.njobs <= 0 || a.njobs > kMaxMultiJobs) return a.njobs == 0 ? cudaSuccess : cudaErrorInvalidValue;
+    int64_t maxn = 0;
+    for (int j = 0; j < a.njobs; ++j) maxn = a.job[j].n > maxn ? a.job[j].n : maxn;
+    if (maxn <= 0) return cudaSuccess;
+    int64_t blocks = ((maxn + 31) / 32 + 7) / 8;
+    // per job as many blocks as its own launch would take: blocks of a job
+    // with fewer rows end at once
+    if (blocks > (int64_t)num_sms * 16) blocks = (int64_t)num_sms * 16;
+    mask_to_list_multi_kernel<<<dim3((unsigned)blocks, (unsigned)a.njobs), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_multi(const FinalizeMultiArgs& a, const int64_t* max_rows, int num_sms,
+                                  cudaStream_t st) {
+    if (a.njobs <= 0 || a.njobs > kMaxMultiJobs) return a.njobs == 0 ? cudaSuccess : cudaErrorInvalidValue;
+    int64_t rows = 0;
+    int maxL = 1;
+    for (int j = 0; j < a.njobs; ++j) {
+        rows = max_rows[j] > rows ? max_rows[j] : rows;
+        maxL = a.job[j].src.L > maxL ? a.job[j].src.L : maxL;
+    }
+    if (rows <= 0) return cudaSuccess;
+    int64_t blocks = (rows + kWarps - 1) / kWarps;
+    // per job as many blocks as its own launch would take: blocks of a job
+    // with fewer rows end at once
+    if (blocks > (int64_t)num_sms * 16) blocks = (int64_t)num_sms * 16;
+    const size_t smem = finalize_smem(maxL);
+    cudaError_t e =
+        cudaFuncSetAttribute(finalize_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    finalize_multi_kernel<<<dim3((unsigned)blocks, (unsigned)a.njobs), kWarps * 32, smem, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -45,4 +45,28 @@ cudaError_t launch_mask_to_list(const uint32_t* mask, int64_t n, uint32_t* out, 
                                 const unsigned long long* n_dev = nullptr);
 cudaError_t launch_finalize(const FinalizeArgs& a, int64_t max_rows, int num_sms, cudaStream_t st);
 
+// The same two steps for several jobs in one launch each (grid row y = job y).
+constexpr int kMaxMultiJobs = 8;
+struct ListJob {
+    const uint32_t* mask;
+    int64_t n;                          // rows (capacity), or min(n, *n_dev)
+    const unsigned long long* n_dev;
+    uint32_t* out;
+    unsigned long long* count;
+    int64_t cap;
+};
+struct ListMultiArgs {
+    ListJob job[kMaxMultiJobs];
+    int njobs;
+    int* status;
+};
+struct FinalizeMultiArgs {
+    FinalizeArgs job[kMaxMultiJobs];
+    int njobs;
+};
+cudaError_t launch_mask_to_list_multi(const ListMultiArgs& a, int num_sms, cudaStream_t st);
+// max_rows[j]: the most rows job j can list (its index capacity)
+cudaError_t launch_finalize_multi(const FinalizeMultiArgs& a, const int64_t* max_rows, int num_sms,
+                                  cudaStream_t st);
+
 }  // namespace gp

@@ -85,6 +85,37 @@ float tc_err_coef(int K);              // |X| error per unit of sum|x|
 
 cudaError_t launch_psd_tc(const PsdTcArgs& a, int num_sms, cudaStream_t st);
 
+// One job of a multi-job tensor-core filter launch: packed words of one
+// length / alphabet, their own twiddle image (at the job's own padded K) and
+// their own verdict outputs.  Tiles never straddle jobs.
+constexpr int kMaxTcJobs = 8;
+constexpr int kMaxMultiK = 64;  // largest padded K of a multi-job launch
+struct PsdTcJob {
+    const uint4* words;
+    const unsigned long long* n_dev;  // rows of this launch (read on the device), at most cap
+    int64_t cap;
+    int L, K, bits, alpha_c;          // K = tc_k_for_len(L); value = 2 * digit - alpha_c
+    float thr;                        // 2n - paf + 0.001
+    float guard_cfg;                  // configured guard band
+    float dc_hi, dc_lo;               // per-row |X| error bounds: hi twiddles alone, hi + lo
+    const void* bimage;               // the job's twiddle image (build_twiddle_image(L, K))
+    uint32_t* mask;                   // ceil(cap / 32) words
+    uint32_t* unsure;
+    unsigned long long* unsure_count;
+};
+struct PsdTcMultiArgs {
+    PsdTcJob job[kMaxTcJobs];
+    int njobs;
+    int grid_per_sm;  // CTAs per SM (0 = as many as fit)
+    int* status;
+};
+// Every job's rows in one launch (one persistent grid over all jobs' tiles,
+// each tile at its job's K).
+cudaError_t launch_psd_tc_multi(const PsdTcMultiArgs& a, int num_sms, cudaStream_t st);
+// True when a multi-job launch takes packed rows of length L with b bits per
+// digit (padded K at most kMaxMultiK).
+bool tc_multi_supported(int L, int b);
+
 // Where the FP64 kernels read candidate rows: int8 rows or packed words.
 struct RowSrc {
     const int8_t* seqs;
@@ -112,6 +143,22 @@ cudaError_t launch_psd_fp64(const PsdF64Args& a, cudaStream_t st);
 cudaError_t launch_psd_recheck(const RowSrc& src, const double* tw, double thr, const uint32_t* unsure,
                                const unsigned long long* unsure_count, int64_t cap, uint32_t* mask,
                                int num_sms, cudaStream_t st);
+
+// The same recheck for several jobs in one launch (one grid row per job).
+struct RecheckJob {
+    RowSrc src;
+    const double* tw;
+    double thr;
+    const uint32_t* unsure;
+    const unsigned long long* unsure_count;
+    int64_t cap;
+    uint32_t* mask;
+};
+struct RecheckMultiArgs {
+    RecheckJob job[8];
+    int njobs;
+};
+cudaError_t launch_psd_recheck_multi(const RecheckMultiArgs& a, int num_sms, cudaStream_t st);
 
 // Exact FP64 PSD values (all L bins) of rows 0..n-1 (testing)
 cudaError_t launch_psd_fp64_values(const RowSrc& src, const double* tw, int64_t n, double* out, cudaStream_t st);

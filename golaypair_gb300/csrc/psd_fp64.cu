@@ -71,11 +71,9 @@ __global__ void __launch_bounds__(kBlock) psd_fp64_filter_kernel(PsdF64Args a) {
 }
 
 // one warp per unsure row; lane l computes bins l+1, l+33, ...
-__global__ void __launch_bounds__(kBlock) psd_recheck_kernel(RowSrc src, const double* tw, double thr,
-                                                             const uint32_t* unsure,
-                                                             const unsigned long long* unsure_count, int64_t cap,
-                                                             uint32_t* mask) {
-    extern __shared__ double2 sh_tw[];
+__device__ __forceinline__ void recheck_rows(const RowSrc& src, const double* tw, double thr, const uint32_t* unsure,
+                                             const unsigned long long* unsure_count, int64_t cap, uint32_t* mask,
+                                             double2* sh_tw) {
     const int L = src.L;
     int8_t* xs = reinterpret_cast<int8_t*>(sh_tw + L) + (threadIdx.x >> 5) * kMaxLen;
     load_tw(sh_tw, tw, L);
@@ -98,6 +96,21 @@ __global__ void __launch_bounds__(kBlock) psd_recheck_kernel(RowSrc src, const d
         if (fail && lane == 0) atomicAnd(&mask[row >> 5], ~(1u << (row & 31)));
         __syncwarp();
     }
+}
+
+__global__ void __launch_bounds__(kBlock) psd_recheck_kernel(RowSrc src, const double* tw, double thr,
+                                                             const uint32_t* unsure,
+                                                             const unsigned long long* unsure_count, int64_t cap,
+                                                             uint32_t* mask) {
+    extern __shared__ double2 sh_tw[];
+    recheck_rows(src, tw, thr, unsure, unsure_count, cap, mask, sh_tw);
+}
+
+// every job's unsure rows in one launch: grid row y serves job y
+__global__ void __launch_bounds__(kBlock) psd_recheck_multi_kernel(RecheckMultiArgs a) {
+    extern __shared__ double2 sh_tw[];
+    const RecheckJob& j = a.job[blockIdx.y];
+    recheck_rows(j.src, j.tw, j.thr, j.unsure, j.unsure_count, j.cap, j.mask, sh_tw);
 }
 
 __global__ void __launch_bounds__(kBlock) psd_values_kernel(RowSrc src, const double* tw, int64_t n, double* out) {
@@ -143,6 +156,27 @@ cudaError_t launch_psd_recheck(const RowSrc& src, const double* tw, double thr, 
     cudaError_t e = cudaFuncSetAttribute(psd_recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     psd_recheck_kernel<<<(unsigned)blocks, kBlock, smem, st>>>(src, tw, thr, unsure, unsure_count, cap, mask);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_psd_recheck_multi(const RecheckMultiArgs& a, int num_sms, cudaStream_t st) {
+    if (a.njobs <= 0) return cudaSuccess;
+    int maxL = 1;
+    int64_t maxcap = 0;
+    for (int j = 0; j < a.njobs; ++j) {
+        maxL = a.job[j].src.L > maxL ? a.job[j].src.L : maxL;
+        maxcap = a.job[j].cap > maxcap ? a.job[j].cap : maxcap;
+    }
+    if (maxcap <= 0) return cudaSuccess;
+    int64_t blocks = (maxcap + (kBlock / 32) - 1) / (kBlock / 32);
+    // per job as many blocks as its own launch would take: blocks of a job
+    // with fewer rows end at once
+    if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
+    const size_t smem = sizeof(double2) * maxL + (size_t)(kBlock / 32) * kMaxLen;
+    cudaError_t e =
+        cudaFuncSetAttribute(psd_recheck_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    psd_recheck_multi_kernel<<<dim3((unsigned)blocks, (unsigned)a.njobs), kBlock, smem, st>>>(a);
     return cudaGetLastError();
 }
 

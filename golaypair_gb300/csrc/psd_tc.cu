@@ -53,6 +53,7 @@
 // converters.
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "gp_device.cuh"
@@ -136,6 +137,25 @@ __device__ void build_lut(uint8_t* lut, int b, int c) {
             reinterpret_cast<__half*>(lut)[e * per + d] = __int2half_rn(2 * digit - c);
         }
     }
+}
+
+// Normalises a packed word: the 128-bit left shift by norm (0..127) that
+// puts digit 0 at bit 127.  sw[0] holds bits 0-31 ... sw[3] bits 96-127.
+// norm is the same for every row of a tile, so the word shift is a uniform
+// branch and the bit shift four funnel shifts.
+__device__ __forceinline__ void shl128(uint4 v, int norm, uint32_t (&sw)[4]) {
+    uint32_t a0 = v.x, a1 = v.y, a2 = v.z, a3 = v.w;
+    switch (norm >> 5) {
+        case 1: a3 = a2; a2 = a1; a1 = a0; a0 = 0u; break;
+        case 2: a3 = a1; a2 = a0; a1 = 0u; a0 = 0u; break;
+        case 3: a3 = a0; a2 = 0u; a1 = 0u; a0 = 0u; break;
+        default: break;
+    }
+    const uint32_t bs = (uint32_t)norm & 31u;
+    sw[3] = __funnelshift_l(a2, a3, bs);
+    sw[2] = __funnelshift_l(a1, a2, bs);
+    sw[1] = __funnelshift_l(a0, a1, bs);
+    sw[0] = a0 << bs;
 }
 
 // 8 halves of digits 8*ch .. 8*ch+7 from the normalised word (digit 0 at bit
@@ -461,21 +481,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(
                 } else {
                     wv = row < n ? a.words[row] : make_uint4(0, 0, 0, 0);
                 }
-                // normalise: 128-bit left shift by `norm` puts digit 0 at bit 127
-                const uint32_t w[4] = {wv.x, wv.y, wv.z, wv.w};
                 uint32_t sw[4];
-                const int ws = norm >> 5, bs = norm & 31;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int si = i - ws;
-                    uint32_t cur = 0u, prev = 0u;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        cur = (si == k) ? w[k] : cur;
-                        prev = (si - 1 == k) ? w[k] : prev;
-                    }
-                    sw[i] = bs ? ((cur << bs) | (prev >> (32 - bs))) : cur;
-                }
+                shl128(wv, norm, sw);
                 packed_row<B, 0, C::KCH>(sw, sLut, h);
             }
             const long long c25t = tclock<TR>();
@@ -805,6 +812,370 @@ double half_value(uint16_t h) {
     return s ? -v : v;
 }
 
+
+// ------------------------------------------------------------ multi-job filter
+// Several jobs' packed rows (different lengths, alphabets and bounds) in one
+// persistent launch: the tiles of job j are the global tiles [T_j, T_j+1),
+// a tile never straddles jobs, and every tile runs at its own job's padded
+// length K_j (16, 32, 48 or 64; the launch is instantiated for the largest).
+// Each role looks its tile's job up and takes that job's words, digit
+// table, twiddle image, UMMA shape (N = 2 K_j, K_j / 16 steps), bound and
+// outputs; the barrier rings and the TMEM layout (sized for the largest K)
+// are those of psd_tc_kernel.
+
+struct MultiLayout {
+    uint32_t lut_off, raw_off, raw_stride, raw_stages, bar_off, misc_off, total;
+};
+
+// b_bytes: the jobs' twiddle images, back to back from offset 0
+template <int K>
+MultiLayout multi_layout(uint32_t b_bytes, int njobs, uint32_t budget) {
+    using C = TcCfg<K>;
+    MultiLayout s;
+    uint32_t off = (b_bytes + 1023) & ~1023u;
+    s.lut_off = off;
+    off += (uint32_t)njobs * kLutBytes;
+    s.bar_off = off;
+    off += (2 * kMaxRawStages + 2 * C::AS + 2 * C::NACC + 2) * 8;
+    s.misc_off = off;
+    // TMEM slot, abort flag; first tile of each job (+ end); rows, whole
+    // tiles, K and image offset of each job
+    off += 16 + 4 * (kMaxTcJobs + 1) + 4 * 4 * kMaxTcJobs;
+    off = (off + 127) & ~127u;
+    s.raw_stride = (uint32_t)((kTileM * 16 + kRawSlack + 127) & ~127);
+    s.raw_off = off;
+    const uint32_t room = budget > off + 1024 ? budget - off - 1024 : 0;
+    int st = (int)(room / s.raw_stride);
+    if (st > kMaxRawStages) st = kMaxRawStages;
+    s.raw_stages = (uint32_t)(st < 2 ? 0 : st);  // 0: does not fit this budget
+    off += (uint32_t)(st < 2 ? 2 : st) * s.raw_stride;
+    s.total = off + 1024;
+    // at most two CTAs per SM, as in psd_tc_kernel
+    if (s.total < 96 * 1024) s.total = 96 * 1024;
+    return s;
+}
+
+// Calls f(std::integral_constant<int, kj>) for kj in {16, 32, 48, 64}, kj <= KMAX.
+template <int KMAX, class F>
+__device__ __forceinline__ void dispatch_k(int kj, F&& f) {
+    if (kj == 16) {
+        f(std::integral_constant<int, 16>{});
+    } else if constexpr (KMAX >= 32) {
+        if (kj == 32) {
+            f(std::integral_constant<int, 32>{});
+        } else if constexpr (KMAX >= 48) {
+            if (kj == 48) {
+                f(std::integral_constant<int, 48>{});
+            } else if constexpr (KMAX >= 64) {
+                if (kj == 64) f(std::integral_constant<int, 64>{});
+            }
+        }
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_multi_kernel(PsdTcMultiArgs a,
+                                                                                        MultiLayout lay) {
+    using C = TcCfg<K>;
+    extern __shared__ uint8_t smem_raw_base[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw_base) + 1023) & ~uintptr_t(1023));
+    uint8_t* sB = smem;
+    uint8_t* sLut = smem + lay.lut_off;
+    uint8_t* sRaw = smem + lay.raw_off;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + lay.bar_off);
+    uint64_t* raw_full = bars;
+    uint64_t* raw_empty = bars + kMaxRawStages;
+    uint64_t* a_full = bars + 2 * kMaxRawStages;
+    uint64_t* a_empty = a_full + C::AS;
+    uint64_t* acc_full = a_empty + C::AS;
+    uint64_t* acc_empty = acc_full + C::NACC;
+    uint64_t* b_full = acc_empty + C::NACC;
+    uint64_t* final_bar = b_full + 1;
+    const uint32_t u_raw_full = smem_u32(raw_full), u_raw_empty = smem_u32(raw_empty);
+    const uint32_t u_a_full = smem_u32(a_full), u_a_empty = smem_u32(a_empty);
+    const uint32_t u_acc_full = smem_u32(acc_full), u_acc_empty = smem_u32(acc_empty);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + lay.misc_off);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + lay.misc_off + 4);
+    int* s_tile0 = reinterpret_cast<int*>(smem + lay.misc_off + 16);  // [njobs + 1] first global tile of each job
+    int* s_rows = s_tile0 + kMaxTcJobs + 1;                           // rows of each job
+    int* s_nfull = s_rows + kMaxTcJobs;  // tiles bulk-copied (whole, from 16-byte aligned words)
+    int* s_k = s_nfull + kMaxTcJobs;     // padded length
+    int* s_boff = s_k + kMaxTcJobs;      // twiddle image offset in sB
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int nj = a.njobs;
+    const int RS = (int)lay.raw_stages;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < RS; ++i) {
+            mbar_init(&raw_full[i], 1);
+            mbar_init(&raw_empty[i], kConvWarps);
+        }
+        for (int i = 0; i < C::AS; ++i) {
+            mbar_init(&a_full[i], kConvWarps);
+            mbar_init(&a_empty[i], 1);
+        }
+        for (int i = 0; i < C::NACC; ++i) {
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], 4);
+        }
+        mbar_init(b_full, 1);
+        mbar_init(final_bar, 1);
+        *abort_flag = 0;
+        int t = 0, boff = 0;
+        for (int j = 0; j < nj; ++j) {
+            int64_t n = a.job[j].cap;
+            if (a.job[j].n_dev) {
+                const int64_t nd = (int64_t)*reinterpret_cast<const volatile unsigned long long*>(a.job[j].n_dev);
+                if (nd < n) n = nd;
+            }
+            s_rows[j] = (int)n;
+            const bool aligned = (reinterpret_cast<uintptr_t>(a.job[j].words) & 15) == 0;
+            s_nfull[j] = aligned ? (int)(n / kTileM) : 0;
+            s_tile0[j] = t;
+            t += (int)((n + kTileM - 1) / kTileM);
+            s_k[j] = a.job[j].K;
+            s_boff[j] = boff;
+            boff += 4 * a.job[j].K * a.job[j].K;  // 2K x K fp16: a multiple of 1024 bytes
+        }
+        s_tile0[nj] = t;
+        mbar_fence_init();
+    }
+    for (int j = 0; j < nj; ++j) build_lut(sLut + j * kLutBytes, a.job[j].bits, a.job[j].alpha_c);
+    if (warp == 9) {
+        tmem_alloc(tmem_slot, C::TMEM_COLS);
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
+    const int ntiles = s_tile0[nj];
+    // the job of global tile t (at most eight jobs: a short scan)
+    auto job_of = [&](int t) {
+        int j = 0;
+        while (j + 1 < nj && s_tile0[j + 1] <= t) ++j;
+        return j;
+    };
+
+    if (warp < kConvWarps) {
+        // ------------------------------------------------ converters
+        const int r = threadIdx.x;
+        const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16) + (uint32_t)C::A_COL0;
+        Ring raw, ast;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, raw.next(RS), ast.next(C::AS)) {
+            const int rs = raw.slot, as = ast.slot;
+            const uint32_t rph = raw.phase, aph = ast.phase;
+            if (!mbar_wait(u_raw_full + 8u * rs, rph, abort_flag, a.status, 1)) break;
+            if (!mbar_wait((C::AS == C::NACC ? u_acc_full : u_a_empty) + 8u * as, aph ^ 1u, abort_flag, a.status, 2))
+                break;
+            tc_fence_after();
+            const int j = job_of(t);
+            const PsdTcJob& jb = a.job[j];
+            const int lt = t - s_tile0[j];
+            const int row = lt * kTileM + r;
+            uint4 wv;
+            if (lt < s_nfull[j])
+                wv = *reinterpret_cast<const uint4*>(sRaw + rs * lay.raw_stride + r * 16);
+            else
+                wv = row < s_rows[j] ? jb.words[row] : make_uint4(0, 0, 0, 0);
+            uint32_t sw[4];
+            shl128(wv, 128 - jb.bits * jb.L, sw);
+            const uint8_t* lut = sLut + j * kLutBytes;
+            const uint32_t aaddr = lane_base + (uint32_t)(as * (K / 2));
+            const int bits = jb.bits;
+            dispatch_k<K>(s_k[j], [&](auto kc) {
+                constexpr int KJ = decltype(kc)::value;
+                uint32_t h[KJ / 2];
+                switch (bits) {
+                    case 1: packed_row<1, 0, KJ / 8>(sw, lut, h); break;
+                    case 2: packed_row<2, 0, KJ / 8>(sw, lut, h); break;
+                    case 3:
+                        if constexpr (KJ <= 48) packed_row<3, 0, KJ / 8>(sw, lut, h);
+                        break;
+                    default:
+                        if constexpr (KJ <= 48) packed_row<4, 0, KJ / 8>(sw, lut, h);
+                        break;
+                }
+#pragma unroll
+                for (int g = 0; g < KJ / 16; ++g) tmem_st8(aaddr + 8 * g, h + 8 * g);
+            });
+            tmem_wait_st();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(u_a_full + 8u * as);
+                mbar_arrive(u_raw_empty + 8u * rs);
+            }
+        }
+    } else if (warp < kConvWarps + 4) {
+        // ------------------------------------------------ epilogue
+        const int q = warp & 3;
+        Ring acc;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, acc.next(C::NACC)) {
+            const int b = acc.slot;
+            if (!mbar_wait(u_acc_full + 8u * b, acc.phase, abort_flag, a.status, 3)) break;
+            tc_fence_after();
+            const int j = job_of(t);
+            const PsdTcJob& jb = a.job[j];
+            const int lt = t - s_tile0[j];
+            const int row = lt * kTileM + q * 32 + lane;
+            const bool valid = row < s_rows[j];
+            const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * C::N);
+            const float thr = jb.thr, sq2 = 2.f * sqrtf(thr);
+            // packed rows: |value| <= c, so the per-bin error is at most coef L c
+            auto guard = [&](float d) { return fmaxf(jb.guard_cfg, fmaf(sq2, d, fmaf(3.f * d, d, 1e-4f))); };
+            float pmax = 0.f, g = 0.f;
+            dispatch_k<K>(s_k[j], [&](auto kc) {
+                constexpr int HB = decltype(kc)::value / 2;
+                float x0 = 0.f;
+                long long c_ld = 0;
+                psd_hi_all<HB, false>(taddr, pmax, x0, c_ld);
+                g = guard(jb.dc_hi);
+                if (__any_sync(0xFFFFFFFFu, valid && fabsf(pmax - thr) <= g)) {
+                    pmax = exact_pass<HB, false>(taddr, nullptr).x;
+                    g = guard(jb.dc_lo);
+                }
+            });
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(u_acc_empty + 8u * b);
+            const bool sure = valid && pmax < thr - g;
+            const bool unsure = valid && !sure && pmax <= thr + g;
+            const uint32_t bits = __ballot_sync(0xFFFFFFFFu, sure || unsure);
+            const int word = lt * 4 + q;
+            if (lane == 0 && (int64_t)word < ((jb.cap + 31) >> 5)) jb.mask[word] = bits;
+            const uint32_t ub = __ballot_sync(0xFFFFFFFFu, unsure);
+            if (ub) {
+                unsigned long long basei = 0;
+                if (lane == 0) basei = atomicAdd(jb.unsure_count, (unsigned long long)__popc(ub));
+                basei = __shfl_sync(0xFFFFFFFFu, basei, 0);
+                if (unsure) {
+                    const unsigned long long pos = basei + __popc(ub & ((1u << lane) - 1u));
+                    if ((int64_t)pos < jb.cap)
+                        jb.unsure[pos] = (uint32_t)row;
+                    else
+                        atomicCAS(a.status, 0, GP_KSTATUS_OVERFLOW);
+                }
+            }
+        }
+    } else if (warp == kConvWarps + 4) {
+        // ------------------------------------------------ producer
+        int64_t it = 0;
+        if (lane == 0) {
+            uint32_t bbytes = 0;
+            for (int j = 0; j < nj; ++j) bbytes += 4u * (uint32_t)(s_k[j] * s_k[j]);
+            mbar_arrive_expect_tx(b_full, bbytes);
+            for (int j = 0; j < nj; ++j)
+                bulk_g2s(sB + s_boff[j], a.job[j].bimage, 4u * (uint32_t)(s_k[j] * s_k[j]), b_full);
+            const uint32_t u_raw = smem_u32(sRaw);
+            Ring raw;
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it, raw.next(RS)) {
+                const int rs = raw.slot;
+                if (!mbar_wait(u_raw_empty + 8u * rs, raw.phase ^ 1u, abort_flag, a.status, 4)) break;
+                const int j = job_of(t);
+                const int lt = t - s_tile0[j];
+                if (lt < s_nfull[j]) {
+                    const uint32_t bytes = (uint32_t)(kTileM * 16);
+                    mbar_arrive_expect_tx(u_raw_full + 8u * rs, bytes);
+                    bulk_g2s(u_raw + (uint32_t)rs * lay.raw_stride,
+                             reinterpret_cast<const uint8_t*>(a.job[j].words) + (int64_t)lt * kTileM * 16, bytes,
+                             u_raw_full + 8u * rs);
+                } else {
+                    mbar_arrive(u_raw_full + 8u * rs);
+                }
+            }
+            // no copies left in flight: wait (bounded) for the last phase of every stage
+            const int issued = (int)(it < RS ? it : RS);
+            for (int k = 0; k < issued; ++k) {
+                const int64_t jj = it - 1 - k;
+                const int rs = (int)(jj % RS);
+                const uint32_t ph = (uint32_t)((jj / RS) & 1);
+                const uint64_t t0 = globaltimer_ns();
+                while (!mbar_try_wait(&raw_full[rs], ph)) {
+                    if (globaltimer_ns() - t0 > kWaitTimeoutNs) {
+                        atomicCAS(a.status, 0, GP_KSTATUS_TIMEOUT_BASE + 7);
+                        break;
+                    }
+                }
+            }
+            const uint64_t t0 = globaltimer_ns();
+            while (!mbar_try_wait(b_full, 0)) {
+                if (globaltimer_ns() - t0 > kWaitTimeoutNs) {
+                    atomicCAS(a.status, 0, GP_KSTATUS_TIMEOUT_BASE + 8);
+                    break;
+                }
+            }
+        }
+    } else {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            bool ok = mbar_wait(b_full, 0, abort_flag, a.status, 5);
+            Ring ast, acc;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ast.next(C::AS), acc.next(C::NACC)) {
+                const int as = ast.slot, b = acc.slot;
+                if (!mbar_wait(u_a_full + 8u * as, ast.phase, abort_flag, a.status, 6)) break;
+                if (!mbar_wait(u_acc_empty + 8u * b, acc.phase ^ 1u, abort_flag, a.status, 9)) break;
+                tc_fence_after();
+                const int j = job_of(t);
+                const int kj = s_k[j];
+                // the tile's job's shape and twiddle image: N = 2 K_j, K_j / 16 steps
+                const uint32_t idesc = idesc_f16_f32(C::M, 2 * kj);
+                const uint32_t kstride = (uint32_t)(2 * kj / 8) * 128;
+                const uint64_t bdesc0 = sdesc_noswizzle(smem_u32(sB + s_boff[j]), kstride, 128);
+                const uint32_t d = tmem_base + (uint32_t)(b * C::N);
+                const uint32_t a0 = tmem_base + (uint32_t)(C::A_COL0 + as * (K / 2));
+                for (int ks = 0; ks < kj / 16; ++ks)
+                    umma_f16_ts(d, a0 + (uint32_t)(8 * ks), bdesc0 + (uint64_t)((2 * ks * kstride) >> 4), idesc,
+                                ks != 0 ? 1u : 0u);
+                if constexpr (C::AS != C::NACC) umma_commit(u_a_empty + 8u * as);
+                umma_commit(u_acc_full + 8u * b);
+            }
+            umma_commit(final_bar);
+            const uint64_t t0 = globaltimer_ns();
+            while (!mbar_try_wait(final_bar, 0)) {
+                if (globaltimer_ns() - t0 > kWaitTimeoutNs) {
+                    atomicCAS(a.status, 0, GP_KSTATUS_TIMEOUT_BASE + 10);
+                    break;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 9) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, C::TMEM_COLS);
+    }
+}
+
+template <int K>
+cudaError_t launch_multi_k(const PsdTcMultiArgs& a, int num_sms, cudaStream_t st) {
+    using C = TcCfg<K>;
+    uint32_t b_bytes = 0;
+    for (int j = 0; j < a.njobs; ++j) b_bytes += 4u * (uint32_t)(a.job[j].K * a.job[j].K);
+    // two CTAs per SM when every job's twiddle image and digit table fit beside
+    // the raw ring in the two-CTA budget, else one
+    MultiLayout lay = multi_layout<K>(b_bytes, a.njobs, kSmemBudget2Cta);
+    int fit = C::MIN_BLOCKS;
+    if (lay.raw_stages == 0 || C::MIN_BLOCKS < 2) {
+        lay = multi_layout<K>(b_bytes, a.njobs, kSmemBudget1Cta);
+        fit = 1;
+    }
+    if (lay.raw_stages == 0) return cudaErrorInvalidValue;
+    auto kern = psd_tc_multi_kernel<K>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
+    if (e != cudaSuccess) return e;
+    int64_t cap_tiles = 0;
+    for (int j = 0; j < a.njobs; ++j) cap_tiles += (a.job[j].cap + kTileM - 1) / kTileM;
+    if (cap_tiles == 0) return cudaSuccess;
+    const int per_sm = a.grid_per_sm > 0 && a.grid_per_sm < fit ? a.grid_per_sm : fit;
+    int64_t grid = (int64_t)num_sms * per_sm;
+    if (grid > cap_tiles) grid = cap_tiles;
+    kern<<<(unsigned)grid, kThreads, lay.total, st>>>(a, lay);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 // K: L + 1 rounded up to 16, so that the last cosine row is free for the
@@ -853,6 +1224,30 @@ size_t build_twiddle_image(int L, int K, void* out) {
     }
     std::memcpy(out, img.data(), bytes);
     return bytes;
+}
+
+bool tc_multi_supported(int L, int b) { return tc_packed_supported(L, b) && tc_k_for_len(L) <= kMaxMultiK; }
+
+cudaError_t launch_psd_tc_multi(const PsdTcMultiArgs& a, int num_sms, cudaStream_t st) {
+    if (a.njobs < 1 || a.njobs > kMaxTcJobs) return cudaErrorInvalidValue;
+    int kmax = 0;
+    int64_t tiles = 0;
+    for (int j = 0; j < a.njobs; ++j) {
+        const PsdTcJob& q = a.job[j];
+        if (!tc_multi_supported(q.L, q.bits) || q.K != tc_k_for_len(q.L) || q.cap < 0 ||
+            q.cap >= (int64_t(1) << 31))
+            return cudaErrorInvalidValue;
+        kmax = q.K > kmax ? q.K : kmax;
+        tiles += (q.cap + kTileM - 1) / kTileM;
+    }
+    if (tiles >= (int64_t(1) << 31)) return cudaErrorInvalidValue;  // 32-bit global tile index
+    switch (kmax) {
+        case 16: return launch_multi_k<16>(a, num_sms, st);
+        case 32: return launch_multi_k<32>(a, num_sms, st);
+        case 48: return launch_multi_k<48>(a, num_sms, st);
+        case 64: return launch_multi_k<64>(a, num_sms, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_psd_tc(const PsdTcArgs& a, int num_sms, cudaStream_t st) {

@@ -253,12 +253,16 @@ typedef struct gp_batch_config {
     int no_graph;            /* 1: launch each iteration's kernels directly instead of replaying a CUDA graph */
     int iterations;          /* out: pipeline iterations run */
     double tune_seconds;     /* out: time spent by the tuner (0 when its result was cached) */
+    int multi_launch;        /* 1: one launch per kernel and iteration over every job (lengths
+                                order / compression up to 63); 0: per-job launches on the jobs'
+                                own streams */
 } gp_batch_config;
 
 /* Generation of up to 8 jobs of different orders / compressions at once:
- * one enumerator launch covers every job's rank windows, and each job's
- * filter / finalize kernels run on their own branch of a per-iteration CUDA
- * graph that is captured once and replayed until all windows are done.
+ * one enumerator launch covers every job's rank windows, and the jobs'
+ * filter / finalize kernels run either on one branch per job or (multi_launch)
+ * as one launch each over every job, in a per-iteration CUDA graph that is
+ * captured once and replayed until all windows are done.
  * With autotune != 0 the engine first times its settings on a sample of
  * the jobs and uses (and writes to *cfg) the fastest; otherwise it uses
  * *cfg (or defaults when cfg is NULL).  stats, when not NULL, receives one
@@ -270,7 +274,7 @@ int gp_generate_batch(gp_ctx* ctx, const gp_gen_job* jobs, int njobs, int autotu
 
 /* The settings the tuners chose so far on this context, one line per tuned
  * workload: "batch:<jobs> enum_variant windows_per_thread cand_cap
- * tc_ctas_per_sm use_graph" for gp_generate_batch, "sort:W<words> radix_bits
+ * tc_ctas_per_sm use_graph multi_launch" for gp_generate_batch, "sort:W<words> radix_bits
  * microseconds" for gp_sort (which tunes its radix width per key width on
  * first use).  Writes at most cap bytes (NUL-terminated) to buf; returns the
  * length needed including the NUL.  No counterpart in the reference. */

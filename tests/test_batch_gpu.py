@@ -5,7 +5,8 @@ and a replayed CUDA graph.
 Bar: every job's A and B files are byte-identical to those of the
 reference (golden hashes) or of the oracle over the same word window, and
 do not depend on the engine's settings (graph or direct launches, soft
-capacity, enumerator variant, windows per thread, filter grid, tuner).
+capacity, enumerator variant, windows per thread, filter grid, one launch
+per kernel over all jobs or per-job launches, tuner).
 """
 import ctypes
 import hashlib
@@ -88,6 +89,10 @@ def test_batch_equals_single_windows(default_run, tmp_path):
     {"enum_variant": 2},
     {"windows_per_thread": 4},
     {"tc_ctas_per_sm": 1},
+    {"multi_launch": 1},                     # one launch per kernel over all jobs (K = 16 and 32 tiles)
+    {"multi_launch": 1, "no_graph": 1},
+    {"multi_launch": 1, "cand_cap": 5000},
+    {"multi_launch": 1, "tc_ctas_per_sm": 1},
 ])
 def test_batch_settings_do_not_change_results(default_run, tmp_path, settings):
     files, stats, _ = default_run
@@ -98,6 +103,34 @@ def test_batch_settings_do_not_change_results(default_run, tmp_path, settings):
         assert (a.necklaces, a.candidates, a.psd_pass) == (b.necklaces, b.candidates, b.psd_pass)
     if "cand_cap" in settings:
         assert cfg.iterations > 1
+    assert cfg.multi_launch == settings.get("multi_launch", 0)
+
+
+def test_batch_multi_launch_at_k64(tmp_path):
+    """One filter launch over rows of lengths 17, 19 (K = 32 tiles) and 50
+    (K = 64 tiles, the one-CTA-per-SM instance) gives the files of per-job
+    launches."""
+    jobs = [(34, 2, 0, 0, 3 ** 17), (100, 2, 0, 271828182845904523, 271828182845904523 + (1 << 24)),
+            (57, 3, -2, 1 << 30, (1 << 30) + (1 << 22))]
+    with gp.Context(0) as ctx:
+        per_job, st1, _ = run_batch(ctx, tmp_path, "p", jobs=jobs)
+        multi, st2, cfg = run_batch(ctx, tmp_path, "m", jobs=jobs, multi_launch=1, cand_cap=1 << 18)
+    assert cfg.multi_launch == 1 and cfg.iterations > 1
+    assert multi == per_job
+    for a, b in zip(st1, st2):
+        assert (a.necklaces, a.candidates, a.psd_pass) == (b.necklaces, b.candidates, b.psd_pass)
+    assert sum(len(a) + len(b) for a, b in multi) > 0
+
+
+def test_batch_multi_launch_rejects_long_rows(tmp_path):
+    """Rows of length 68 need K = 80, beyond the multi-job filter (K <= 64): asking
+    for one launch is an error, the per-job engine runs them."""
+    jobs = [(68, 1, 0, 0, 1 << 20), (34, 2, 0, 0, 1 << 20)]
+    with gp.Context(0) as ctx:
+        with pytest.raises(gp.GPError):
+            run_batch(ctx, tmp_path, "r", jobs=jobs, multi_launch=1)
+        _, _, cfg = run_batch(ctx, tmp_path, "q", jobs=jobs)
+        assert cfg.multi_launch == 0
 
 
 def test_batch_autotune_is_cached_and_exact(default_run, tmp_path):
@@ -123,17 +156,21 @@ def test_batch_rejects_bad_jobs(tmp_path):
             ctx.generate_batch([(16, 2, 0, 0, 10, tmp_path / "a", tmp_path / "b")] * 9)  # more than 8 jobs
 
 
-@pytest.mark.parametrize("size", [1 << 24, 1 << 32])
-def test_uneven_batch_windows_match_reference(golden_manifest, tmp_path, size):
+@pytest.mark.parametrize("size,multi", [(1 << 24, 0), (1 << 24, 1), (1 << 32, None)])
+def test_uneven_batch_windows_match_reference(golden_manifest, tmp_path, size, multi):
     """The uneven batch (orders 34, 50, 58, 68 at compression 2, 90 at
     compression 5) over its seed-chosen windows, against the reference's own
     generation functions run over the same windows (the bench's workload at
-    2^32 words)."""
+    2^32 words): per-job launches, one launch per kernel over all jobs
+    (K = 32 and 48 tiles), and the tuner's choice."""
     from golaypair_gb300.workloads import batch_windows
     wins = batch_windows(size)
     recs = golden_manifest["windows"]
+    kw = {"autotune": True} if multi is None else {"multi_launch": multi}
     with gp.Context(0) as ctx:
-        files, stats, _ = run_batch(ctx, tmp_path, "w", jobs=wins, autotune=size > (1 << 24))
+        files, stats, cfg = run_batch(ctx, tmp_path, "w", jobs=wins, **kw)
+    if multi is not None:
+        assert cfg.multi_launch == multi
     for i, (w, (a, b), st) in enumerate(zip(wins, files, stats)):
         rec = recs["%d/%d/%d/%d-%d" % tuple(w)]
         assert st.necklaces == rec["necklaces"], w
