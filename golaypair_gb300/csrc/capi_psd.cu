@@ -129,37 +129,39 @@ int gp_ctx::enqueue_filter_multi(const gp::RowSrc* src, const int64_t* cap, cons
                                  uint32_t* const* d_unsure, unsigned long long* const* d_ucount, int njobs,
                                  int grid_per_sm, cudaStream_t st) {
     if (njobs < 1 || njobs > gp::kMaxTcJobs) return fail(GP_ERR_ARG, "multi-job filter: %d jobs", njobs);
-    gp::PsdTcMultiArgs a{};
+    gp::PsdTcMultiArgs m{};
     gp::RecheckMultiArgs r{};
-    a.njobs = r.njobs = njobs;
-    a.grid_per_sm = grid_per_sm;
-    a.status = status.as<int>();
+    m.njobs = r.njobs = njobs;
+    m.grid_per_sm = grid_per_sm;
     for (int j = 0; j < njobs; ++j) {
         const int L = src[j].L;
         if (!src[j].words || !gp::tc_multi_supported(L, src[j].pack_bits))
             return fail(GP_ERR_UNSUPPORTED, "multi-job filter: length %d x %d bits", L, src[j].pack_bits);
-        const int K = gp::tc_k_for_len(L);
-        // the per-row error bounds of the packed rows (as psd_tc_kernel forms them)
-        const float coef = gp::tc_err_coef(K);
         const double* tw = twiddle64(L);
         const void* img = twiddle_image(L);
         if (!tw || !img) return fail(GP_ERR_NOMEM, "multi-job filter: twiddle tables for length %d", L);
-        gp::PsdTcJob& q = a.job[j];
-        q.words = src[j].words;
-        q.n_dev = n_dev[j];
-        q.cap = cap[j];
-        q.L = L;
-        q.K = K;
-        q.bits = src[j].pack_bits;
-        q.alpha_c = src[j].alpha_c;
-        q.thr = (float)threshold(order[j], paf[j]);
-        q.guard_cfg = guard_band(order[j]);
-        q.dc_hi = (coef + 3.4527e-4f) * (float)L * (float)src[j].alpha_c;
-        q.dc_lo = coef * (float)L * (float)src[j].alpha_c;
-        q.bimage = img;
-        q.mask = d_mask[j];
-        q.unsure = d_unsure[j];
-        q.unsure_count = d_ucount[j];
+        // each job's arguments as enqueue_filter_dev forms them
+        gp::PsdTcArgs& a = m.job[j];
+        a.seqs = nullptr;
+        a.words = src[j].words;
+        a.pack_bits = src[j].pack_bits;
+        a.alpha_c = src[j].alpha_c;
+        a.n = cap[j];
+        a.n_dev = n_dev[j];
+        a.grid_per_sm = grid_per_sm;
+        a.L = L;
+        a.bimage = img;
+        a.thr = (float)threshold(order[j], paf[j]);
+        a.guard_cfg = guard_band(order[j]);
+        a.err_coef = gp::tc_err_coef(gp::tc_k_for_len(L));
+        a.mask = d_mask[j];
+        a.mask_words = (cap[j] + 31) / 32;
+        a.unsure = d_unsure[j];
+        a.unsure_count = d_ucount[j];
+        a.unsure_cap = cap[j];
+        a.psd_out = nullptr;
+        a.status = status.as<int>();
+        a.trace = nullptr;
         gp::RecheckJob& w = r.job[j];
         w.src = src[j];
         w.tw = tw;
@@ -169,7 +171,7 @@ int gp_ctx::enqueue_filter_multi(const gp::RowSrc* src, const int64_t* cap, cons
         w.cap = cap[j];
         w.mask = d_mask[j];
     }
-    GP_CUDA_TRY(this, gp::launch_psd_tc_multi(a, num_sms, st));
+    GP_CUDA_TRY(this, gp::launch_psd_tc_multi(m, num_sms, st));
     GP_CUDA_TRY(this, gp::launch_psd_recheck_multi(r, num_sms, st));
     return GP_OK;
 }

@@ -85,32 +85,18 @@ float tc_err_coef(int K);              // |X| error per unit of sum|x|
 
 cudaError_t launch_psd_tc(const PsdTcArgs& a, int num_sms, cudaStream_t st);
 
-// One job of a multi-job tensor-core filter launch: packed words of one
-// length / alphabet, their own twiddle image (at the job's own padded K) and
-// their own verdict outputs.  Tiles never straddle jobs.
+// Several jobs' tensor-core filters (packed words, lengths up to 63) in one
+// launch: each CTA serves one job for its whole life, with that job's
+// one-job kernel body; CTAs are shared out in proportion to the jobs' tile
+// counts read on the device.  Every job as for launch_psd_tc (n = its
+// capacity, n_dev its count), one status word for all.
 constexpr int kMaxTcJobs = 8;
 constexpr int kMaxMultiK = 64;  // largest padded K of a multi-job launch
-struct PsdTcJob {
-    const uint4* words;
-    const unsigned long long* n_dev;  // rows of this launch (read on the device), at most cap
-    int64_t cap;
-    int L, K, bits, alpha_c;          // K = tc_k_for_len(L); value = 2 * digit - alpha_c
-    float thr;                        // 2n - paf + 0.001
-    float guard_cfg;                  // configured guard band
-    float dc_hi, dc_lo;               // per-row |X| error bounds: hi twiddles alone, hi + lo
-    const void* bimage;               // the job's twiddle image (build_twiddle_image(L, K))
-    uint32_t* mask;                   // ceil(cap / 32) words
-    uint32_t* unsure;
-    unsigned long long* unsure_count;
-};
 struct PsdTcMultiArgs {
-    PsdTcJob job[kMaxTcJobs];
+    PsdTcArgs job[kMaxTcJobs];
     int njobs;
     int grid_per_sm;  // CTAs per SM (0 = as many as fit)
-    int* status;
 };
-// Every job's rows in one launch (one persistent grid over all jobs' tiles,
-// each tile at its job's K).
 cudaError_t launch_psd_tc_multi(const PsdTcMultiArgs& a, int num_sms, cudaStream_t st);
 // True when a multi-job launch takes packed rows of length L with b bits per
 // digit (padded K at most kMaxMultiK).
