@@ -107,6 +107,7 @@ _STAGE_SIGS = {
     "gp_match": [_P, _i32, _i32, _i32, _cp, _cp, _cp, _i32, _P],
     "gp_uncompress": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp],
     "gp_uncompress_lines": [_P, _i32, _i32, _i32, _i32, _cp, _cp, _cp, _cp, _i64, _i64, _i64],
+    "gp_uncompress_chain": [_P, _i32, _P, _i32, _i32, _cp, _P, _i64, _i64, _i64],
     "gp_equiv_filter": [_P, _i32, _i32, _cp, _cp],
     "gp_set_output_format": [_P, _i32],
     "gp_export_text": [_P, _cp, _cp],

@@ -557,6 +557,113 @@ __global__ void __launch_bounds__(256) ux_join_kernel(JoinArgs a) {
     }
 }
 
+// ------------------------------------------------------------ side planning
+// uncompression.cpp:107-142, one thread per side of a compressed pair:
+//  * the rotation: the first distinct letter (ascending value) with the most
+//    partitions; the sequence is rotated left by i whenever position i holds
+//    that letter, on the already rotated sequence (the reference's loop);
+//  * the rows: the letter's index at every position, plus A at position 0
+//    (the first entry's partitions reduced to rotation/reversal minima);
+//  * the bins that are multiples of r: the compressed sequence's DFT, the
+//    same for every expansion, checked once in FP64 (no fused multiply-add,
+//    as the host's loop);
+//  * the expansion count and the split into scan prefixes and the suffix
+//    table (the trailing free positions whose combinations fit smax).
+struct PlanOut {
+    uint64_t total;         // expansions (0: none can pass)
+    uint64_t prefix_count;  // total / suffix_count
+    uint32_t nsuf, suffix_count, free_choices, overflow;
+};
+
+struct PlanArgs {
+    const uint8_t* seqs;     // [sides][L] letter indices (validated on the host)
+    int n_sides, L, A, Lnew, n_cbins, smax;
+    const int* cbins;        // [n_cbins]
+    const int* cnt;          // [2A] choices per row
+    const double2* tw;       // [Lnew] (cos, sin)(2 pi m / Lnew)
+    const int8_t* letter;    // [A] value of each letter index
+    const uint8_t* asc;      // [A] letter indices by ascending value
+    double thr;
+    uint8_t* rows;           // [sides][L]
+    PlanOut* out;            // [sides]
+};
+
+__global__ void __launch_bounds__(128) ux_plan_kernel(PlanArgs a) {
+    const int64_t sid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (sid >= a.n_sides) return;
+    const int L = a.L;
+    uint8_t x[kMaxL], y[kMaxL];
+    uint32_t present = 0;
+    for (int i = 0; i < L; ++i) {
+        x[i] = a.seqs[sid * L + i];
+        present |= 1u << x[i];
+    }
+    int best = x[0], best_n = 0;
+    for (int t = 0; t < a.A; ++t) {
+        const int e = a.asc[t];
+        if (!((present >> e) & 1u)) continue;
+        if (a.cnt[e] > best_n) {
+            best_n = a.cnt[e];
+            best = e;
+        }
+    }
+    for (int i = 0; i < L; ++i) {
+        if (x[i] != best) continue;
+        for (int j = 0; j < L; ++j) y[j] = x[j + i < L ? j + i : j + i - L];
+        for (int j = 0; j < L; ++j) x[j] = y[j];
+    }
+    uint8_t* rows = a.rows + sid * L;
+    for (int i = 0; i < L; ++i) rows[i] = (uint8_t)(x[i] + (i == 0 ? a.A : 0));
+    PlanOut o{0, 0, 0, 1, 0, 0};
+    bool pass = true;
+    for (int b = 0; b < a.n_cbins && pass; ++b) {
+        const int k = a.cbins[b];
+        double re = 0.0, im = 0.0;
+        for (int i = 0; i < L; ++i) {
+            const int m = (int)(((long long)i * k) % a.Lnew);
+            const double v = (double)a.letter[x[i]];
+            re = __dadd_rn(re, __dmul_rn(v, a.tw[m].x));
+            im = __dsub_rn(im, __dmul_rn(v, a.tw[m].y));
+        }
+        pass = !(__dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)) > a.thr);
+    }
+    if (pass) {
+        uint64_t total = 1;
+        for (int i = 0; i < L && total; ++i) {
+            const uint64_t n = (uint64_t)a.cnt[rows[i]];
+            if (n == 0) {
+                total = 0;
+            } else if (total > (kRankMask >> 1) / n) {
+                o.overflow = 1;
+                total = 0;
+            } else {
+                total *= n;
+            }
+        }
+        if (total) {
+            uint32_t sc = 1, nsuf = 0, fc = 0;
+            bool fits = true;
+            for (int i = L - 1; i >= 0; --i) {
+                const uint32_t n = (uint32_t)a.cnt[rows[i]];
+                if (n <= 1) continue;
+                fc += n;
+                if (fits && (uint64_t)sc * n <= (uint64_t)a.smax) {
+                    sc *= n;
+                    ++nsuf;
+                } else {
+                    fits = false;
+                }
+            }
+            o.total = total;
+            o.nsuf = nsuf;
+            o.suffix_count = sc;
+            o.free_choices = fc;
+            o.prefix_count = total / sc;
+        }
+    }
+    a.out[sid] = o;
+}
+
 // ------------------------------------------------------------ host side
 
 // src/utils/array.cpp:131-160: non-decreasing sequences of length len
@@ -580,7 +687,8 @@ struct Level {
     int order = 0, c = 0, cn = 0, paf = 0, L = 0, r = 0, Lnew = 0, H = 0, nb = 0, np = 0;
     int A = 0, nrows = 0, dmax = 0, smax = 0;
     std::vector<int> alpha, nalpha;
-    std::map<int, int> letter_index;
+    std::map<int, int> letter_index;  // letter value -> index into alpha
+    std::vector<uint8_t> asc;         // letter indices by ascending value
     std::vector<std::vector<std::vector<int>>> rowparts;  // [row][choice] -> r values
     std::vector<int> bins;     // varying bins
     std::vector<int> cbins;    // bins that are multiples of r (constant per side)
@@ -641,6 +749,7 @@ int build_level(gp_ctx* c, Level& lv, int order, int compress, int new_compress,
         lv.rowparts[a] = list;
         lv.rowparts[lv.A + a] = std::vector<std::vector<int>>(first.begin(), first.end());
     }
+    for (auto& kv : lv.letter_index) lv.asc.push_back((uint8_t)kv.second);  // std::map: ascending values
     lv.nrows = 2 * lv.A;
     lv.dmax = 1;
     for (auto& row : lv.rowparts) lv.dmax = std::max<int>(lv.dmax, (int)row.size());
@@ -752,66 +861,68 @@ struct Side {
     uint32_t free_choices = 0;  // choices summed over the free positions (the scan's term table)
 };
 
-// src/core/uncompression/uncompression.cpp:107-142: rotation, rows, sizes.
-int plan_side(gp_ctx* c, const Level& lv, std::vector<int> orig, Side& sd) {
+// Plans every side on the device (ux_plan_kernel) from the sides' letter
+// indices (2 per pair), and copies the plans back: the host batches the
+// pairs by expansion count and sizes the scan's shared memory from them.
+int plan_sides(gp_ctx* c, const Level& lv, const std::vector<uint8_t>& seqs, std::vector<Side>& sides,
+               cudaStream_t s) {
     const int L = lv.L;
-    for (int v : orig)
-        if (!lv.letter_index.count(v))
-            return c->fail(GP_ERR_FORMAT, "uncompress: value %d is not a letter of compression %d", v, lv.c);
-    // first distinct element (ascending) with the most partitions
-    std::set<int> distinct(orig.begin(), orig.end());
-    size_t best_n = 0;
-    int best = orig[0];
-    for (int e : distinct) {
-        const size_t n = lv.rowparts[lv.letter_index.at(e)].size();
-        if (n > best_n) {
-            best_n = n;
-            best = e;
-        }
+    const int64_t ns = (int64_t)seqs.size() / L;
+    sides.assign(ns, Side{});
+    if (ns == 0) return GP_OK;
+    if (ns > INT32_MAX) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %lld sides", (long long)ns);
+    std::vector<double2> tw(lv.Lnew);
+    for (int m = 0; m < lv.Lnew; ++m) tw[m] = make_double2(lv.cs[m], lv.sn[m]);
+    std::vector<int8_t> letter(lv.A);
+    for (int i = 0; i < lv.A; ++i) letter[i] = (int8_t)lv.alpha[i];
+    DevBuf &dseq = c->ux[23], &drows = c->ux[24], &dout = c->ux[25], &dcb = c->ux[26], &dtw = c->ux[27],
+           &dlet = c->ux[28], &dasc = c->ux[29], &dcnt = c->ux[30];
+    std::vector<int> cnt(lv.nrows);
+    for (int row = 0; row < lv.nrows; ++row) cnt[row] = (int)lv.rowparts[row].size();
+    if (!dseq.ensure(seqs.size()) || !drows.ensure(seqs.size()) || !dout.ensure((size_t)ns * sizeof(PlanOut)) ||
+        !dcb.ensure(lv.cbins.size() * 4 + 4) || !dtw.ensure(tw.size() * 16) || !dlet.ensure(16) ||
+        !dasc.ensure(16) || !dcnt.ensure(cnt.size() * 4))
+        return c->fail(GP_ERR_NOMEM, "uncompress: planning buffers");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dseq.p, seqs.data(), seqs.size(), cudaMemcpyHostToDevice, s));
+    if (!lv.cbins.empty())
+        GP_CUDA_TRY(c, cudaMemcpyAsync(dcb.p, lv.cbins.data(), lv.cbins.size() * 4, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dtw.p, tw.data(), tw.size() * 16, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dlet.p, letter.data(), letter.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dasc.p, lv.asc.data(), lv.asc.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dcnt.p, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, s));
+    PlanArgs pa{};
+    pa.seqs = dseq.as<uint8_t>();
+    pa.n_sides = (int)ns;
+    pa.L = L;
+    pa.A = lv.A;
+    pa.Lnew = lv.Lnew;
+    pa.n_cbins = (int)lv.cbins.size();
+    pa.smax = lv.smax;
+    pa.cbins = dcb.as<int>();
+    pa.cnt = dcnt.as<int>();
+    pa.tw = dtw.as<double2>();
+    pa.letter = dlet.as<int8_t>();
+    pa.asc = dasc.as<uint8_t>();
+    pa.thr = lv.thr;
+    pa.rows = drows.as<uint8_t>();
+    pa.out = dout.as<PlanOut>();
+    ux_plan_kernel<<<(unsigned)((ns + 127) / 128), 128, 0, s>>>(pa);
+    GP_CUDA_TRY(c, cudaGetLastError());
+    std::vector<uint8_t> rows(seqs.size());
+    std::vector<PlanOut> po(ns);
+    GP_CUDA_TRY(c, cudaMemcpyAsync(rows.data(), drows.p, rows.size(), cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(po.data(), dout.p, (size_t)ns * sizeof(PlanOut), cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    for (int64_t k = 0; k < ns; ++k) {
+        if (po[k].overflow) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: more than 2^39 expansions of one side");
+        Side& sd = sides[k];
+        sd.rows.assign(rows.begin() + k * L, rows.begin() + (k + 1) * L);
+        sd.total = po[k].total;
+        sd.prefix_count = po[k].prefix_count;
+        sd.nsuf = po[k].nsuf;
+        sd.suffix_count = po[k].suffix_count;
+        sd.free_choices = po[k].free_choices;
     }
-    // rotate left by i whenever orig[i] == best, on the already rotated sequence
-    for (int i = 0; i < L; ++i)
-        if (orig[i] == best) std::rotate(orig.begin(), orig.begin() + i, orig.end());
-    sd.rows.resize(L);
-    for (int i = 0; i < L; ++i) sd.rows[i] = (uint8_t)(lv.letter_index.at(orig[i]) + (i == 0 ? lv.A : 0));
-    // bins that are multiples of r equal the compressed sequence's DFT:
-    // the same for every expansion, checked here in FP64
-    for (int k : lv.cbins) {
-        double re = 0, im = 0;
-        for (int i = 0; i < L; ++i) {
-            const int m = (int)(((long long)i * k) % lv.Lnew);
-            re += orig[i] * lv.cs[m];
-            im -= orig[i] * lv.sn[m];
-        }
-        if (re * re + im * im > lv.thr) {
-            sd.total = 0;
-            return GP_OK;
-        }
-    }
-    uint64_t total = 1;
-    std::vector<int> free_cnt;
-    for (int i = 0; i < L; ++i) {
-        const uint64_t n = lv.rowparts[sd.rows[i]].size();
-        if (n == 0) {
-            sd.total = 0;
-            return GP_OK;
-        }
-        if (total > (kRankMask >> 1) / n) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: more than 2^39 expansions of one side");
-        total *= n;
-        if (n > 1) free_cnt.push_back((int)n);
-    }
-    sd.total = total;
-    // suffix table: the trailing free positions whose combinations fit
-    uint32_t sc = 1, nsuf = 0;
-    for (int f = (int)free_cnt.size() - 1; f >= 0; --f) {
-        if ((uint64_t)sc * (uint64_t)free_cnt[f] > (uint64_t)lv.smax) break;
-        sc *= (uint32_t)free_cnt[f];
-        ++nsuf;
-    }
-    sd.nsuf = nsuf;
-    sd.suffix_count = sc;
-    for (int n : free_cnt) sd.free_choices += (uint32_t)n;
-    sd.prefix_count = total / sc;
     return GP_OK;
 }
 
@@ -907,6 +1018,13 @@ unsigned grid_for(uint64_t n, unsigned cap) {
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(g, cap));
 }
 
+// A matched pair of expansions: its two candidate lines (the reference's
+// sorted scratch files' order), the output line and the two sequences.
+struct Match {
+    std::string la, lb, line;
+    std::vector<int> xa, xb;
+};
+
 // The engine over consecutive pairs [p0, p1): device scratch in ux[4..].
 struct Batcher {
     gp_ctx* c;
@@ -917,8 +1035,8 @@ struct Batcher {
     ScanKernel scan;
     int scan_blocks = 0;
     size_t smem = 0;
-    // matched (a line, b line, pair line) per pair of the batch
-    std::vector<std::vector<std::array<std::string, 3>>> out;
+    // the matched pairs of each pair of the batch, in output order
+    std::vector<std::vector<Match>> out;
 
     // Runs the batch; on overflow of a device list returns GP_ERR_OVERFLOW
     // with *overflowed set, so the caller can halve the batch.
@@ -1086,7 +1204,7 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     GP_CUDA_TRY(c, cudaMemcpy(hm.data(), dm.p, nm * 16, cudaMemcpyDeviceToHost));
     // signatures of the matched expansions; the reference joins on the
     // signature string, which the PAF condition implies up to FP64 rounding
-    std::vector<std::array<std::string, 3>> items(nm);
+    std::vector<Match> items(nm);
     std::vector<char> keep(nm, 0);
     std::vector<int64_t> pair_of(nm);
     auto work = [&](uint64_t lo, uint64_t hi) {
@@ -1102,7 +1220,7 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
             pair_of[m] = side_a >> 1;
             if (signature_token(la) != signature_token(lb)) continue;
             keep[m] = 1;
-            items[m] = {la, lb, sa_ + " " + sb_ + "\n"};
+            items[m] = Match{la, lb, sa_ + " " + sb_ + "\n", xa, xb};
         }
     };
     const unsigned nt = (unsigned)std::min<uint64_t>(16, (nm + 63) / 64);
@@ -1116,113 +1234,76 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     for (uint64_t m = 0; m < nm; ++m)
         if (keep[m]) out[pair_of[m]].push_back(std::move(items[m]));
     for (auto& v : out)
-        std::sort(v.begin(), v.end(), [](const std::array<std::string, 3>& p, const std::array<std::string, 3>& q) {
-            return p[0] != q[0] ? p[0] < q[0] : p[1] < q[1];
-        });
+        std::sort(v.begin(), v.end(),
+                  [](const Match& p, const Match& q) { return p.la != q.la ? p.la < q.la : p.lb < q.lb; });
     return GP_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int gp_uncompress(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
-                  const char* out_pairs, const char* work_dir, const char* prefix) {
-    return gp_uncompress_lines(c, order, compress, new_compress, paf, in_pairs, out_pairs, work_dir, prefix, 0,
-                               INT64_MAX, 1);
-}
-
-static int gp_uncompress_lines_impl(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
-                        const char* out_pairs, const char* work_dir, const char* prefix, int64_t first, int64_t end_line,
-                        int64_t step) {
-    StageRange nvtx_range("gp_uncompress");
-    if (!c || !in_pairs || !out_pairs) return GP_ERR_ARG;
-    if (first < 0 || step < 1) return c->fail(GP_ERR_ARG, "uncompress: bad line range (first %lld, step %lld)",
-                                              (long long)first, (long long)step);
-    (void)work_dir;
-    (void)prefix;
-    cudaSetDevice(c->device);
-    // the reference constructs its PairReader / PairWriter before the
-    // pipeline runs (src/main.cpp:122-123): the output is truncated even
-    // when nothing is uncompressed
-    FILE* out = fopen(out_pairs, "w");
-    if (!out) return c->fail(GP_ERR_IO, "uncompress: cannot open %s", out_pairs);
-    if (compress <= 1) {  // uncompression.cpp:42
-        fclose(out);
-        return GP_OK;
-    }
-    if (new_compress < 1 || compress % new_compress || order % compress) {
-        fclose(out);
-        return c->fail(GP_ERR_ARG, "uncompress: compression %d -> %d of order %d", compress, new_compress, order);
-    }
-    std::string text;
-    if (!slurp(in_pairs, text)) {
-        fclose(out);
-        return GP_OK;  // an unreadable input yields no pairs (the reader is simply not good)
-    }
-    Level lv;
-    int rc = build_level(c, lv, order, compress, new_compress, paf);
-    if (rc) {
-        fclose(out);
-        return rc;
-    }
+// The selected lines of a pair file as letter indices, 2L per pair.
+// io.cpp:52-55: a line of the wrong length is an error, the pairs before it
+// are still uncompressed and written (format_rc).  A value that is not a
+// letter of the compression is an error before anything is written.
+int parse_pairs(gp_ctx* c, const Level& lv, const std::string& text, int64_t first, int64_t end_line, int64_t step,
+                std::vector<uint8_t>& seqs, int& format_rc) {
     const int L = lv.L;
-    // parse the selected lines; io.cpp:52-55: a line of the wrong length is
-    // an error, the pairs before it are still written
-    std::vector<Side> sides;
-    int format_rc = GP_OK;
-    {
-        const char* p = text.data();
-        const char* end = p + text.size();
-        int64_t line_no = 0;
-        std::vector<int> vals;
-        while (p < end) {
-            const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
-            if (!nl) nl = end;
-            const int64_t this_line = line_no;
-            if (this_line < first || this_line >= end_line || (this_line - first) % step != 0) {
-                ++line_no;
-                p = nl + 1;
-                if (this_line >= end_line) break;
-                continue;
-            }
-            vals.clear();
-            const char* q = p;
-            while (q < nl) {
-                while (q < nl && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
-                if (q >= nl) break;
-                char* e2;
-                const long v = strtol(q, &e2, 10);
-                if (e2 == q) break;
-                vals.push_back((int)v);
-                q = e2;
-            }
-            p = nl + 1;
-            if ((int)vals.size() != 2 * L) {
-                format_rc = c->fail(GP_ERR_FORMAT, "PairReader: input line %lld: length is %zu. Expected %d",
-                                    (long long)line_no, vals.size(), 2 * L);
-                break;
-            }
+    const char* p = text.data();
+    const char* end = p + text.size();
+    int64_t line_no = 0;
+    std::vector<int> vals;
+    while (p < end) {
+        const char* nl = (const char*)memchr(p, '\n', (size_t)(end - p));
+        if (!nl) nl = end;
+        const int64_t this_line = line_no;
+        if (this_line < first || this_line >= end_line || (this_line - first) % step != 0) {
             ++line_no;
-            for (int h = 0; h < 2; ++h) {
-                Side sd;
-                rc = plan_side(c, lv, std::vector<int>(vals.begin() + h * L, vals.begin() + (h + 1) * L), sd);
-                if (rc) break;
-                sides.push_back(std::move(sd));
-            }
-            if (rc) break;
+            p = nl + 1;
+            if (this_line >= end_line) break;
+            continue;
+        }
+        vals.clear();
+        const char* q = p;
+        while (q < nl) {
+            while (q < nl && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
+            if (q >= nl) break;
+            char* e2;
+            const long v = strtol(q, &e2, 10);
+            if (e2 == q) break;
+            vals.push_back((int)v);
+            q = e2;
+        }
+        p = nl + 1;
+        if ((int)vals.size() != 2 * L) {
+            format_rc = c->fail(GP_ERR_FORMAT, "PairReader: input line %lld: length is %zu. Expected %d",
+                                (long long)line_no, vals.size(), 2 * L);
+            break;
+        }
+        ++line_no;
+        for (int v : vals) {
+            const auto it = lv.letter_index.find(v);
+            if (it == lv.letter_index.end())
+                return c->fail(GP_ERR_FORMAT, "uncompress: value %d is not a letter of compression %d", v, lv.c);
+            seqs.push_back((uint8_t)it->second);
         }
     }
-    if (rc) {
-        fclose(out);
-        return rc;
-    }
-    const int64_t npairs = (int64_t)sides.size() / 2;
+    return GP_OK;
+}
+
+// One level over the pairs in seqs (letter indices, 2L per pair): plans the
+// sides on the device, runs the engine in batches of consecutive pairs,
+// writes the matched pairs to out and, when next is set, appends their
+// sequences (values, 2 L' per pair, in output order) for the next level.
+int run_level(gp_ctx* c, const Level& lv, const std::vector<uint8_t>& seqs, FILE* out, std::vector<int8_t>* next) {
     cudaStream_t s = c->s_comp;
+    std::vector<Side> sides;
+    int rc = plan_sides(c, lv, seqs, sides, s);
+    if (rc) return rc;
+    const int64_t npairs = (int64_t)sides.size() / 2;
+    if (npairs == 0) return GP_OK;
     LevelDev ld{};
-    if (npairs) rc = upload_level(c, lv, ld, s);
+    rc = upload_level(c, lv, ld, s);
+    if (rc) return rc;
     Batcher bt{c, lv, ld, sides, s, scan_kernel_for(lv.np)};
-    if (!rc && npairs) {
+    {
         // shared memory of the scan: the largest suffix table and term table
         // any side of this call needs (a few tens of KB: several CTAs per SM)
         uint64_t max_sc = 1, max_fc = 0;
@@ -1237,14 +1318,14 @@ static int gp_uncompress_lines_impl(gp_ctx* c, int order, int compress, int new_
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bt.scan, kScanThreads, bt.smem);
         if (e != cudaSuccess || per_sm < 1)
-            rc = c->fail(GP_ERR_CUDA, "uncompress: scan kernel occupancy (%s)", cudaGetErrorString(e));
+            return c->fail(GP_ERR_CUDA, "uncompress: scan kernel occupancy (%s)", cudaGetErrorString(e));
         bt.scan_blocks = c->num_sms * std::max(1, per_sm);
     }
     // batches of consecutive pairs, by expansions; a batch whose device
     // lists overflow is split in half and run again
     constexpr uint64_t kBatchExpansions = uint64_t(1) << 35;
     std::vector<std::pair<int64_t, int64_t>> todo;
-    for (int64_t p = 0; p < npairs && !rc;) {
+    for (int64_t p = 0; p < npairs;) {
         int64_t q = p;
         uint64_t tot = 0;
         while (q < npairs && (q == p || (tot + sides[2 * q].total + sides[2 * q + 1].total <= kBatchExpansions &&
@@ -1257,7 +1338,7 @@ static int gp_uncompress_lines_impl(gp_ctx* c, int order, int compress, int new_
     }
     std::reverse(todo.begin(), todo.end());
     std::string buf;
-    while (!rc && !todo.empty()) {
+    while (!todo.empty()) {
         const auto [p0, p1] = todo.back();
         todo.pop_back();
         bool over = false;
@@ -1266,19 +1347,108 @@ static int gp_uncompress_lines_impl(gp_ctx* c, int order, int compress, int new_
             const int64_t mid = p0 + (p1 - p0) / 2;
             todo.emplace_back(mid, p1);
             todo.emplace_back(p0, mid);
-            rc = GP_OK;
             continue;
         }
-        if (rc == GP_ERR_OVERFLOW && over) rc = c->fail(GP_ERR_OVERFLOW, "uncompress: one pair overflows the device lists");
-        if (rc) break;
+        if (rc == GP_ERR_OVERFLOW && over) return c->fail(GP_ERR_OVERFLOW, "uncompress: one pair overflows the device lists");
+        if (rc) return rc;
         buf.clear();
         for (auto& v : bt.out)
-            for (auto& it : v) buf += it[2];
-        if (!buf.empty()) fwrite(buf.data(), 1, buf.size(), out);
+            for (auto& m : v) {
+                buf += m.line;
+                if (next) {
+                    for (int x : m.xa) next->push_back((int8_t)x);
+                    for (int x : m.xb) next->push_back((int8_t)x);
+                }
+            }
+        if (!buf.empty() && fwrite(buf.data(), 1, buf.size(), out) != buf.size())
+            return c->fail(GP_ERR_IO, "uncompress: write failed");
     }
-    cudaStreamSynchronize(s);
-    fclose(out);
-    return rc ? rc : format_rc;
+    return GP_OK;
+}
+
+// The levels compress[0] -> compress[1] -> ... of one chain (src/main.cpp:
+// 117-139 runs uncompress_pipeline once per level, each reading the file
+// the previous one wrote).  Level 0 reads the selected lines of in_pairs;
+// each later level takes the previous level's pairs from memory, in the
+// order they were written, so its input equals the file the previous level
+// wrote.  Every level's file is written.
+int uncompress_chain_impl(gp_ctx* c, int order, const int* compress, int ncomp, int paf, const char* in_pairs,
+                                 const char* const* out_pairs, int64_t first, int64_t end_line, int64_t step) {
+    StageRange nvtx_range("gp_uncompress");
+    if (!c || !compress || ncomp < 2 || !in_pairs || !out_pairs) return GP_ERR_ARG;
+    for (int i = 0; i + 1 < ncomp; ++i)
+        if (!out_pairs[i]) return GP_ERR_ARG;
+    if (first < 0 || step < 1) return c->fail(GP_ERR_ARG, "uncompress: bad line range (first %lld, step %lld)",
+                                              (long long)first, (long long)step);
+    cudaSetDevice(c->device);
+    std::vector<int8_t> carried;  // the previous level's pairs (values), 2 L per pair
+    bool have_input = true;
+    for (int lvl = 0; lvl + 1 < ncomp; ++lvl) {
+        const int cc = compress[lvl], cn = compress[lvl + 1];
+        // the reference constructs its PairReader / PairWriter before the
+        // pipeline runs (src/main.cpp:122-123): the output is truncated even
+        // when nothing is uncompressed
+        FILE* out = fopen(out_pairs[lvl], "w");
+        if (!out) return c->fail(GP_ERR_IO, "uncompress: cannot open %s", out_pairs[lvl]);
+        struct Closer {
+            FILE* f;
+            ~Closer() { fclose(f); }
+        } closer{out};
+        std::vector<int8_t> next;
+        if (cc <= 1) {  // uncompression.cpp:42
+            carried.clear();
+            continue;
+        }
+        if (cn < 1 || cc % cn || order % cc)
+            return c->fail(GP_ERR_ARG, "uncompress: compression %d -> %d of order %d", cc, cn, order);
+        Level lv;
+        int rc = build_level(c, lv, order, cc, cn, paf);
+        if (rc) return rc;
+        std::vector<uint8_t> seqs;
+        int format_rc = GP_OK;
+        if (lvl == 0) {
+            std::string text;
+            // an unreadable input yields no pairs (the reader is simply not good)
+            have_input = slurp(in_pairs, text);
+            if (have_input) rc = parse_pairs(c, lv, text, first, end_line, step, seqs, format_rc);
+            if (rc) return rc;
+        } else {
+            seqs.reserve(carried.size());
+            for (int8_t v : carried) {
+                const auto it = lv.letter_index.find(v);
+                if (it == lv.letter_index.end())
+                    return c->fail(GP_ERR_FORMAT, "uncompress: value %d is not a letter of compression %d", v, cc);
+                seqs.push_back((uint8_t)it->second);
+            }
+        }
+        const bool more = lvl + 2 < ncomp;
+        rc = run_level(c, lv, seqs, out, more ? &next : nullptr);
+        if (rc) return rc;
+        if (format_rc) return format_rc;  // the chain stops at a malformed input line
+        carried.swap(next);
+    }
+    return GP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gp_uncompress(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
+                  const char* out_pairs, const char* work_dir, const char* prefix) {
+    return gp_uncompress_lines(c, order, compress, new_compress, paf, in_pairs, out_pairs, work_dir, prefix, 0,
+                               INT64_MAX, 1);
+}
+
+static int gp_uncompress_lines_impl(gp_ctx* c, int order, int compress, int new_compress, int paf, const char* in_pairs,
+                                    const char* out_pairs, const char* work_dir, const char* prefix, int64_t first,
+                                    int64_t end_line, int64_t step) {
+    (void)work_dir;
+    (void)prefix;
+    if (!c || !in_pairs || !out_pairs) return GP_ERR_ARG;
+    const int comps[2] = {compress, new_compress};
+    const char* outs[1] = {out_pairs};
+    return uncompress_chain_impl(c, order, comps, 2, paf, in_pairs, outs, first, end_line, step);
 }
 
 // No C++ exception (an allocation failure on a huge input) crosses the C ABI.
@@ -1286,6 +1456,15 @@ int gp_uncompress_lines(gp_ctx* c, int order, int compress, int new_compress, in
                         const char* work_dir, const char* prefix, int64_t first, int64_t end_line, int64_t step) {
     try {
         return gp_uncompress_lines_impl(c, order, compress, new_compress, paf, in_pairs, out_pairs, work_dir, prefix, first, end_line, step);
+    } catch (const std::exception& e) {
+        return c ? c->fail(GP_ERR_NOMEM, "uncompress: %s", e.what()) : GP_ERR_NOMEM;
+    }
+}
+
+int gp_uncompress_chain(gp_ctx* c, int order, const int* compress, int ncomp, int paf, const char* in_pairs,
+                        const char* const* out_pairs, int64_t first, int64_t end_line, int64_t step) {
+    try {
+        return uncompress_chain_impl(c, order, compress, ncomp, paf, in_pairs, out_pairs, first, end_line, step);
     } catch (const std::exception& e) {
         return c ? c->fail(GP_ERR_NOMEM, "uncompress: %s", e.what()) : GP_ERR_NOMEM;
     }

@@ -188,28 +188,28 @@ int stage_match(const Options& o, const MatchOpts& m) {
     return 0;
 }
 
-// src/main.cpp:117-139
+// src/main.cpp:117-139: every level of the chain in one call; level i
+// reads the pairs of level i - 1 from memory and writes its own file
 int stage_uncompress(const Options& o, const UncompressOpts& u) {
-    for (size_t i = 0; i + 1 < o.compress.size(); ++i) {
-        const std::string prefix = i == 0 ? u.input_prefix : u.output_prefix;
-        const std::string in = match_file(o, prefix, (int)i);
-        const std::string out = match_file(o, u.output_prefix, (int)i + 1);
-        int64_t first = 0, end = INT64_MAX, step = 1;
-        if (i == 0) {
-            if (u.line >= 1) {
-                first = u.line - 1;
-                end = u.line;
-            } else {
-                first = u.range_begin;
-                end = u.range_end >= 0 ? u.range_end : INT64_MAX;
-                step = u.range_step;
-            }
-        }
-        const int rc = gp_uncompress_lines(g_ctx, o.order, o.compress[i], o.compress[i + 1], o.paf_constant,
-                                           in.c_str(), out.c_str(), o.work_dir().c_str(), u.temp_prefix.c_str(),
-                                           first, end, step);
-        if (rc < 0) return die("uncompress", rc);
+    const int nlev = (int)o.compress.size() - 1;
+    if (nlev < 1) return 0;
+    const std::string in = match_file(o, u.input_prefix, 0);
+    std::vector<std::string> outs;
+    for (int i = 0; i < nlev; ++i) outs.push_back(match_file(o, u.output_prefix, i + 1));
+    std::vector<const char*> out_ptrs;
+    for (auto& s : outs) out_ptrs.push_back(s.c_str());
+    int64_t first = 0, end = INT64_MAX, step = 1;
+    if (u.line >= 1) {
+        first = u.line - 1;
+        end = u.line;
+    } else {
+        first = u.range_begin;
+        end = u.range_end >= 0 ? u.range_end : INT64_MAX;
+        step = u.range_step;
     }
+    const int rc = gp_uncompress_chain(g_ctx, o.order, o.compress.data(), (int)o.compress.size(), o.paf_constant,
+                                       in.c_str(), out_ptrs.data(), first, end, step);
+    if (rc < 0) return die("uncompress", rc);
     return 0;
 }
 

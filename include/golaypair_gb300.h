@@ -329,6 +329,17 @@ int gp_uncompress_lines(gp_ctx* ctx, int order, int compress, int new_compress, 
                         const char* out_pairs, const char* work_dir, const char* prefix, int64_t first,
                         int64_t end_line, int64_t step);
 
+/* A whole chain compress[0] -> compress[1] -> ... -> compress[ncomp-1]
+ * (ncomp >= 2), as src/main.cpp:117-139 runs uncompress_pipeline once per
+ * level: level i writes out_pairs[i] (ncomp - 1 paths).  Level 0 reads the
+ * selected lines of in_pairs (first, end_line, step as gp_uncompress_lines);
+ * each later level takes the previous level's pairs from memory, in the
+ * order they were written, instead of reading the file back.  The files
+ * equal those of one gp_uncompress_lines call per level.  A malformed line
+ * of in_pairs stops the chain after level 0 with GP_ERR_FORMAT. */
+int gp_uncompress_chain(gp_ctx* ctx, int order, const int* compress, int ncomp, int paf, const char* in_pairs,
+                        const char* const* out_pairs, int64_t first, int64_t end_line, int64_t step);
+
 /*
  * Replaces int cache_filter(int ORDER, int COMPRESS, const std::string& in,
  * const std::string& out) (src/core/filter/filter.h, filter.cpp:18-163):

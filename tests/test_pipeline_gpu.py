@@ -166,6 +166,46 @@ def test_uncompress_line_ranges_split_the_work(tmp_path, golden_manifest):
     assert sorted(both.splitlines()) == sorted(full.splitlines())
 
 
+def test_uncompress_chain_equals_level_by_level(tmp_path, golden_manifest):
+    """gp_uncompress_chain runs 4 -> 2 -> 1 at order 32 with the middle
+    level's pairs handed over in memory; its two files equal the
+    reference's (golden hashes) and one gp_uncompress_lines call per level
+    reading the file back.  A line range applies to the first level only."""
+    golay(["32", "-c", "4", "2", "1", "gen", "sort", "match"], tmp_path)
+    wd = os.path.join(str(tmp_path), "order-32")
+    p4 = os.path.join(wd, "32-pairs-4")
+    meta = golden_manifest["runs"]["n32_c421"]["files"]
+    big = 2 ** 63 - 1
+    with gp.Context(0) as ctx:
+        L = ctx._lib
+
+        def chain(outs, first=0, end=big, step=1):
+            comps = (ctypes.c_int * 3)(4, 2, 1)
+            paths = (ctypes.c_char_p * 2)(*[o.encode() for o in outs])
+            ctx.check(L.gp_uncompress_chain(ctx.handle, 32, ctypes.cast(comps, ctypes.c_void_p), 3, 0, p4.encode(),
+                                            ctypes.cast(paths, ctypes.c_void_p), first, end, step),
+                      "gp_uncompress_chain")
+
+        def level(src, dst, c, cn, first=0, end=big, step=1):
+            ctx.check(L.gp_uncompress_lines(ctx.handle, 32, c, cn, 0, src.encode(), dst.encode(), wd.encode(), b"",
+                                            first, end, step), "gp_uncompress_lines")
+
+        c2, c1 = os.path.join(wd, "chain-2"), os.path.join(wd, "chain-1")
+        chain([c2, c1])
+        assert hashlib.sha256(read(c2)).hexdigest() == meta["32-pairs-2"]["sha256"]
+        assert hashlib.sha256(read(c1)).hexdigest() == meta["32-pairs-1"]["sha256"]
+        l2, l1 = os.path.join(wd, "lvl-2"), os.path.join(wd, "lvl-1")
+        level(p4, l2, 4, 2)
+        level(l2, l1, 2, 1)
+        assert read(l2) == read(c2) and read(l1) == read(c1)
+        # every third input line from line 1
+        chain([c2, c1], first=1, step=3)
+        level(p4, l2, 4, 2, first=1, step=3)
+        level(l2, l1, 2, 1)
+        assert read(l2) == read(c2) and read(l1) == read(c1)
+        assert len(read(c1)) > 0
+
+
 def _filter_gpu_vs_oracle(oracle_lib, tmp_path, order, pairs_file):
     with gp.Context(0) as ctx:
         ctx.check(ctx._lib.gp_equiv_filter(ctx.handle, order, 1, str(pairs_file).encode(),
