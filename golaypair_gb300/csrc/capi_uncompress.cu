@@ -10,9 +10,10 @@
 // files, sorts both and merge-joins them on the signature string with an
 // exact PAF check.  Here many pairs are uncompressed per launch sequence:
 //
-// 1. Host plan (uncompression.cpp:88-142): one partition table per letter,
-//    the reference's rotation of each side, its first entry's partitions
-//    reduced to rotation/reversal minima.  A side is a mixed-radix number
+// 1. Plan (uncompression.cpp:88-142): one partition table per letter and the
+//    first entry's partitions reduced to rotation/reversal minima (host, once
+//    per level); the reference's rotation of each side, its rows and counts
+//    (ux_plan_kernel, one thread per side).  A side is a mixed-radix number
 //    over its positions; the expansion of rank t has digit d_i at position i.
 //
 // 2. ux_scan_kernel (fused expansion + PSD filter).  The DFT of an expansion
@@ -20,7 +21,7 @@
 //    C_i(d, k) = sum_q v_q(d) w^((i + L q) k), w = exp(-2 pi i / L').  Bins
 //    k that are multiples of the ratio r = c / c' do not depend on the
 //    expansion (they are the compressed sequence's DFT) and are checked once
-//    per side on the host.  For the other bins a thread adds the terms of the
+//    per side when it is planned.  For the other bins a thread adds the terms of the
 //    side's leading free positions once (its "prefix"), then walks a table of
 //    precomputed sums over the trailing free positions (the "suffix", up to a
 //    few hundred combinations in shared memory): one packed fp32 add per bin
