@@ -10,6 +10,7 @@
 // The host then orders each role's records by word (the reference's FKM
 // order) and writes the candidate files.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -258,8 +259,19 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     const int64_t target = threads * std::max(1, cfg.windows_per_thread);
     double total_words = 0;
     for (auto& j : jobs) total_words += (double)range_words(j);
-    std::vector<uint4> cur, end;
-    std::vector<uint8_t> wjob;
+    // Each range is cut into windows of wsize words (the last one shorter);
+    // the windows are laid out job by job, range by range, and built by
+    // host threads over chunks of consecutive windows (each chunk steps its
+    // own rank counter from its first window).
+    struct Chunk {
+        int ji;
+        gp::u128 r0, r1, wsize;  // the range and the job's window size
+        int64_t w0, nw;          // first window of the chunk (in its range), count
+        int64_t out;             // index of its first window in cur / end / wjob
+    };
+    std::vector<Chunk> chunks;
+    int64_t nwin = 0;
+    constexpr int64_t kChunkWindows = 8192;
     for (int ji = 0; ji < nj; ++ji) {
         JobRun& j = jobs[ji];
         const gp::u128 words = range_words(j);
@@ -268,27 +280,49 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
         if (nw < 256) nw = 256;
         gp::u128 wsize = words / (gp::u128)nw;
         if (wsize < 1) wsize = 1;
-        const gp::u128 space = gp::upow(j.p.k, j.p.L);
-        const gp::u128 maxw = gp::rank_to_word(space - 1, j.p.k, j.p.b, j.p.L);
         for (auto& r : j.ranges) {
             if (r.first >= r.second) continue;
-            gp::RankStepper step(r.first, wsize < space ? wsize : space, j.p.k, j.p.b, j.p.L);
-            for (gp::u128 lo = r.first; lo < r.second; lo += wsize) {
-                const bool whole = lo + wsize <= r.second;  // the window ends wsize words on
-                const gp::u128 hi = whole ? lo + wsize : r.second;
-                cur.push_back(to_u4(step.word()));
-                step.advance();
-                if (hi >= space)
-                    end.push_back(to_u4(maxw + 1));
-                else if (whole)
-                    end.push_back(to_u4(step.word()));
-                else
-                    end.push_back(to_u4(gp::rank_to_word(hi, j.p.k, j.p.b, j.p.L)));
-                wjob.push_back((uint8_t)ji);
+            const int64_t n = (int64_t)((r.second - r.first + wsize - 1) / wsize);
+            for (int64_t w0 = 0; w0 < n; w0 += kChunkWindows) {
+                chunks.push_back({ji, r.first, r.second, wsize, w0, std::min(kChunkWindows, n - w0), nwin});
+                nwin += std::min(kChunkWindows, n - w0);
             }
         }
     }
-    const int64_t nwin = (int64_t)cur.size();
+    std::vector<uint4> cur(nwin), end(nwin);
+    std::vector<uint8_t> wjob(nwin);
+    {
+        std::atomic<size_t> next{0};
+        auto work = [&]() {
+            for (size_t ci = next++; ci < chunks.size(); ci = next++) {
+                const Chunk& ch = chunks[ci];
+                const GenPlan& p = jobs[ch.ji].p;
+                const gp::u128 space = gp::upow(p.k, p.L);
+                const gp::u128 maxw = gp::rank_to_word(space - 1, p.k, p.b, p.L);
+                gp::u128 lo = ch.r0 + (gp::u128)ch.w0 * ch.wsize;
+                gp::RankStepper step(lo, ch.wsize < space ? ch.wsize : space, p.k, p.b, p.L);
+                for (int64_t i = 0; i < ch.nw; ++i, lo += ch.wsize) {
+                    const bool whole = lo + ch.wsize <= ch.r1;  // the window ends wsize words on
+                    const gp::u128 hi = whole ? lo + ch.wsize : ch.r1;
+                    const int64_t o = ch.out + i;
+                    cur[o] = to_u4(step.word());
+                    step.advance();
+                    if (hi >= space)
+                        end[o] = to_u4(maxw + 1);
+                    else if (whole)
+                        end[o] = to_u4(step.word());
+                    else
+                        end[o] = to_u4(gp::rank_to_word(hi, p.k, p.b, p.L));
+                    wjob[o] = (uint8_t)ch.ji;
+                }
+            }
+        };
+        const unsigned nt = (unsigned)std::min<size_t>(chunks.size(), std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nt; ++t) th.emplace_back(work);
+        work();
+        for (auto& t : th) t.join();
+    }
     t_win = since(tb);
     // ---- capacities and the device arena
     // appends after a job met its soft cap: a lane sees the count at most 16
@@ -715,10 +749,12 @@ int plan_for(gp_ctx* c, int order, int compress, int paf, GenPlan& p) {
 
 int finish(gp_ctx* c, const GenPlan& p, const RecordSet& ra, const RecordSet& rb, const char* path_a,
            const char* path_b, gp_gen_stats* st) {
-    int rc = write_records(c, p, ra, 0, path_a);
-    if (rc) return rc;
-    rc = write_records(c, p, rb, 1, path_b);
-    if (rc) return rc;
+    int rc_a = GP_OK;
+    std::thread ta([&] { rc_a = write_records(c, p, ra, 0, path_a); });  // A and B files side by side
+    const int rc_b = write_records(c, p, rb, 1, path_b);
+    ta.join();
+    if (rc_a) return rc_a;
+    if (rc_b) return rc_b;
     st->written_a = (int64_t)ra.size();
     st->written_b = (int64_t)rb.size();
     return GP_OK;
@@ -1031,9 +1067,17 @@ extern "C" int gp_generate_batch(gp_ctx* c, const gp_gen_job* jobs, int njobs, i
     int rc = run_batch(c, run, bc, &iters);
     if (rc) return rc;
     const auto tf = std::chrono::steady_clock::now();
-    for (int i = 0; i < njobs; ++i) {
-        rc = finish(c, run[i].p, run[i].ra, run[i].rb, jobs[i].path_a, jobs[i].path_b, &run[i].st);
-        if (rc) return rc;
+    {
+        // the jobs' files in parallel (each file is formatted by host threads too)
+        std::vector<int> rcs(njobs, GP_OK);
+        std::vector<std::thread> th;
+        for (int i = 0; i < njobs; ++i)
+            th.emplace_back([&, i] {
+                rcs[i] = finish(c, run[i].p, run[i].ra, run[i].rb, jobs[i].path_a, jobs[i].path_b, &run[i].st);
+            });
+        for (auto& t : th) t.join();
+        for (int i = 0; i < njobs; ++i)
+            if (rcs[i]) return rcs[i];
     }
     if (getenv("GP_GEN_TIMING")) fprintf(stderr, "[gen] files %.4f s\n", since(tf));
     const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstdint>
 #include <map>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -103,6 +104,7 @@ struct gp_ctx {
     cudaEvent_t ev_h2d[2] = {nullptr, nullptr};
     cudaEvent_t ev_done[2] = {nullptr, nullptr};
     std::string err;
+    std::mutex err_mu;
     // status word and counters (device)
     DevBuf status;          // int
     DevBuf counts;          // unsigned long long [8]
@@ -152,6 +154,7 @@ struct gp_ctx {
         va_start(ap, fmt);
         vsnprintf(buf, sizeof buf, fmt, ap);
         va_end(ap);
+        std::lock_guard<std::mutex> lock(err_mu);  // host threads of one call may fail together
         err = buf;
         return code;
     }
