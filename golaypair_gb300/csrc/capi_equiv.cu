@@ -18,11 +18,14 @@
 // reference's in-order erase loop (filter.cpp:117-144) on those class sizes
 // and member lists.
 #include <algorithm>
+#include <chrono>
 #include <stdexcept>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ctx.h"
@@ -365,38 +368,93 @@ static int gp_equiv_filter_impl(gp_ctx* c, int order, int compress, const char* 
     if (pair_group_size(L, compress) * (uint64_t)(2 * W) > kMaxGroupBytes)
         return c->fail(GP_ERR_UNSUPPORTED, "equivalence filter: %llu generators at length %d exceed %llu bytes",
                        (unsigned long long)pair_group_size(L, compress), L, (unsigned long long)kMaxGroupBytes);
+    // GP_EQUIV_TIMING=1 in the environment prints the phase times to stderr (diagnostics)
+    static const bool timing = getenv("GP_EQUIV_TIMING") != nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](const char* what) {
+        if (timing)
+            fprintf(stderr, "[equiv] %s %.4f s\n", what,
+                    std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+    };
     FILE* out = fopen(out_path, "w");  // filter.cpp:24 opens the output first
     FILE* in = fopen(in_path, "rb");
     if (!in) {
         if (out) fclose(out);
         return GP_OK;  // filter.cpp:33-37: "Bad File." and success
     }
-    // filter.cpp:45-62: L values for a, then (if the stream is still good) L for b
+    // the generator group depends only on (L, compression): built on a host
+    // thread while the pairs are read and sorted
+    std::vector<int16_t> gens;
+    bool group_failed = false;
+    std::thread group_thread([&] {
+        try {
+            gens = pair_generators(L, compress);
+        } catch (const std::exception&) {
+            group_failed = true;
+        }
+    });
+    struct Joiner {
+        std::thread& t;
+        ~Joiner() {
+            if (t.joinable()) t.join();
+        }
+    } joiner{group_thread};
+    // filter.cpp:45-62: L values for a, then (if the stream is still good) L
+    // for b: whitespace-separated integers up to the first token that is not
+    // one, W per pair, a trailing partial pair dropped
     std::vector<std::vector<int8_t>> P;
     {
+        std::string text;
+        fseek(in, 0, SEEK_END);
+        const long sz = ftell(in);
+        fseek(in, 0, SEEK_SET);
+        text.resize(sz > 0 ? (size_t)sz : 0);
+        text.resize(sz > 0 ? fread(&text[0], 1, (size_t)sz, in) : 0);
+        fclose(in);
         std::vector<int8_t> cur;
-        long v;
-        while (fscanf(in, "%ld", &v) == 1) {
+        const char* q = text.c_str();
+        for (;;) {
+            char* e;
+            const long v = strtol(q, &e, 10);
+            if (e == q) break;
+            q = e;
             cur.push_back((int8_t)v);
             if ((int)cur.size() == W) {
                 P.push_back(cur);
                 cur.clear();
             }
         }
-        fclose(in);
     }
+    lap("read");
     std::sort(P.begin(), P.end());
     P.erase(std::unique(P.begin(), P.end()), P.end());
     const int64_t np = (int64_t)P.size();
     std::vector<char> alive(np, 1);
     if (np > 0) {
-        const auto gens = pair_generators(L, compress);
+        lap("sort");
+        group_thread.join();
+        if (group_failed) {
+            if (out) fclose(out);
+            return c->fail(GP_ERR_NOMEM, "equivalence filter: generator group of length %d", L);
+        }
+        lap("group");
         const int64_t ng = (int64_t)(gens.size() / (size_t)W);
         std::vector<int16_t> items((size_t)ng * W);  // transposed: items[o * ng + g]
-        for (int64_t g = 0; g < ng; ++g) {
-            const auto s = as_sources(gens.data() + (size_t)g * W, L);
-            for (int o = 0; o < W; ++o) items[(size_t)o * ng + g] = s[o];
+        {
+            const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+            std::vector<std::thread> th;
+            for (unsigned t = 0; t < nt; ++t)
+                th.emplace_back([&, t] {
+                    // blocks of 64 generators: each thread writes whole cache lines of every row
+                    for (int64_t g0 = (int64_t)t * 64; g0 < ng; g0 += (int64_t)nt * 64)
+                        for (int64_t g = g0; g < std::min<int64_t>(g0 + 64, ng); ++g) {
+                            const auto s = as_sources(gens.data() + (size_t)g * W, L);
+                            for (int o = 0; o < W; ++o) items[(size_t)o * ng + g] = s[o];
+                        }
+                });
+            for (auto& x : th) x.join();
         }
+        lap("table");
         std::vector<int8_t> pairs((size_t)np * W);
         for (int64_t i = 0; i < np; ++i)
             for (int j = 0; j < W; ++j) pairs[i * W + j] = P[i][j];
@@ -453,6 +511,7 @@ static int gp_equiv_filter_impl(gp_ctx* c, int order, int compress, const char* 
         }
         GP_CUDA_TRY(c, cudaGetLastError());
         GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+        lap("classes");
         int rc = c->check_status("equivalence filter");
         if (rc) {
             if (out) fclose(out);
@@ -499,16 +558,36 @@ static int gp_equiv_filter_impl(gp_ctx* c, int order, int compress, const char* 
             }
         }
     }
+    lap("erase");
     if (out) {
+        // "%d " per entry of a, " ", "%d " per entry of b, newline
+        std::string buf;
+        buf.reserve((size_t)np * (3 * W + 2));
+        auto put = [&](int v) {
+            if (v < 0) {
+                buf.push_back('-');
+                v = -v;
+            }
+            char tmp[8];
+            int n = 0;
+            do {
+                tmp[n++] = (char)('0' + v % 10);
+                v /= 10;
+            } while (v);
+            while (n) buf.push_back(tmp[--n]);
+            buf.push_back(' ');
+        };
         for (int64_t i = 0; i < np; ++i) {
             if (!alive[i]) continue;
-            for (int k = 0; k < L; ++k) fprintf(out, "%d ", P[i][k]);
-            fprintf(out, " ");
-            for (int k = 0; k < L; ++k) fprintf(out, "%d ", P[i][L + k]);
-            fprintf(out, "\n");
+            for (int k = 0; k < L; ++k) put(P[i][k]);
+            buf.push_back(' ');
+            for (int k = 0; k < L; ++k) put(P[i][L + k]);
+            buf.push_back('\n');
         }
-        fclose(out);
+        const bool ok = buf.empty() || fwrite(buf.data(), 1, buf.size(), out) == buf.size();
+        if (fclose(out) != 0 || !ok) return c->fail(GP_ERR_IO, "equivalence filter: write failed: %s", out_path);
     }
+    lap("written");
     return GP_OK;
 }
 

@@ -54,12 +54,48 @@ void format_line(std::string& out, const GenPlan& p, gp::u128 word, const uint16
 int write_records_binary(gp_ctx* c, const GenPlan& p, const RecordSet& recs, const std::vector<uint32_t>& order,
                          int role, const char* path);
 
+// Sorts v with cmp: host threads sort equal chunks, then merge them pairwise
+// in rounds (every merge of a round on its own thread).
+template <class T, class Cmp>
+void parallel_sort(std::vector<T>& v, Cmp cmp) {
+    const size_t n = v.size();
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (n < (size_t(1) << 16) || hw == 1) {
+        std::sort(v.begin(), v.end(), cmp);
+        return;
+    }
+    std::vector<size_t> bounds;
+    for (unsigned t = 0; t <= hw; ++t) bounds.push_back(n * t / hw);
+    {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < hw; ++t)
+            th.emplace_back([&, t] { std::sort(v.begin() + bounds[t], v.begin() + bounds[t + 1], cmp); });
+        for (auto& x : th) x.join();
+    }
+    std::vector<T> tmp(n);
+    while (bounds.size() > 2) {
+        std::vector<size_t> nb;
+        std::vector<std::thread> th;
+        for (size_t i = 0; i + 1 < bounds.size(); i += 2) {
+            const size_t lo = bounds[i], mid = bounds[i + 1], hi = i + 2 < bounds.size() ? bounds[i + 2] : mid;
+            nb.push_back(lo);
+            th.emplace_back([&, lo, mid, hi] {
+                std::merge(v.begin() + lo, v.begin() + mid, v.begin() + mid, v.begin() + hi, tmp.begin() + lo, cmp);
+            });
+        }
+        nb.push_back(n);
+        for (auto& x : th) x.join();
+        v.swap(tmp);
+        bounds.swap(nb);
+    }
+}
+
 int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, int role, const char* path) {
     const size_t n = recs.size();
     const int S = p.L - 1;
     std::vector<uint32_t> order(n);
     for (size_t i = 0; i < n; ++i) order[i] = (uint32_t)i;
-    std::sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return recs.words[x] < recs.words[y]; });
+    parallel_sort(order, [&](uint32_t x, uint32_t y) { return recs.words[x] < recs.words[y]; });
     if (c->out_format == GP_FORMAT_BINARY) return write_records_binary(c, p, recs, order, role, path);
     FILE* f = fopen(path, "w");
     if (!f) return c->fail(GP_ERR_IO, "cannot open %s for writing", path);
@@ -68,14 +104,15 @@ int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, int role, 
     unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     if (nblocks < nthreads) nthreads = (unsigned)std::max<size_t>(1, nblocks);
     bool ok = true;
-    // rounds of nthreads blocks: format in parallel, write in order
-    std::vector<std::string> bufs(nthreads);
-    for (size_t b0 = 0; b0 < nblocks && ok; b0 += nthreads) {
-        const unsigned m = (unsigned)std::min<size_t>(nthreads, nblocks - b0);
+    // rounds of nthreads blocks: format in parallel, write in order; the
+    // next round is formatted while this one is written
+    std::vector<std::string> bufs[2] = {std::vector<std::string>(nthreads), std::vector<std::string>(nthreads)};
+    auto format_round = [&](size_t b0, std::vector<std::string>& bs) {
         std::vector<std::thread> th;
+        const unsigned m = (unsigned)std::min<size_t>(nthreads, nblocks - b0);
         for (unsigned t = 0; t < m; ++t) {
-            th.emplace_back([&, t] {
-                std::string& out = bufs[t];
+            th.emplace_back([&, t, b0] {
+                std::string& out = bs[t];
                 out.clear();
                 const size_t lo = (b0 + t) * per_block, hi = std::min(n, lo + per_block);
                 out.reserve((hi - lo) * (size_t)(4 * p.L + 8));
@@ -85,9 +122,18 @@ int write_records(gp_ctx* c, const GenPlan& p, const RecordSet& recs, int role, 
                 }
             });
         }
+        return th;
+    };
+    if (nblocks) {
+        std::vector<std::thread> th = format_round(0, bufs[0]);
+        for (size_t b0 = 0, r = 0; b0 < nblocks; b0 += nthreads, r ^= 1) {
+            for (auto& x : th) x.join();
+            const unsigned m = (unsigned)std::min<size_t>(nthreads, nblocks - b0);
+            th = b0 + nthreads < nblocks ? format_round(b0 + nthreads, bufs[r ^ 1]) : std::vector<std::thread>();
+            for (unsigned t = 0; t < m && ok; ++t)
+                if (fwrite(bufs[r][t].data(), 1, bufs[r][t].size(), f) != bufs[r][t].size()) ok = false;
+        }
         for (auto& x : th) x.join();
-        for (unsigned t = 0; t < m; ++t)
-            if (fwrite(bufs[t].data(), 1, bufs[t].size(), f) != bufs[t].size()) ok = false;
     }
     ok = (fclose(f) == 0) && ok;
     return ok ? GP_OK : c->fail(GP_ERR_IO, "write failed: %s", path);
@@ -987,8 +1033,10 @@ int gp_generate(gp_ctx* c, int order, int compress, int paf, int proc_id, int pr
     rc = run_batch(c, jobs, single_job_cfg(), nullptr);
     if (rc) return rc;
     st = jobs[0].st;
+    const auto tf = std::chrono::steady_clock::now();
     rc = finish(c, p, jobs[0].ra, jobs[0].rb, path_a, path_b, &st);
     if (rc) return rc;
+    if (getenv("GP_GEN_TIMING")) fprintf(stderr, "[gen] files %.4f s\n", since(tf));
     st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = st;
     return GP_OK;
