@@ -51,6 +51,7 @@
 #include <set>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "ctx.h"
@@ -128,14 +129,23 @@ struct ScanArgs {
 
 __device__ __forceinline__ void flag_overflow(int* status) { atomicCAS(status, 0, GP_KSTATUS_OVERFLOW); }
 
-// CTAs per SM the registers are capped for: up to 20 varying bins, 64
-// registers and four CTAs (measured 6 % faster than three at order 57);
-// wider prefix sums need more registers per thread.
-constexpr int scan_min_ctas(int np) { return np <= 10 ? 4 : np <= 12 ? 3 : np <= 24 ? 2 : 1; }
+// CTAs per SM the registers are capped for.  Up to 8 varying bins (one
+// phase): 64 registers, four CTAs.  Two phases (below), up to 24 bins: three
+// CTAs, 80 registers, no spills (at order 57, 20 bins: 8.5-8.6 s for the
+// whole file against 9.7-9.8 s at four CTAs with spills, and 9.9 s for the
+// one-phase scan at four CTAs).  Wider prefix sums need more registers.
+constexpr int scan_min_ctas(int np) { return np <= 4 ? 4 : np <= 12 ? 3 : np <= 24 ? 2 : 1; }
 
-template <int NP>
+template <int V>
+using Int = std::integral_constant<int, V>;
+
+// NA: bin pairs of the scan's first phase (0: one phase over all NP)
+template <int NP, int NA>
 __global__ void __launch_bounds__(kScanThreads, scan_min_ctas(NP)) ux_scan_kernel(ScanArgs a) {
     extern __shared__ float4 smem[];
+    // the queue of phase B, per warp: (suffix | lane << 16) and the phase-A max
+    __shared__ uint32_t s_qitem[kScanThreads / 32][NA ? 96 : 1];
+    __shared__ float s_qmax[kScanThreads / 32][NA ? 96 : 1];
     __shared__ int s_nfree, s_npre;
     __shared__ uint32_t s_scount;
     __shared__ int s_pos[kMaxL], s_cnt[kMaxL], s_coff[kMaxL];
@@ -265,14 +275,14 @@ __global__ void __launch_bounds__(kScanThreads, scan_min_ctas(NP)) ux_scan_kerne
                 }
             }
         }
-        const uint64_t rank0 = pidx * (uint64_t)scount;
+        const uint64_t unit_pidx0 = (u - a.unit_begin[side]) * (uint64_t)kScanThreads + (uint64_t)(tid & ~31);
         const float init = active ? 0.f : __int_as_float(0x7f800000);
-        // max p over the varying bins of prefix + suffix j
-        auto eval = [&](uint32_t j) {
+        // max p over bin pairs [P0, P1) of prefix + suffix j
+        auto eval_range = [&](uint32_t j, auto p0c, auto p1c, float m0, float m1) {
+            constexpr int P0 = decltype(p0c)::value, P1 = decltype(p1c)::value;
             const float4* S = s_S + j * NP;
-            float m0 = init, m1 = init;
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
+            for (int p = P0; p < P1; ++p) {
                 const float4 s = S[p];
                 const float2 xr = __fadd2_rn(Pr[p], make_float2(s.x, s.y));
                 const float2 xi = __fadd2_rn(Pi[p], make_float2(s.z, s.w));
@@ -285,8 +295,9 @@ __global__ void __launch_bounds__(kScanThreads, scan_min_ctas(NP)) ux_scan_kerne
             return fmaxf(m0, m1);
         };
         // survivors (sure passes) and the band around the bound (unsure),
-        // appended with one atomic per warp and list
-        auto emit = [&](float m, uint32_t j) {
+        // appended with one atomic per warp and list; rank: the expansion's
+        // rank within its side
+        auto emit = [&](float m, uint64_t rank) {
             const bool cand = m <= a.thr_hi;
             const unsigned bal = __ballot_sync(0xFFFFFFFFu, cand);
             if (!bal) return;
@@ -305,7 +316,7 @@ __global__ void __launch_bounds__(kScanThreads, scan_min_ctas(NP)) ux_scan_kerne
             base_u = __shfl_sync(0xFFFFFFFFu, base_u, 0);
             if (cand) {
                 const unsigned lt = (1u << lane) - 1u;
-                const uint64_t val = ((uint64_t)side << kRankBits) | (rank0 + j);
+                const uint64_t val = ((uint64_t)side << kRankBits) | rank;
                 if (sure) {
                     const unsigned long long pos = base_s + __popc(bs & lt);
                     if (pos < a.surv_cap)
@@ -321,15 +332,108 @@ __global__ void __launch_bounds__(kScanThreads, scan_min_ctas(NP)) ux_scan_kerne
                 }
             }
         };
-        uint32_t j = 0;
-        for (; j + 2 <= scount; j += 2) {  // two independent suffixes per step
-            const float ma = eval(j), mb = eval(j + 1);
-            if (__any_sync(0xFFFFFFFFu, ma <= a.thr_hi || mb <= a.thr_hi)) {
-                emit(ma, j);
-                emit(mb, j + 1);
+        if constexpr (NA == 0) {
+            const uint64_t rank0 = pidx * (uint64_t)scount;
+            uint32_t j = 0;
+            for (; j + 2 <= scount; j += 2) {  // two independent suffixes per step
+                const float ma = eval_range(j, Int<0>{}, Int<NP>{}, init, init);
+                const float mb = eval_range(j + 1, Int<0>{}, Int<NP>{}, init, init);
+                if (__any_sync(0xFFFFFFFFu, ma <= a.thr_hi || mb <= a.thr_hi)) {
+                    emit(ma, rank0 + j);
+                    emit(mb, rank0 + j + 1);
+                }
+            }
+            if (j < scount) emit(eval_range(j, Int<0>{}, Int<NP>{}, init, init), rank0 + j);
+        } else {
+            // Two phases.  Phase A: the first NA bin pairs of every (prefix,
+            // suffix); most expansions are already above the bound there.
+            // The others are queued per warp as (suffix, lane); phase B takes
+            // 32 queued expansions at a time, one per lane, fetches the
+            // prefix's remaining bin pairs from the queuing lane's registers
+            // by shuffle and finishes the max.  Same max, same verdicts.
+            uint32_t* qi = s_qitem[tid >> 5];
+            float* qm = s_qmax[tid >> 5];
+            int qn = 0;  // queued entries (the same in every lane)
+            auto phase_b = [&](int n) {
+                const bool have = lane < n;
+                const uint32_t item = have ? qi[lane] : (uint32_t)lane << 16;
+                const uint32_t j = item & 0xFFFFu;
+                const int src = (int)(item >> 16);
+                float m0 = have ? qm[lane] : __int_as_float(0x7f800000), m1 = m0;
+                const float4* S = s_S + j * NP;
+#pragma unroll
+                for (int p = NA; p < NP; ++p) {
+                    const float2 pr = make_float2(__shfl_sync(0xFFFFFFFFu, Pr[p].x, src),
+                                                  __shfl_sync(0xFFFFFFFFu, Pr[p].y, src));
+                    const float2 pi = make_float2(__shfl_sync(0xFFFFFFFFu, Pi[p].x, src),
+                                                  __shfl_sync(0xFFFFFFFFu, Pi[p].y, src));
+                    const float4 sv = S[p];
+                    const float2 xr = __fadd2_rn(pr, make_float2(sv.x, sv.y));
+                    const float2 xi = __fadd2_rn(pi, make_float2(sv.z, sv.w));
+                    const float2 q = __ffma2_rn(xr, xr, __fmul2_rn(xi, xi));
+                    if (p & 1)
+                        m1 = max3f(m1, q.x, q.y);
+                    else
+                        m0 = max3f(m0, q.x, q.y);
+                }
+                emit(fmaxf(m0, m1), (unit_pidx0 + (uint64_t)src) * scount + j);
+            };
+            auto push = [&](float m, uint32_t j) {
+                const bool c = m <= a.thr_hi;
+                const unsigned b = __ballot_sync(0xFFFFFFFFu, c);
+                if (c) {
+                    const int slot = qn + __popc(b & ((1u << lane) - 1u));
+                    qi[slot] = j | ((uint32_t)lane << 16);
+                    qm[slot] = m;
+                }
+                qn += __popc(b);
+            };
+            auto drain = [&]() {  // phase B over the first 32 entries; the rest move to the front
+                __syncwarp();
+                phase_b(32);
+                __syncwarp();
+                const int rest = qn - 32;
+                uint32_t i0 = 0, i1 = 0;
+                float m0 = 0.f, m1 = 0.f;
+                if (lane < rest) {
+                    i0 = qi[32 + lane];
+                    m0 = qm[32 + lane];
+                }
+                if (lane + 32 < rest) {
+                    i1 = qi[64 + lane];
+                    m1 = qm[64 + lane];
+                }
+                __syncwarp();
+                if (lane < rest) {
+                    qi[lane] = i0;
+                    qm[lane] = m0;
+                }
+                if (lane + 32 < rest) {
+                    qi[32 + lane] = i1;
+                    qm[32 + lane] = m1;
+                }
+                qn = rest;
+                __syncwarp();
+            };
+            uint32_t j = 0;
+            for (; j + 2 <= scount; j += 2) {  // two independent suffixes per step
+                const float ma = eval_range(j, Int<0>{}, Int<NA>{}, init, init);
+                const float mb = eval_range(j + 1, Int<0>{}, Int<NA>{}, init, init);
+                push(ma, j);
+                push(mb, j + 1);
+                while (qn >= 32) drain();  // below 32 again: the next step's 64 pushes fit the 96 slots
+            }
+            if (j < scount) {
+                push(eval_range(j, Int<0>{}, Int<NA>{}, init, init), j);
+                while (qn >= 32) drain();
+            }
+            if (qn > 0) {
+                __syncwarp();
+                phase_b(qn);
+                qn = 0;
+                __syncwarp();
             }
         }
-        if (j < scount) emit(eval(j), j);
     }
 }
 
@@ -1001,15 +1105,18 @@ using ScanKernel = void (*)(ScanArgs);
 
 ScanKernel scan_kernel_for(int np) {
     switch (np) {
-        case 2: return ux_scan_kernel<2>;
-        case 4: return ux_scan_kernel<4>;
-        case 6: return ux_scan_kernel<6>;
-        case 8: return ux_scan_kernel<8>;
-        case 10: return ux_scan_kernel<10>;
-        case 12: return ux_scan_kernel<12>;
-        case 16: return ux_scan_kernel<16>;
-        case 24: return ux_scan_kernel<24>;
-        case 32: return ux_scan_kernel<32>;
+        case 2: return ux_scan_kernel<2, 0>;
+        case 4: return ux_scan_kernel<4, 0>;
+        // phase A over about 3/5 of the bin pairs (order 57, 10 pairs, whole
+        // file: 6 pairs 8.5-8.6 s, 7 pairs 8.7 s, 5 pairs 8.9 s, 8 pairs 8.9 s,
+        // 4 pairs 9.4 s, 9 pairs 9.3-9.4 s)
+        case 6: return ux_scan_kernel<6, 3>;
+        case 8: return ux_scan_kernel<8, 4>;
+        case 10: return ux_scan_kernel<10, 6>;
+        case 12: return ux_scan_kernel<12, 7>;
+        case 16: return ux_scan_kernel<16, 9>;
+        case 24: return ux_scan_kernel<24, 14>;
+        case 32: return ux_scan_kernel<32, 19>;
     }
     return nullptr;
 }
