@@ -116,6 +116,7 @@ _STAGE_SIGS = {
     "gp_debug_wait_timeout": [_P, _i64],
     "gp_check": [_P, _P],
     "gp_debug_pair_generator_count": [_i32, _i32],
+    "gp_debug_pair_group_check": [_i32, _i32],
 }
 
 

@@ -142,6 +142,177 @@ __global__ void __launch_bounds__(256) class_kernel(ClassArgs a, int splits) {
     }
 }
 
+// ------------------------------------------------------------ canonical forms
+// For L >= 3 every element of the pair group is, on each half of the
+// result, an affine map of one source half: optionally swap the halves,
+// then
+//     a'[i] = (-1)^(alpha i + beta_a) * src_a[(u i + s_a) mod L]
+//     b'[i] = (-1)^(alpha i + beta_b) * src_b[(e u i + s_b) mod L]
+// with u a unit mod L, e = +-1, s_a, s_b any shifts, and the signs only
+// where the alternating negation is a generator (alpha, beta_a, beta_b:
+// 8 patterns).  These 2 * 2 * phi(L) * L^2 (* 8) maps are all in the group
+// (decimation by u, reversal of b, shifts of b and their conjugates by the
+// swap, and the negation of one half, which the alternating negation and an
+// odd shift give) and as many as its order, so they are the group;
+// gp_debug_pair_group_check compares them with the closure.  Two pairs are
+// in one class iff they have the same least image (lexicographic, entries as
+// signed integers), and the class size is the group order over the number of
+// elements that fix the pair.  Per (swap, e, signs, u) the least image takes
+// the least shift of each half separately, so a pair costs
+// O(4 phi(L) (8) L^2) instead of O(|G| L).
+struct CanonArgs {
+    const int8_t* pairs;   // np x W
+    int64_t np;
+    int L;
+    const int16_t* units;  // every unit mod L
+    int nu;
+    int alt;               // 1: the 8 sign patterns
+    int8_t* canon;         // np x W: least image
+    uint32_t* fixers;      // elements fixing the pair
+};
+
+struct Combo {
+    int ha, hb;  // source half of a' and b' (offset 0 or L)
+    int ma, mb;  // multipliers
+    int pa, pb;  // sign pattern: bit 0 alpha, bit 1 beta
+};
+
+__device__ __forceinline__ Combo combo_of(const CanonArgs& a, int c) {
+    const int swap = c & 1;
+    c >>= 1;
+    const int e = c & 1;
+    c >>= 1;
+    int alpha = 0, ba = 0, bb = 0;
+    if (a.alt) {
+        alpha = c & 1;
+        ba = (c >> 1) & 1;
+        bb = (c >> 2) & 1;
+        c >>= 3;
+    }
+    const int u = a.units[c];
+    Combo k;
+    k.ha = swap ? a.L : 0;
+    k.hb = swap ? 0 : a.L;
+    k.ma = u;
+    k.mb = e ? a.L - u : u;
+    k.pa = alpha | (ba << 1);
+    k.pb = alpha | (bb << 1);
+    return k;
+}
+
+// (-1)^(alpha i + beta) for pattern pat
+__device__ __forceinline__ int sign_of(int pat, int i) { return (((pat & 1) & i) ^ (pat >> 1)) ? -1 : 1; }
+
+// Entry o of the image of x under (combo, s_a, s_b).
+__device__ __forceinline__ int image_entry(const int8_t* x, int L, const Combo& k, int sa, int sb, int o) {
+    if (o < L) return sign_of(k.pa, o) * x[k.ha + (int)(((long long)k.ma * o + sa) % L)];
+    const int i = o - L;
+    return sign_of(k.pb, i) * x[k.hb + (int)(((long long)k.mb * i + sb) % L)];
+}
+
+// The least shift of one half, H(s)[i] = sign(i) x[h + (m i + s) mod L],
+// and how many shifts give exactly target.
+__device__ void least_shift(const int8_t* x, int L, int h, int m, int pat, const int8_t* target, int& s_best,
+                            int& n_fix) {
+    s_best = 0;
+    n_fix = 0;
+    for (int s = 0; s < L; ++s) {
+        int cmp = 0;  // sign of H(s) - H(s_best) at the first difference
+        bool eq = true;
+        int i1 = s, i2 = s_best;
+        for (int i = 0; i < L; ++i) {
+            const int sg = sign_of(pat, i);
+            const int v = sg * x[h + i1];
+            if (cmp == 0 && s > 0) {
+                const int w = sg * x[h + i2];
+                if (v != w) cmp = v < w ? -1 : 1;
+            }
+            if (eq && v != target[i]) eq = false;
+            if (!eq && (cmp != 0 || s == 0)) break;
+            i1 += m;
+            i1 -= i1 >= L ? L : 0;
+            i2 += m;
+            i2 -= i2 >= L ? L : 0;
+        }
+        if (cmp < 0) s_best = s;
+        n_fix += eq ? 1 : 0;
+    }
+}
+
+// -1, 0, 1: image (c1, sa1, sb1) against image (c2, sa2, sb2)
+__device__ int compare_images(const CanonArgs& a, const int8_t* x, int c1, int sa1, int sb1, int c2, int sa2,
+                              int sb2) {
+    const Combo k1 = combo_of(a, c1), k2 = combo_of(a, c2);
+    for (int o = 0; o < 2 * a.L; ++o) {
+        const int v = image_entry(x, a.L, k1, sa1, sb1, o), w = image_entry(x, a.L, k2, sa2, sb2, o);
+        if (v != w) return v < w ? -1 : 1;
+    }
+    return 0;
+}
+
+constexpr int kCanonThreads = 128;
+
+__global__ void __launch_bounds__(kCanonThreads) canon_kernel(CanonArgs a) {
+    __shared__ int8_t x[kMaxW];
+    __shared__ int s_c[kCanonThreads], s_sa[kCanonThreads], s_sb[kCanonThreads];
+    __shared__ unsigned s_fix[kCanonThreads / 32];
+    const int L = a.L, W = 2 * L;
+    const int ncombo = 4 * a.nu * (a.alt ? 8 : 1);
+    for (int64_t pr = blockIdx.x; pr < a.np; pr += gridDim.x) {
+        __syncthreads();
+        for (int o = threadIdx.x; o < W; o += blockDim.x) x[o] = a.pairs[pr * W + o];
+        __syncthreads();
+        int bc = -1, bsa = 0, bsb = 0;
+        unsigned fix = 0;
+        for (int c = threadIdx.x; c < ncombo; c += blockDim.x) {
+            const Combo k = combo_of(a, c);
+            int sa, sb, fa, fb;
+            least_shift(x, L, k.ha, k.ma, k.pa, x, sa, fa);
+            least_shift(x, L, k.hb, k.mb, k.pb, x + L, sb, fb);
+            fix += (unsigned)(fa * fb);
+            if (bc < 0 || compare_images(a, x, c, sa, sb, bc, bsa, bsb) < 0) {
+                bc = c;
+                bsa = sa;
+                bsb = sb;
+            }
+        }
+        s_c[threadIdx.x] = bc;
+        s_sa[threadIdx.x] = bsa;
+        s_sb[threadIdx.x] = bsb;
+        fix = __reduce_add_sync(0xFFFFFFFFu, fix);
+        if ((threadIdx.x & 31) == 0) s_fix[threadIdx.x >> 5] = fix;
+        __syncthreads();
+        for (int stride = kCanonThreads / 2; stride > 0; stride >>= 1) {
+            if (threadIdx.x < stride) {
+                const int o = threadIdx.x + stride;
+                if (s_c[o] >= 0 &&
+                    (s_c[threadIdx.x] < 0 || compare_images(a, x, s_c[o], s_sa[o], s_sb[o], s_c[threadIdx.x],
+                                                            s_sa[threadIdx.x], s_sb[threadIdx.x]) < 0)) {
+                    s_c[threadIdx.x] = s_c[o];
+                    s_sa[threadIdx.x] = s_sa[o];
+                    s_sb[threadIdx.x] = s_sb[o];
+                }
+            }
+            __syncthreads();
+        }
+        const Combo k = combo_of(a, s_c[0]);
+        for (int o = threadIdx.x; o < W; o += blockDim.x)
+            a.canon[pr * W + o] = (int8_t)image_entry(x, L, k, s_sa[0], s_sb[0], o);
+        if (threadIdx.x == 0) {
+            unsigned t = 0;
+            for (int w = 0; w < kCanonThreads / 32; ++w) t += s_fix[w];
+            a.fixers[pr] = t;
+        }
+    }
+}
+
+std::vector<int16_t> all_units(int L) {
+    std::vector<int16_t> u;
+    for (int v = 1; v < L; ++v)
+        if (std::gcd(v, L) == 1) u.push_back((int16_t)v);
+    return u;
+}
+
 // Units that generate the group of units mod L (greedy: each one added is
 // not yet in the subgroup generated by the ones before).
 std::vector<int> unit_generators(int L) {
@@ -334,6 +505,70 @@ std::vector<int16_t> as_sources(const int16_t* item, int L) {
     return out;
 }
 
+uint64_t pair_group_size(int L, int compress);
+
+// Class sizes and members of the pairs P (sorted, distinct) by canonical
+// forms on the device (canon_kernel): member_list[span[i].first ..
+// span[i].second) are the pairs with the same least image as pair i (itself
+// included), csize[i] is the group order over the number of elements fixing
+// pair i.  L >= 3.
+int canonical_classes(gp_ctx* c, int L, int compress, const std::vector<std::vector<int8_t>>& P,
+                      std::vector<unsigned long long>& csize, std::vector<uint32_t>& member_list,
+                      std::vector<std::pair<uint32_t, uint32_t>>& span) {
+    const int W = 2 * L;
+    const int64_t np = (int64_t)P.size();
+    const std::vector<int16_t> units = all_units(L);
+    std::vector<int8_t> pairs((size_t)np * W);
+    for (int64_t i = 0; i < np; ++i) std::memcpy(&pairs[(size_t)i * W], P[i].data(), W);
+    cudaStream_t s = c->s_comp;
+    DevBuf dp, du, dc, df;
+    if (!dp.ensure(pairs.size()) || !du.ensure(units.size() * 2) || !dc.ensure(pairs.size()) ||
+        !df.ensure((size_t)np * 4))
+        return c->fail(GP_ERR_NOMEM, "equivalence filter: device allocation");
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dp.p, pairs.data(), pairs.size(), cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(du.p, units.data(), units.size() * 2, cudaMemcpyHostToDevice, s));
+    CanonArgs ca{};
+    ca.pairs = dp.as<int8_t>();
+    ca.np = np;
+    ca.L = L;
+    ca.units = du.as<int16_t>();
+    ca.nu = (int)units.size();
+    ca.alt = !(compress > 1 || L % 2 == 1) ? 1 : 0;  // filter.cpp:83-87
+    ca.canon = dc.as<int8_t>();
+    ca.fixers = df.as<uint32_t>();
+    const int64_t grid = std::min<int64_t>(np, (int64_t)c->num_sms * 16);
+    canon_kernel<<<(unsigned)grid, kCanonThreads, 0, s>>>(ca);
+    GP_CUDA_TRY(c, cudaGetLastError());
+    std::vector<int8_t> canon(pairs.size());
+    std::vector<uint32_t> fixers(np);
+    GP_CUDA_TRY(c, cudaMemcpyAsync(canon.data(), dc.p, canon.size(), cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(fixers.data(), df.p, (size_t)np * 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+    const uint64_t G = pair_group_size(L, compress);
+    for (int64_t i = 0; i < np; ++i) {
+        if (fixers[i] == 0 || G % fixers[i] != 0)
+            return c->fail(GP_ERR_CUDA, "equivalence filter: %u of %llu elements fix pair %lld", fixers[i],
+                           (unsigned long long)G, (long long)i);
+        csize[i] = G / fixers[i];
+    }
+    // the classes: runs of equal least images
+    std::vector<uint32_t> ord(np);
+    for (int64_t i = 0; i < np; ++i) ord[i] = (uint32_t)i;
+    auto row = [&](uint32_t i) { return canon.data() + (size_t)i * W; };
+    std::sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) {
+        const int d = std::memcmp(row(x), row(y), (size_t)W);
+        return d != 0 ? d < 0 : x < y;
+    });
+    for (int64_t r0 = 0; r0 < np;) {
+        int64_t r1 = r0 + 1;
+        while (r1 < np && std::memcmp(row(ord[r0]), row(ord[r1]), (size_t)W) == 0) ++r1;
+        for (int64_t k = r0; k < r1; ++k) span[ord[k]] = {(uint32_t)r0, (uint32_t)r1};
+        r0 = r1;
+    }
+    member_list.swap(ord);
+    return GP_OK;
+}
+
 // Size of the generator group: 4 phi(L) L^2, times 8 sign patterns with the
 // alternating negation (exact for L >= 3, an upper bound at L = 2).
 uint64_t pair_group_size(int L, int compress) {
@@ -350,6 +585,40 @@ extern const uint64_t kMaxGroupBytes = uint64_t(1) << 32;
 }  // namespace
 
 extern "C" {
+
+// 1 when the affine parametrisation the canonical-form kernel enumerates
+// (swap, e, signs, u, s_a, s_b) gives exactly the closure's group of length
+// L at this compression, 0 when not, -1 when not applicable (L < 3 or too
+// large).  Host only; a test hook.
+int gp_debug_pair_group_check(int L, int compress) {
+    if (L < 3 || 2 * L > kMaxW || compress < 1) return -1;
+    if (pair_group_size(L, compress) * (uint64_t)(4 * L) > kMaxGroupBytes) return -1;
+    const int W = 2 * L;
+    const bool alt = !(compress > 1 || L % 2 == 1);
+    const std::vector<int16_t> units = all_units(L);
+    std::vector<std::vector<int16_t>> mine, closure;
+    for (int swap = 0; swap < 2; ++swap)
+        for (int e = 0; e < 2; ++e)
+            for (int pat = 0; pat < (alt ? 8 : 1); ++pat)
+                for (int16_t u : units)
+                    for (int sa = 0; sa < L; ++sa)
+                        for (int sb = 0; sb < L; ++sb) {
+                            const int ha = swap ? L : 0, hb = swap ? 0 : L, ma = u, mb = e ? L - u : u;
+                            const int alpha = pat & 1, ba = (pat >> 1) & 1, bb = (pat >> 2) & 1;
+                            std::vector<int16_t> item(W);
+                            for (int i = 0; i < L; ++i) {
+                                const int sga = ((alpha & i) ^ ba) & 1 ? -1 : 1, sgb = ((alpha & i) ^ bb) & 1 ? -1 : 1;
+                                item[i] = (int16_t)(sga * (ha + (int)(((long long)ma * i + sa) % L) + 1));
+                                item[L + i] = (int16_t)(sgb * (hb + (int)(((long long)mb * i + sb) % L) + 1));
+                            }
+                            mine.push_back(std::move(item));
+                        }
+    const std::vector<int16_t> g = pair_generators(L, compress);
+    for (size_t i = 0; i + W <= g.size(); i += W) closure.emplace_back(g.begin() + i, g.begin() + i + W);
+    std::sort(mine.begin(), mine.end());
+    std::sort(closure.begin(), closure.end());
+    return mine == closure ? 1 : 0;
+}
 
 int64_t gp_debug_pair_generator_count(int L, int compress) {
     if (L < 1 || 2 * L > kMaxW || compress < 1) return -1;
@@ -386,13 +655,15 @@ static int gp_equiv_filter_impl(gp_ctx* c, int order, int compress, const char* 
     // thread while the pairs are read and sorted
     std::vector<int16_t> gens;
     bool group_failed = false;
-    std::thread group_thread([&] {
-        try {
-            gens = pair_generators(L, compress);
-        } catch (const std::exception&) {
-            group_failed = true;
-        }
-    });
+    std::thread group_thread;
+    if (L < 3)  // the table of every element (longer lengths use canonical forms)
+        group_thread = std::thread([&] {
+            try {
+                gens = pair_generators(L, compress);
+            } catch (const std::exception&) {
+                group_failed = true;
+            }
+        });
     struct Joiner {
         std::thread& t;
         ~Joiner() {
@@ -431,124 +702,144 @@ static int gp_equiv_filter_impl(gp_ctx* c, int order, int compress, const char* 
     const int64_t np = (int64_t)P.size();
     std::vector<char> alive(np, 1);
     if (np > 0) {
-        lap("sort");
-        group_thread.join();
-        if (group_failed) {
-            if (out) fclose(out);
-            return c->fail(GP_ERR_NOMEM, "equivalence filter: generator group of length %d", L);
-        }
-        lap("group");
-        const int64_t ng = (int64_t)(gens.size() / (size_t)W);
-        std::vector<int16_t> items((size_t)ng * W);  // transposed: items[o * ng + g]
-        {
-            const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-            std::vector<std::thread> th;
-            for (unsigned t = 0; t < nt; ++t)
-                th.emplace_back([&, t] {
-                    // blocks of 64 generators: each thread writes whole cache lines of every row
-                    for (int64_t g0 = (int64_t)t * 64; g0 < ng; g0 += (int64_t)nt * 64)
-                        for (int64_t g = g0; g < std::min<int64_t>(g0 + 64, ng); ++g) {
-                            const auto s = as_sources(gens.data() + (size_t)g * W, L);
-                            for (int o = 0; o < W; ++o) items[(size_t)o * ng + g] = s[o];
-                        }
-                });
-            for (auto& x : th) x.join();
-        }
-        lap("table");
-        std::vector<int8_t> pairs((size_t)np * W);
-        for (int64_t i = 0; i < np; ++i)
-            for (int j = 0; j < W; ++j) pairs[i * W + j] = P[i][j];
-        // hash set of the pairs (the image lookup), same hash as the kernel's
-        uint32_t set_size = 1;
-        while (set_size < 2 * (uint64_t)np) set_size <<= 1;
-        std::vector<uint32_t> set_h(set_size, 0), set_i(set_size, 0xFFFFFFFFu);
-        for (int64_t i = 0; i < np; ++i) {
-            uint32_t h = kFnvBasis;
-            for (int j = 0; j < W; ++j) h = fnv_step(h, P[i][j]);
-            h = fnv_fold(h);
-            uint32_t slot = h & (set_size - 1);
-            while (set_i[slot] != 0xFFFFFFFFu) slot = (slot + 1) & (set_size - 1);
-            set_h[slot] = h;
-            set_i[slot] = (uint32_t)i;
-        }
-        const int64_t mcap = std::max<int64_t>(np * 64, 1 << 20);
-        cudaStream_t s = c->s_comp;
-        DevBuf di, dp, dsh, dsi, dst, dm, dmisc;
-        if (!di.ensure(items.size() * 2) || !dp.ensure(pairs.size()) || !dsh.ensure((size_t)set_size * 4) ||
-            !dsi.ensure((size_t)set_size * 4) || !dst.ensure(np * 4) || !dm.ensure((size_t)mcap * 8) ||
-            !dmisc.ensure(64))
-            return c->fail(GP_ERR_NOMEM, "equivalence filter: device allocation");
-        GP_CUDA_TRY(c, cudaMemcpyAsync(di.p, items.data(), items.size() * 2, cudaMemcpyHostToDevice, s));
-        GP_CUDA_TRY(c, cudaMemcpyAsync(dp.p, pairs.data(), pairs.size(), cudaMemcpyHostToDevice, s));
-        GP_CUDA_TRY(c, cudaMemcpyAsync(dsh.p, set_h.data(), (size_t)set_size * 4, cudaMemcpyHostToDevice, s));
-        GP_CUDA_TRY(c, cudaMemcpyAsync(dsi.p, set_i.data(), (size_t)set_size * 4, cudaMemcpyHostToDevice, s));
-        GP_CUDA_TRY(c, cudaMemsetAsync(dst.p, 0, np * 4, s));
-        GP_CUDA_TRY(c, cudaMemsetAsync(dmisc.p, 0, 64, s));
-        ClassArgs ca{};
-        ca.srcT = di.as<int16_t>();
-        ca.ng = ng;
-        ca.pairs = dp.as<int8_t>();
-        ca.np = np;
-        ca.W = W;
-        ca.set_h = dsh.as<uint32_t>();
-        ca.set_i = dsi.as<uint32_t>();
-        ca.set_mask = set_size - 1;
-        ca.stab = dst.as<uint32_t>();
-        ca.members = dm.as<uint32_t>();
-        ca.nmembers = dmisc.as<unsigned long long>();
-        ca.mcap = mcap;
-        ca.status = c->status.as<int>();
-        const int64_t groups = (np + kPairsPerCta - 1) / kPairsPerCta;
-        // generator shares per group: enough CTAs for eight per SM, each share
-        // at least one generator per thread
-        const int64_t want = std::max<int64_t>(1, (8 * (int64_t)c->num_sms + groups - 1) / groups);
-        const int splits = (int)std::max<int64_t>(1, std::min<int64_t>(want, (ng + 255) / 256));
-        for (int64_t g0 = 0; g0 < groups; g0 += (int64_t(1) << 20)) {  // grids of at most 2^20 groups
-            const int64_t gn = std::min<int64_t>(groups - g0, int64_t(1) << 20);
-            ClassArgs cb = ca;
-            cb.group0 = g0;
-            class_kernel<<<(unsigned)(gn * splits), 256, 0, s>>>(cb, splits);
-        }
-        GP_CUDA_TRY(c, cudaGetLastError());
-        GP_CUDA_TRY(c, cudaStreamSynchronize(s));
-        lap("classes");
-        int rc = c->check_status("equivalence filter");
-        if (rc) {
-            if (out) fclose(out);
-            return rc;
-        }
-        std::vector<uint32_t> stab(np);
-        unsigned long long nmem = 0;
-        GP_CUDA_TRY(c, cudaMemcpy(stab.data(), dst.p, np * 4, cudaMemcpyDeviceToHost));
-        GP_CUDA_TRY(c, cudaMemcpy(&nmem, dmisc.p, 8, cudaMemcpyDeviceToHost));
-        // orbit-stabiliser: class size = group order / generators fixing the pair
         std::vector<unsigned long long> csize(np);
-        for (int64_t i = 0; i < np; ++i) {
-            if (stab[i] == 0 || ng % stab[i] != 0) {
+        // the input pairs of each pair's class: member_list[span[i].first .. span[i].second)
+        std::vector<uint32_t> member_list;
+        std::vector<std::pair<uint32_t, uint32_t>> span(np);
+        if (L >= 3) {
+            lap("sort");
+            int rc = canonical_classes(c, L, compress, P, csize, member_list, span);
+            if (rc) {
                 if (out) fclose(out);
-                return c->fail(GP_ERR_CUDA, "equivalence filter: stabiliser of pair %lld is %u of %lld generators",
-                               (long long)i, stab[i], (long long)ng);
+                return rc;
             }
-            csize[i] = (unsigned long long)(ng / stab[i]);
+            lap("classes");
+        } else {
+            lap("sort");
+            group_thread.join();
+            if (group_failed) {
+                if (out) fclose(out);
+                return c->fail(GP_ERR_NOMEM, "equivalence filter: generator group of length %d", L);
+            }
+            lap("group");
+            const int64_t ng = (int64_t)(gens.size() / (size_t)W);
+            std::vector<int16_t> items((size_t)ng * W);  // transposed: items[o * ng + g]
+            {
+                const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+                std::vector<std::thread> th;
+                for (unsigned t = 0; t < nt; ++t)
+                    th.emplace_back([&, t] {
+                        // blocks of 64 generators: each thread writes whole cache lines of every row
+                        for (int64_t g0 = (int64_t)t * 64; g0 < ng; g0 += (int64_t)nt * 64)
+                            for (int64_t g = g0; g < std::min<int64_t>(g0 + 64, ng); ++g) {
+                                const auto s = as_sources(gens.data() + (size_t)g * W, L);
+                                for (int o = 0; o < W; ++o) items[(size_t)o * ng + g] = s[o];
+                            }
+                    });
+                for (auto& x : th) x.join();
+            }
+            lap("table");
+            std::vector<int8_t> pairs((size_t)np * W);
+            for (int64_t i = 0; i < np; ++i)
+                for (int j = 0; j < W; ++j) pairs[i * W + j] = P[i][j];
+            // hash set of the pairs (the image lookup), same hash as the kernel's
+            uint32_t set_size = 1;
+            while (set_size < 2 * (uint64_t)np) set_size <<= 1;
+            std::vector<uint32_t> set_h(set_size, 0), set_i(set_size, 0xFFFFFFFFu);
+            for (int64_t i = 0; i < np; ++i) {
+                uint32_t h = kFnvBasis;
+                for (int j = 0; j < W; ++j) h = fnv_step(h, P[i][j]);
+                h = fnv_fold(h);
+                uint32_t slot = h & (set_size - 1);
+                while (set_i[slot] != 0xFFFFFFFFu) slot = (slot + 1) & (set_size - 1);
+                set_h[slot] = h;
+                set_i[slot] = (uint32_t)i;
+            }
+            const int64_t mcap = std::max<int64_t>(np * 64, 1 << 20);
+            cudaStream_t s = c->s_comp;
+            DevBuf di, dp, dsh, dsi, dst, dm, dmisc;
+            if (!di.ensure(items.size() * 2) || !dp.ensure(pairs.size()) || !dsh.ensure((size_t)set_size * 4) ||
+                !dsi.ensure((size_t)set_size * 4) || !dst.ensure(np * 4) || !dm.ensure((size_t)mcap * 8) ||
+                !dmisc.ensure(64))
+                return c->fail(GP_ERR_NOMEM, "equivalence filter: device allocation");
+            GP_CUDA_TRY(c, cudaMemcpyAsync(di.p, items.data(), items.size() * 2, cudaMemcpyHostToDevice, s));
+            GP_CUDA_TRY(c, cudaMemcpyAsync(dp.p, pairs.data(), pairs.size(), cudaMemcpyHostToDevice, s));
+            GP_CUDA_TRY(c, cudaMemcpyAsync(dsh.p, set_h.data(), (size_t)set_size * 4, cudaMemcpyHostToDevice, s));
+            GP_CUDA_TRY(c, cudaMemcpyAsync(dsi.p, set_i.data(), (size_t)set_size * 4, cudaMemcpyHostToDevice, s));
+            GP_CUDA_TRY(c, cudaMemsetAsync(dst.p, 0, np * 4, s));
+            GP_CUDA_TRY(c, cudaMemsetAsync(dmisc.p, 0, 64, s));
+            ClassArgs ca{};
+            ca.srcT = di.as<int16_t>();
+            ca.ng = ng;
+            ca.pairs = dp.as<int8_t>();
+            ca.np = np;
+            ca.W = W;
+            ca.set_h = dsh.as<uint32_t>();
+            ca.set_i = dsi.as<uint32_t>();
+            ca.set_mask = set_size - 1;
+            ca.stab = dst.as<uint32_t>();
+            ca.members = dm.as<uint32_t>();
+            ca.nmembers = dmisc.as<unsigned long long>();
+            ca.mcap = mcap;
+            ca.status = c->status.as<int>();
+            const int64_t groups = (np + kPairsPerCta - 1) / kPairsPerCta;
+            // generator shares per group: enough CTAs for eight per SM, each share
+            // at least one generator per thread
+            const int64_t want = std::max<int64_t>(1, (8 * (int64_t)c->num_sms + groups - 1) / groups);
+            const int splits = (int)std::max<int64_t>(1, std::min<int64_t>(want, (ng + 255) / 256));
+            for (int64_t g0 = 0; g0 < groups; g0 += (int64_t(1) << 20)) {  // grids of at most 2^20 groups
+                const int64_t gn = std::min<int64_t>(groups - g0, int64_t(1) << 20);
+                ClassArgs cb = ca;
+                cb.group0 = g0;
+                class_kernel<<<(unsigned)(gn * splits), 256, 0, s>>>(cb, splits);
+            }
+            GP_CUDA_TRY(c, cudaGetLastError());
+            GP_CUDA_TRY(c, cudaStreamSynchronize(s));
+            lap("classes");
+            int rc = c->check_status("equivalence filter");
+            if (rc) {
+                if (out) fclose(out);
+                return rc;
+            }
+            std::vector<uint32_t> stab(np);
+            unsigned long long nmem = 0;
+            GP_CUDA_TRY(c, cudaMemcpy(stab.data(), dst.p, np * 4, cudaMemcpyDeviceToHost));
+            GP_CUDA_TRY(c, cudaMemcpy(&nmem, dmisc.p, 8, cudaMemcpyDeviceToHost));
+            // orbit-stabiliser: class size = group order / generators fixing the pair
+            for (int64_t i = 0; i < np; ++i) {
+                if (stab[i] == 0 || ng % stab[i] != 0) {
+                    if (out) fclose(out);
+                    return c->fail(GP_ERR_CUDA, "equivalence filter: stabiliser of pair %lld is %u of %lld generators",
+                                   (long long)i, stab[i], (long long)ng);
+                }
+                csize[i] = (unsigned long long)(ng / stab[i]);
+            }
+            std::vector<uint32_t> mem((size_t)nmem * 2);
+            if (nmem) GP_CUDA_TRY(c, cudaMemcpy(mem.data(), dm.p, mem.size() * 4, cudaMemcpyDeviceToHost));
+            std::vector<std::vector<uint32_t>> members(np);
+            for (unsigned long long i = 0; i < nmem; ++i) members[mem[2 * i]].push_back(mem[2 * i + 1]);
+            for (int64_t i = 0; i < np; ++i) {
+                span[i].first = (uint32_t)member_list.size();
+                member_list.insert(member_list.end(), members[i].begin(), members[i].end());
+                span[i].second = (uint32_t)member_list.size();
+            }
         }
-        std::vector<uint32_t> mem((size_t)nmem * 2);
-        if (nmem) GP_CUDA_TRY(c, cudaMemcpy(mem.data(), dm.p, mem.size() * 4, cudaMemcpyDeviceToHost));
-        std::vector<std::vector<uint32_t>> members(np);
-        for (unsigned long long i = 0; i < nmem; ++i) members[mem[2 * i]].push_back(mem[2 * i + 1]);
         // filter.cpp:117-144, in set order
         int64_t n_alive = np;
         for (int64_t it = 0; it < np; ++it) {
             if (!alive[it]) continue;
+            const uint32_t* mb = member_list.data() + span[it].first;
+            const uint32_t* me = member_list.data() + span[it].second;
             if ((int64_t)csize[it] > n_alive) {
-                for (uint32_t m : members[it])
-                    if ((int64_t)m > it && alive[m]) {
-                        alive[m] = 0;
+                for (const uint32_t* m = mb; m < me; ++m)
+                    if ((int64_t)*m > it && alive[*m]) {
+                        alive[*m] = 0;
                         --n_alive;
                     }
             } else {
-                for (uint32_t m : members[it])
-                    if (alive[m]) {
-                        alive[m] = 0;
+                for (const uint32_t* m = mb; m < me; ++m)
+                    if (alive[*m]) {
+                        alive[*m] = 0;
                         --n_alive;
                     }
                 if (!alive[it]) {

@@ -356,6 +356,12 @@ int gp_equiv_filter(gp_ctx* ctx, int order, int compress, const char* in_path, c
  * -1 for an unsupported length.  Host only. */
 int64_t gp_debug_pair_generator_count(int L, int compress);
 
+/* Diagnostics: 1 when the affine description of that group gp_equiv_filter
+ * uses for L >= 3 (swap, multiplier +-u, shifts of each half, the
+ * alternating signs) gives exactly the closure's elements, 0 when not, -1
+ * when not applicable (L < 3 or an unsupported length).  Host only. */
+int gp_debug_pair_group_check(int L, int compress);
+
 #ifdef __cplusplus
 }
 #endif

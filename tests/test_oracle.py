@@ -124,6 +124,19 @@ def test_pair_generator_set_matches_oracle_closure(oracle_lib, compress):
     assert lib.gp_debug_pair_generator_count(128, 1) == -1
 
 
+@pytest.mark.parametrize("compress", [1, 2, 3])
+def test_pair_group_affine_description_equals_closure(compress):
+    """For L >= 3 gp_equiv_filter finds classes by least images over an
+    affine description of the pair group (swap, multiplier +-u, a shift per
+    half, the alternating signs at compression 1 and even L); that
+    description must give exactly the closure's elements."""
+    import golaypair_gb300 as gp
+    lib = gp.lib()
+    for L in list(range(3, 27)) + [32, 39]:
+        assert lib.gp_debug_pair_group_check(L, compress) == 1, (L, compress)
+    assert lib.gp_debug_pair_group_check(2, compress) == -1
+
+
 # Known answers recorded in the reference's notes (NOTES.md:455,459 and :436)
 NOTES_ORDER26_A = [-1, -1, -1, -1, 1, 1, -1, -1, 1, 1, 1, -1, 1, -1, 1, -1, 1, 1, -1, 1, 1, -1, 1, 1, 1, 1]
 NOTES_ORDER26_A_C2 = [-2, 0, -2, 0, 2, 0, 0, 0, 0, 2, 2, 0, 2]
