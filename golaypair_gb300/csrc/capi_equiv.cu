@@ -7,16 +7,18 @@
 // and (compression 1, even L only) negate the odd positions of both.  It is
 // built on the host, as the reference builds it once per run.
 //
-// class_kernel applies every generator to the pairs with the reference's
-// application rule (equivalence.cpp:97-144).  One pass over the (transposed)
-// generator table hashes the images of several pairs at once, so the table
-// is read once per group of pairs, not once per pair.  Per pair it counts
-// the generators that fix the pair (its stabiliser: the class size is the
-// group order over that count, orbit-stabiliser, the generator set being a
-// group) and looks every image up in a hash set of the input pairs
-// (verified entry by entry on a hash match).  The host then replays the
-// reference's in-order erase loop (filter.cpp:117-144) on those class sizes
-// and member lists.
+// Per pair the filter needs its class size and the input pairs in its
+// class.  For L >= 3, canon_kernel finds both from canonical forms: every
+// group element is an affine map per half (the description below, checked
+// against the closure by gp_debug_pair_group_check), so a pair's least image
+// over the group takes O(4 phi(L) L^2) work; pairs with equal least images
+// are in one class, and the class size is the group order over the number
+// of elements that fix the pair (orbit-stabiliser).  For L < 3 class_kernel
+// applies every element of the closure with the reference's application
+// rule (equivalence.cpp:97-144), hashing the images of several pairs per
+// pass over the transposed table and looking them up in a hash set of the
+// input pairs.  Either way the host then replays the reference's in-order
+// erase loop (filter.cpp:117-144) on those class sizes and member lists.
 #include <algorithm>
 #include <chrono>
 #include <stdexcept>
