@@ -636,7 +636,7 @@ static int gp_equiv_filter_impl(gp_ctx* c, int order, int compress, const char* 
     const int L = order / compress;
     const int W = 2 * L;
     if (W > kMaxW) return c->fail(GP_ERR_UNSUPPORTED, "equivalence filter: length %d", L);
-    if (pair_group_size(L, compress) * (uint64_t)(2 * W) > kMaxGroupBytes)
+    if (L < 3 && pair_group_size(L, compress) * (uint64_t)(2 * W) > kMaxGroupBytes)  // the table path only
         return c->fail(GP_ERR_UNSUPPORTED, "equivalence filter: %llu generators at length %d exceed %llu bytes",
                        (unsigned long long)pair_group_size(L, compress), L, (unsigned long long)kMaxGroupBytes);
     // GP_EQUIV_TIMING=1 in the environment prints the phase times to stderr (diagnostics)

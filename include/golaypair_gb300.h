@@ -346,8 +346,10 @@ int gp_uncompress_chain(gp_ctx* ctx, int order, const int* compress, int ncomp, 
  * keeps the first pair of every equivalence class (in the reference's set
  * order and erase rules) and writes them in sorted order.  The generator
  * group has 4 phi(L) L^2 elements (8 times more at compression 1 with even
- * L); GP_ERR_UNSUPPORTED when its table would exceed 4 GB (e.g. L = 128 at
- * compression 1), where the reference would run out of memory.
+ * L); classes are found from each pair's least image over the group, so no
+ * table of the group is built for L >= 3 and every length up to 128 runs
+ * (at L = 128, compression 1, the reference's table of 33.5 million
+ * elements would run it out of memory).
  */
 int gp_equiv_filter(gp_ctx* ctx, int order, int compress, const char* in_path, const char* out_path);
 

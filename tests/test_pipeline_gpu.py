@@ -268,6 +268,48 @@ def test_filter_n57_matches_oracle(oracle_lib, tmp_path):
     _filter_gpu_vs_oracle(oracle_lib, tmp_path, 57, pairs)
 
 
+@pytest.mark.parametrize("L", [64, 127, 128])
+def test_filter_long_pairs_by_least_images(tmp_path, L):
+    """Lengths whose group table the reference (and the table kernel) could
+    not hold (L = 128, compression 1: 33.5 million elements of 256 entries):
+    three random pairs and two images of each under known group elements
+    (a shift of b with a swap, a decimation with a reversal of b, the
+    alternating negation at even L) form three classes; with classes this
+    small against their class sizes the reference's erase loop keeps the
+    first member of each class in set order."""
+    rng = np.random.default_rng(L)
+    units = [u for u in range(2, L) if np.gcd(u, L) == 1]
+
+    def images(a, b):
+        i = np.arange(L)
+        out = [(np.roll(b, -5), a)]                           # shift b by 5, then swap
+        u = units[len(units) // 2]
+        a2, b2 = a[(u * i) % L], b[(u * i) % L]               # decimate both by u
+        out.append((a2, b2[::-1].copy()))                     # reverse b
+        if L % 2 == 0:
+            sg = np.where(i % 2 == 1, -1, 1)
+            out.append((a * sg, b * sg))                      # alternating negation
+        return out
+
+    pairs = []
+    classes = []
+    for _ in range(3):
+        a = rng.choice([-1, 1], L).astype(np.int8)
+        b = rng.choice([-1, 1], L).astype(np.int8)
+        cls = [(a, b)] + images(a, b)
+        keys = [tuple(int(v) for v in np.concatenate([x, y])) for x, y in cls]
+        classes.append(sorted(set(keys)))
+        pairs += keys
+    src = tmp_path / "pairs"
+    src.write_text("".join(" ".join(map(str, p[:L])) + "  " + " ".join(map(str, p[L:])) + "\n" for p in pairs))
+    out = tmp_path / "unique"
+    with gp.Context(0) as ctx:
+        ctx.check(ctx._lib.gp_equiv_filter(ctx.handle, L, 1, str(src).encode(), str(out).encode()), "gp_equiv_filter")
+    want = sorted(c[0] for c in classes)
+    got = [tuple(int(v) for v in line.split()) for line in read(out).decode().splitlines()]
+    assert got == want
+
+
 def _lines(path):
     return read(path).count(b"\n")
 
