@@ -295,7 +295,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     StageRange nvtx_range("generate");
     static const bool timing = getenv("GP_GEN_TIMING") != nullptr;
     const auto tb = std::chrono::steady_clock::now();
-    double t_win = 0, t_setup = 0, t_capture = 0, t_iter = 0, t_drain = 0;
+    double t_win = 0, t_setup = 0, t_capture = 0, t_iter = 0;
     const int nj = (int)jobs.size();
     if (nj < 1 || nj > gp::kMaxEnumJobs) return c->fail(GP_ERR_ARG, "batch of %d jobs (1..%d)", nj, gp::kMaxEnumJobs);
     cudaStream_t s = c->s_comp;
@@ -672,7 +672,6 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     if (timing)
         fprintf(stderr, "[gen] windows %.4f s, setup %.4f s, capture %.4f s, %d iterations + drains %.4f s\n", t_win,
                 t_setup, t_capture, iters, t_iter);
-    (void)t_drain;
     return GP_OK;
 }
 

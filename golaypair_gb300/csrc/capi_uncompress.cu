@@ -1410,7 +1410,7 @@ int run_level(gp_ctx* c, const Level& lv, const std::vector<uint8_t>& seqs, FILE
     LevelDev ld{};
     rc = upload_level(c, lv, ld, s);
     if (rc) return rc;
-    Batcher bt{c, lv, ld, sides, s, scan_kernel_for(lv.np)};
+    Batcher bt{c, lv, ld, sides, s, scan_kernel_for(lv.np), 0, 0, {}};
     {
         // shared memory of the scan: the largest suffix table and term table
         // any side of this call needs (a few tens of KB: several CTAs per SM)

@@ -50,11 +50,6 @@ __global__ void scan_add_kernel(uint32_t* out, const uint32_t* block_off, int64_
     if (i < n) out[i] += block_off[blockIdx.x];
 }
 
-__global__ void flags_nonzero_kernel(const uint32_t* in, uint32_t* flags, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        flags[i] = in[i] ? 1u : 0u;
-}
-
 __global__ void compact_kernel(const uint32_t* flags, const uint32_t* pos, const uint32_t* src, uint32_t* dst,
                                int64_t n, uint32_t* count) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
