@@ -200,7 +200,8 @@ constexpr int kIterSlots = 4;   // per job: [0] candidates, [1] unsure, [2] surv
 constexpr int kCumSlots = 4;    // per job: [0] necklaces, [1] records, [2] psd passes
 constexpr int kIncomplete = kIterSlots * gp::kMaxEnumJobs;          // u64 slot of the flag
 constexpr int kNextWin = kIncomplete + 1;                          // window handout counter
-constexpr int kIterWords = kIncomplete + 2;
+constexpr int kNextWinWide = kIncomplete + 2;                      // the same for the wide jobs' launch
+constexpr int kIterWords = kIncomplete + 3;
 constexpr int kCumBase = 40;                                        // u64 offset of the cumulative block
 constexpr int kCounterWords = kCumBase + kCumSlots * gp::kMaxEnumJobs;
 
@@ -316,9 +317,14 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
         int64_t out;             // index of its first window in cur / end / wjob
     };
     std::vector<Chunk> chunks;
-    int64_t nwin = 0;
+    int64_t nwin = 0, nwin_narrow = 0;
     constexpr int64_t kChunkWindows = 8192;
+    // the windows of jobs whose words fit 63 bits first: they go to the
+    // enumerator's 64-bit instantiation, the others to a second launch
+    auto narrow_job = [&](int ji) { return jobs[ji].p.b * jobs[ji].p.L <= 63; };
+    for (int pass = 0; pass < 2; ++pass)
     for (int ji = 0; ji < nj; ++ji) {
+        if (narrow_job(ji) != (pass == 0)) continue;
         JobRun& j = jobs[ji];
         const gp::u128 words = range_words(j);
         if (words == 0) continue;
@@ -334,6 +340,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
                 nwin += std::min(kChunkWindows, n - w0);
             }
         }
+        if (pass == 0) nwin_narrow = nwin;
     }
     std::vector<uint4> cur(nwin), end(nwin);
     std::vector<uint8_t> wjob(nwin);
@@ -473,6 +480,17 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     ea.incomplete = reinterpret_cast<int*>(ctr + kIncomplete);
     ea.next_win = ctr + kNextWin;
     ea.status = c->status.as<int>();
+    // two launches per iteration when the batch mixes job widths: windows
+    // [0, nwin_narrow) on the 64-bit enumerator, the rest on the 128-bit one
+    gp::EnumArgs ea_wide = ea;
+    ea.nwin = nwin_narrow;
+    ea.narrow = 1;
+    ea_wide.cur += nwin_narrow;
+    ea_wide.end += nwin_narrow;
+    ea_wide.win_job += nwin_narrow;
+    ea_wide.nwin = nwin - nwin_narrow;
+    ea_wide.next_win = ctr + kNextWinWide;
+    ea_wide.narrow = 0;
 
     // ---- one iteration of the pipeline on stream s
     const bool multi = cfg.multi_launch && multi_launch_ok(jobs);
@@ -545,7 +563,21 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     };
     auto enqueue_iteration = [&]() -> int {
         GP_CUDA_TRY(c, cudaMemsetAsync(ctr, 0, kIterWords * 8, s));
-        GP_CUDA_TRY(c, gp::launch_enumerate(ea, c->num_sms, s, cfg.enum_variant));
+        if (ea.nwin > 0 && ea_wide.nwin > 0) {
+            // both launches side by side (a branch of the graph): the wide
+            // jobs' blocks take the SMs the narrow launch's finished blocks free
+            cudaStream_t sw = c->s_jobs[gp_ctx::kJobStreams - 1];
+            cudaEvent_t done = c->ev_join[gp_ctx::kJobStreams - 1];
+            GP_CUDA_TRY(c, cudaEventRecord(c->ev_fork, s));
+            GP_CUDA_TRY(c, cudaStreamWaitEvent(sw, c->ev_fork, 0));
+            GP_CUDA_TRY(c, gp::launch_enumerate(ea, c->num_sms, s, cfg.enum_variant));
+            GP_CUDA_TRY(c, gp::launch_enumerate(ea_wide, c->num_sms, sw, cfg.enum_variant));
+            GP_CUDA_TRY(c, cudaEventRecord(done, sw));
+            GP_CUDA_TRY(c, cudaStreamWaitEvent(s, done, 0));
+        } else {  // one of the two has no windows (a no-op)
+            GP_CUDA_TRY(c, gp::launch_enumerate(ea, c->num_sms, s, cfg.enum_variant));
+            GP_CUDA_TRY(c, gp::launch_enumerate(ea_wide, c->num_sms, s, cfg.enum_variant));
+        }
         if (multi) {
             const int rc = enqueue_multi();
             if (rc) return rc;

@@ -191,7 +191,9 @@ __device__ __forceinline__ bool job_full(const EnumJob& j) {
 constexpr int kFlushAt = 128;
 constexpr int kQueue = kFlushAt + 32;  // per warp: < kFlushAt queued + 32 from one step
 
-template <int MINB>
+// NARROW: every job's words fit 63 bits, so a word and its window end are
+// 64-bit values (the high halves are zero and drop out of the registers).
+template <int MINB, bool NARROW>
 __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
     __shared__ uint8_t role_tab[kMaxEnumJobs][kMaxDigitSum + 1];
     __shared__ EnumJob jobs[kMaxEnumJobs];
@@ -269,6 +271,10 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
             } else {
                 w = from_u4(a.cur[win]);
                 end = from_u4(a.end[win]);
+                if constexpr (NARROW) {
+                    w.hi = 0;
+                    end.hi = 0;
+                }
                 jv = job_view(jobs[job]);
                 if (lt(w, end)) {
                     p = first_prenecklace(w, jv.b, jv.L);
@@ -288,17 +294,17 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
         if (active) {
             if (divides_L(jv, p)) {
                 ++necklaces;
-                role = role_tab[job][jv.narrow ? digit_sum64(w.lo, jv) : digit_sum(w, jv)];
+                role = role_tab[job][(NARROW || jv.narrow) ? digit_sum64(w.lo, jv) : digit_sum(w, jv)];
             }
             int np;
-            if (jv.narrow) {
+            if (NARROW || jv.narrow) {
                 uint64_t wl = w.lo;
                 np = fkm_next64(wl, jv);
                 w.lo = wl;
             } else {
                 np = fkm_next(w, jv);
             }
-            if (np == 0 || !lt(w, end)) {
+            if (np == 0 || !(NARROW ? w.lo < end.lo : lt(w, end))) {
                 have = false;
                 a.cur[win] = a.end[win];
                 win = take();
@@ -339,31 +345,37 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
     if (necklaces) atomicAdd(jobs[job].necklaces, necklaces);
 }
 
-}  // namespace
-
-cudaError_t launch_enumerate(const EnumArgs& a, int num_sms, cudaStream_t st, int variant) {
-    if (a.nwin <= 0) return cudaSuccess;
-    if (a.njobs < 1 || a.njobs > kMaxEnumJobs) return cudaErrorInvalidValue;
+template <bool NARROW>
+cudaError_t launch_enumerate_t(const EnumArgs& a, int num_sms, cudaStream_t st, int variant) {
     // one wave of resident blocks: windows are handed out dynamically
     static int resident[3] = {0, 0, 0};
     const int vi = variant == 1 ? 1 : variant == 2 ? 2 : 0;
     int& per_sm = resident[vi];
     if (per_sm == 0) {
-        cudaError_t e = vi == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<8>, 256, 0)
-                        : vi == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<3>, 256, 0)
-                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<4>, 256, 0);
+        cudaError_t e = vi == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<8, NARROW>, 256, 0)
+                        : vi == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<3, NARROW>, 256, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel<4, NARROW>, 256, 0);
         if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     }
     int64_t blocks = (a.nwin + 255) / 256;
     const int64_t maxb = (int64_t)num_sms * per_sm;
     if (blocks > maxb) blocks = maxb;
     if (vi == 1)
-        enumerate_kernel<8><<<(unsigned)blocks, 256, 0, st>>>(a);
+        enumerate_kernel<8, NARROW><<<(unsigned)blocks, 256, 0, st>>>(a);
     else if (vi == 2)
-        enumerate_kernel<3><<<(unsigned)blocks, 256, 0, st>>>(a);
+        enumerate_kernel<3, NARROW><<<(unsigned)blocks, 256, 0, st>>>(a);
     else
-        enumerate_kernel<4><<<(unsigned)blocks, 256, 0, st>>>(a);
+        enumerate_kernel<4, NARROW><<<(unsigned)blocks, 256, 0, st>>>(a);
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_enumerate(const EnumArgs& a, int num_sms, cudaStream_t st, int variant) {
+    if (a.nwin <= 0) return cudaSuccess;
+    if (a.njobs < 1 || a.njobs > kMaxEnumJobs) return cudaErrorInvalidValue;
+    return a.narrow ? launch_enumerate_t<true>(a, num_sms, st, variant)
+                    : launch_enumerate_t<false>(a, num_sms, st, variant);
 }
 
 }  // namespace gp

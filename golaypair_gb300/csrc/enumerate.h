@@ -43,6 +43,7 @@ struct EnumArgs {
     unsigned long long* next_win;  // window handout counter (zero before the launch)
     int* incomplete;           // out: 1 if some window is unfinished
     int* status;
+    int narrow;                // 1: every job's word fits 63 bits (b * L <= 63): the 64-bit kernel
 };
 
 // variant 0: unrestricted registers; 1: 32 registers, full occupancy
