@@ -379,8 +379,8 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     t_win = since(tb);
     // ---- capacities and the device arena
     // appends after a job met its soft cap: a lane sees the count at most 16
-    // steps late (one per step), plus up to 160 queued per warp
-    const int64_t slack = threads * 16 + threads / 32 * 160 + 4096;
+    // steps late (one per step), plus a warp's queue
+    const int64_t slack = threads * 16 + threads / 32 * gp::kEnumQueue + 4096;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;

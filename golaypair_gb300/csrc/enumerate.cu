@@ -188,8 +188,8 @@ __device__ __forceinline__ bool job_full(const EnumJob& j) {
 // for, made the kernel memory-latency bound.)  A job's soft capacity is
 // checked on a count loaded at the previous check, so the load's latency
 // overlaps the steps in between.
-constexpr int kFlushAt = 128;
-constexpr int kQueue = kFlushAt + 32;  // per warp: < kFlushAt queued + 32 from one step
+constexpr int kFlushAt = kEnumQueue - 32;
+constexpr int kQueue = kEnumQueue;  // per warp: < kFlushAt queued + 32 from one step
 
 // NARROW: every job's words fit 63 bits, so a word and its window end are
 // 64-bit values (the high halves are zero and drop out of the registers).

@@ -14,6 +14,7 @@ namespace gp {
 
 constexpr int kMaxDigitSum = 1023;
 constexpr int kMaxEnumJobs = 8;
+constexpr int kEnumQueue = 272;  // candidates a warp queues in shared memory (written out from 240; static shared memory stays under 48 KB)
 
 struct U128p {
     uint64_t lo, hi;
