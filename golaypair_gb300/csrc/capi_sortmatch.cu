@@ -647,7 +647,10 @@ static int gp_sort_impl(gp_ctx* c, const char** in_paths, int n_in, const char* 
     StageRange nvtx_range("gp_sort");
     if (!c || (!in_paths && n_in > 0) || !out_path) return GP_ERR_ARG;
     cudaSetDevice(c->device);
-    std::string all, one;
+    // every input is read once
+    std::vector<std::string> texts(n_in);
+    for (int i = 0; i < n_in; ++i)
+        if (!slurp(in_paths[i], texts[i])) return c->fail(GP_ERR_IO, "sort: cannot read %s", in_paths[i]);
     {
         // all inputs binary survivor files of one job: the records are
         // formatted and sorted on the device
@@ -657,10 +660,9 @@ static int gp_sort_impl(gp_ctx* c, const char** in_paths, int n_in, const char* 
         bool binary = n_in > 0;
         gp::SurvHeader h0{};
         for (int i = 0; i < n_in && binary; ++i) {
-            if (!slurp(in_paths[i], one)) return c->fail(GP_ERR_IO, "sort: cannot read %s", in_paths[i]);
             gp::SurvHeader h;
             const uint8_t* body = nullptr;
-            const int kind = gp::surv_parse(one, h, &body);
+            const int kind = gp::surv_parse(texts[i], h, &body);
             if (kind < 0) return c->fail(GP_ERR_FORMAT, "sort: malformed survivor file %s", in_paths[i]);
             if (kind == 0 || (i > 0 && (h.L != h0.L || h.bits != h0.bits || h.k != h0.k || h.sig_bytes != h0.sig_bytes ||
                                         std::memcmp(h.alpha, h0.alpha, 16) != 0))) {
@@ -688,16 +690,21 @@ static int gp_sort_impl(gp_ctx* c, const char** in_paths, int n_in, const char* 
             return fclose(f) == 0 ? GP_OK : c->fail(GP_ERR_IO, "sort: write failed");
         }
     }
+    std::string all;
     for (int i = 0; i < n_in; ++i) {
-        if (!slurp(in_paths[i], one)) return c->fail(GP_ERR_IO, "sort: cannot read %s", in_paths[i]);
+        std::string& one = texts[i];
         gp::SurvHeader h;
         const uint8_t* body = nullptr;
         const int kind = gp::surv_parse(one, h, &body);
         if (kind < 0 || (kind > 0 && !gp::surv_to_text(h, body, all)))
             return c->fail(GP_ERR_FORMAT, "sort: malformed survivor file %s", in_paths[i]);
         if (kind > 0) continue;
-        all += one;
-        if (!one.empty() && one.back() != '\n') all.push_back('\n');
+        if (all.empty())
+            all.swap(one);  // the first text input: no copy
+        else
+            all += one;
+        if (!all.empty() && all.back() != '\n') all.push_back('\n');
+        std::string().swap(one);
     }
     std::string sorted;
     int rc = gp_sort_text(c, all, sorted);
