@@ -379,8 +379,20 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     t_win = since(tb);
     // ---- capacities and the device arena
     // appends after a job met its soft cap: a lane sees the count at most 16
-    // steps late (one per step), plus a warp's queue
-    const int64_t slack = threads * 16 + threads / 32 * gp::kEnumQueue + 4096;
+    // steps late, and a step (a block of words that differ in the last digit)
+    // appends at most one candidate per row sum with a role, and at most k;
+    // plus a warp's queue
+    auto slack_for = [&](const GenPlan& p) {
+        std::vector<int> sums;
+        for (auto& d : p.dec) {
+            sums.push_back(d.first);
+            sums.push_back(d.second);
+        }
+        std::sort(sums.begin(), sums.end());
+        const int64_t per_step =
+            std::max<int64_t>(1, std::min<int64_t>(p.k, (int64_t)(std::unique(sums.begin(), sums.end()) - sums.begin())));
+        return threads * 16 * per_step + threads / 32 * gp::kEnumQueue + 4096;
+    };
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
@@ -400,7 +412,7 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
             j.hard = j.soft;
         } else {
             j.soft = cfg.cand_cap;
-            j.hard = cfg.cand_cap + slack;
+            j.hard = cfg.cand_cap + slack_for(j.p);
         }
         // one iteration adds at most 2 records per candidate (x == y: A and B)
         j.rcap = 2 * j.hard + std::max<int64_t>(j.hard / 2, 4096);

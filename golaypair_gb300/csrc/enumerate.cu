@@ -289,13 +289,28 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
             }
         }
         if (!__any_sync(0xFFFFFFFFu, active)) break;
-        uint8_t role = 0;
-        W128 cand = w;
+        // One step takes a block: the prenecklace w and the words after it
+        // that only raise its last digit (FKM's successor of a word whose
+        // last digit is below the maximum is that word plus one in the last
+        // digit, with period L: a Lyndon word, so a necklace), up to the
+        // maximum digit or the window's end.  The block's necklaces are
+        // counted without visiting them one by one, and its candidates are
+        // the words whose digit sum (the first word's plus j) has a role.
+        const W128 w0 = w;
+        uint32_t cmask = 0;  // bit j: word w0 + j is a candidate
+        int s0 = 0;
         if (active) {
-            if (divides_L(jv, p)) {
-                ++necklaces;
-                role = role_tab[job][(NARROW || jv.narrow) ? digit_sum64(w.lo, jv) : digit_sum(w, jv)];
-            }
+            const uint64_t dmask = (1ull << jv.b) - 1ull;
+            const int dl = (int)(w.lo & dmask);
+            int run = (int)(jv.maxpat.lo & dmask) - dl;  // further words of the block
+            const bool same_hi = NARROW || end.hi == w.hi;
+            if (same_hi && end.lo - w.lo - 1ull < (uint64_t)run) run = (int)(end.lo - w.lo - 1ull);
+            const bool first = divides_L(jv, p);
+            necklaces += (unsigned long long)((first ? 1 : 0) + run);
+            s0 = (NARROW || jv.narrow) ? digit_sum64(w.lo, jv) : digit_sum(w, jv);
+            for (int j = first ? 0 : 1; j <= run; ++j)
+                if (role_tab[job][s0 + j]) cmask |= 1u << j;
+            w.lo += (uint64_t)run;  // the block's last word (its last digit carries into nothing)
             int np;
             if (NARROW || jv.narrow) {
                 uint64_t wl = w.lo;
@@ -313,13 +328,19 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
                 p = np;
             }
         }
-        // queue this step's candidates; write the queue out from kFlushAt
-        const uint32_t want = __ballot_sync(0xFFFFFFFFu, role != 0);
-        if (want) {
-            if (role) {
+        // queue the block's candidates, one per lane per round; write the
+        // queue out from kFlushAt
+        while (__any_sync(0xFFFFFFFFu, cmask != 0)) {
+            const bool has = cmask != 0;
+            const int j = has ? __ffs(cmask) - 1 : 0;
+            cmask &= cmask - 1u;
+            const uint32_t want = __ballot_sync(0xFFFFFFFFu, has);
+            if (has) {
                 const int slot = qlen + __popc(want & lt_mask);
+                W128 cand = w0;
+                cand.lo += (uint64_t)j;
                 q_word[wq][slot] = to_u4(cand);
-                q_role[wq][slot] = role;
+                q_role[wq][slot] = role_tab[job][s0 + j];
                 q_job[wq][slot] = (uint8_t)job;
             }
             qlen += __popc(want);
