@@ -378,10 +378,11 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
     }
     t_win = since(tb);
     // ---- capacities and the device arena
-    // appends after a job met its soft cap: a lane sees the count at most 16
-    // steps late, and a step (a block of words that differ in the last digit)
-    // appends at most one candidate per row sum with a role, and at most k;
-    // plus a warp's queue
+    // appends after a job met its soft cap: a lane sees the count at most
+    // 2 kCapCheck steps late, and a step (a block of the words that differ
+    // from a prenecklace in its last two digits: k rows of up to k words)
+    // appends at most one candidate per row and row sum with a role; plus a
+    // warp's queue
     auto slack_for = [&](const GenPlan& p) {
         std::vector<int> sums;
         for (auto& d : p.dec) {
@@ -389,9 +390,9 @@ int run_batch(gp_ctx* c, std::vector<JobRun>& jobs, const BatchCfg& cfg, int* it
             sums.push_back(d.second);
         }
         std::sort(sums.begin(), sums.end());
-        const int64_t per_step =
-            std::max<int64_t>(1, std::min<int64_t>(p.k, (int64_t)(std::unique(sums.begin(), sums.end()) - sums.begin())));
-        return threads * 16 * per_step + threads / 32 * gp::kEnumQueue + 4096;
+        const int64_t nsums = std::unique(sums.begin(), sums.end()) - sums.begin();
+        const int64_t per_step = std::max<int64_t>(1, (int64_t)p.k * std::min<int64_t>(p.k, nsums));
+        return threads * 2 * gp::kCapCheck * per_step + threads / 32 * gp::kEnumQueue + 4096;
     };
     size_t off = 0;
     auto take = [&](size_t bytes) {

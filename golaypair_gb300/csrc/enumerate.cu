@@ -175,6 +175,14 @@ __device__ __forceinline__ bool job_full(const EnumJob& j) {
     return (int64_t)*reinterpret_cast<volatile unsigned long long*>(j.count) >= j.soft_cap;
 }
 
+// Bits lo .. lo + n - 1 (n <= 16) of a job's digit-sum bitset, as bits 0 .. n - 1.
+__device__ __forceinline__ uint64_t role_bits(const unsigned long long* tb, int lo, int n) {
+    const int wi = lo >> 6, sh = lo & 63;
+    uint64_t x = tb[wi] >> sh;
+    if (sh) x |= tb[wi + 1] << (64 - sh);
+    return x & ((1ull << n) - 1ull);
+}
+
 // Each thread takes windows from a global counter.  A window whose job
 // has reached its soft capacity is left (position saved) and the thread goes
 // on with its next window, so one full job does not idle the others.
@@ -200,8 +208,17 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
     __shared__ uint4 q_word[8][kQueue];
     __shared__ uint8_t q_role[8][kQueue];
     __shared__ uint8_t q_job[8][kQueue];
-    for (int i = threadIdx.x; i < a.njobs * (kMaxDigitSum + 1); i += blockDim.x)
-        role_tab[i / (kMaxDigitSum + 1)][i % (kMaxDigitSum + 1)] = a.roles[i];
+    // bit s of tbits[j]: digit sum s has a role in job j (one spare word so
+    // that a 64-bit window starting below bit 1024 stays inside)
+    __shared__ unsigned long long tbits[kMaxEnumJobs][(kMaxDigitSum + 1) / 64 + 1];
+    for (int i = threadIdx.x; i < kMaxEnumJobs * ((kMaxDigitSum + 1) / 64 + 1); i += blockDim.x)
+        (&tbits[0][0])[i] = 0ull;
+    __syncthreads();
+    for (int i = threadIdx.x; i < a.njobs * (kMaxDigitSum + 1); i += blockDim.x) {
+        const int jj = i / (kMaxDigitSum + 1), ds = i % (kMaxDigitSum + 1);
+        role_tab[jj][ds] = a.roles[i];
+        if (a.roles[i]) atomicOr(&tbits[jj][ds >> 6], 1ull << (ds & 63));
+    }
     if (threadIdx.x < a.njobs) jobs[threadIdx.x] = a.jobs[threadIdx.x];
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -289,28 +306,64 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
             }
         }
         if (!__any_sync(0xFFFFFFFFu, active)) break;
-        // One step takes a block: the prenecklace w and the words after it
-        // that only raise its last digit (FKM's successor of a word whose
-        // last digit is below the maximum is that word plus one in the last
-        // digit, with period L: a Lyndon word, so a necklace), up to the
-        // maximum digit or the window's end.  The block's necklaces are
-        // counted without visiting them one by one, and its candidates are
-        // the words whose digit sum (the first word's plus j) has a role.
-        const W128 w0 = w;
-        uint32_t cmask = 0;  // bit j: word w0 + j is a candidate
-        int s0 = 0;
+        // One step takes a block of words that differ from the prenecklace w
+        // only in the last two digits (v, d), in FKM order:
+        //  * the rest of w's row: FKM's successor of a word whose last digit
+        //    is below the maximum K is the word with that digit raised by
+        //    one, with period L (a Lyndon word, so a necklace);
+        //  * when the last digit reaches K and the second-to-last v is below
+        //    K: the successor raises v and sets the last digit to the first
+        //    digit a_0 (period L - 1), then raises the last digit again
+        //    (period L) up to K; and so on up to v = K (L >= 3, so a_0 is not
+        //    the raised digit, and k^2 <= 64 for the candidate mask);
+        // up to the window's end.  The block's necklaces are counted without
+        // visiting them one by one, its candidates are the words whose digit
+        // sum has a role, and one successor follows the whole block.
+        W128 w0 = w;
+        uint64_t cmask = 0;  // bit (v - v0) * k + d: that word is a candidate
+        int spre = 0, v0 = 0, kk = 1;
         if (active) {
-            const uint64_t dmask = (1ull << jv.b) - 1ull;
-            const int dl = (int)(w.lo & dmask);
-            int run = (int)(jv.maxpat.lo & dmask) - dl;  // further words of the block
-            const bool same_hi = NARROW || end.hi == w.hi;
-            if (same_hi && end.lo - w.lo - 1ull < (uint64_t)run) run = (int)(end.lo - w.lo - 1ull);
-            const bool first = divides_L(jv, p);
-            necklaces += (unsigned long long)((first ? 1 : 0) + run);
-            s0 = (NARROW || jv.narrow) ? digit_sum64(w.lo, jv) : digit_sum(w, jv);
-            for (int j = first ? 0 : 1; j <= run; ++j)
-                if (role_tab[job][s0 + j]) cmask |= 1u << j;
-            w.lo += (uint64_t)run;  // the block's last word (its last digit carries into nothing)
+            const int b = jv.b;
+            const uint64_t dmask = (1ull << b) - 1ull;
+            const int K = (int)(jv.maxpat.lo & dmask);
+            kk = K + 1;
+            const int d0 = (int)(w.lo & dmask);
+            v0 = (int)((w.lo >> b) & dmask);
+            const bool two = jv.L >= 3 && kk * kk <= 64;
+            const int vmax = two ? K : v0;
+            // words at or past the window's end are cut: x = (v << b) | d below xend
+            uint32_t xend = 0xFFFFFFFFu;
+            const uint64_t m2 = (1ull << (2 * b)) - 1ull;
+            if ((NARROW || end.hi == w.hi) && (end.lo & ~m2) == (w.lo & ~m2)) xend = (uint32_t)(end.lo & m2);
+            const int a0 = (NARROW || jv.narrow) ? (int)((w.lo >> (b * (jv.L - 1))) & dmask) : digit(w, b, jv.L, 0);
+            const int s0 = (NARROW || jv.narrow) ? digit_sum64(w.lo, jv) : digit_sum(w, jv);
+            spre = s0 - v0 - d0;
+            const bool neck_first = divides_L(jv, p), neck_row = divides_L(jv, jv.L - 1);
+            int lastv = v0, lastd = d0;
+            for (int v = v0; v <= vmax; ++v) {
+                // row v: words (v, dlo .. dhi); every one a necklace but
+                // perhaps the first; candidates: the digit sums with a role
+                const int dlo = v == v0 ? d0 : a0;
+                int dhi = K;
+                bool cut = false;
+                const int64_t lim = (int64_t)xend - ((int64_t)v << b) - 1;  // xend = 2^32 - 1: no cut
+                if (lim < (int64_t)dhi) {
+                    dhi = (int)lim;
+                    cut = true;
+                }
+                if (dhi < dlo) break;
+                const int n = dhi - dlo + 1;
+                const bool first_neck = v == v0 ? neck_first : neck_row;
+                necklaces += (unsigned long long)(n - (first_neck ? 0 : 1));
+                uint64_t rm = role_bits(tbits[job], spre + v + dlo, n);
+                if (!first_neck) rm &= ~1ull;
+                cmask |= rm << ((v - v0) * kk + dlo);
+                lastv = v;
+                lastd = dhi;
+                if (cut) break;
+            }
+            // the block's last word, then its successor
+            w.lo = (w.lo & ~m2) | ((uint64_t)lastv << b) | (uint64_t)lastd;
             int np;
             if (NARROW || jv.narrow) {
                 uint64_t wl = w.lo;
@@ -332,23 +385,27 @@ __global__ void __launch_bounds__(256, MINB) enumerate_kernel(EnumArgs a) {
         // queue out from kFlushAt
         while (__any_sync(0xFFFFFFFFu, cmask != 0)) {
             const bool has = cmask != 0;
-            const int j = has ? __ffs(cmask) - 1 : 0;
-            cmask &= cmask - 1u;
+            const int t = has ? __ffsll((long long)cmask) - 1 : 0;
+            cmask &= cmask - 1ull;
             const uint32_t want = __ballot_sync(0xFFFFFFFFu, has);
             if (has) {
                 const int slot = qlen + __popc(want & lt_mask);
+                const int v = v0 + t / kk, d = t % kk;
                 W128 cand = w0;
-                cand.lo += (uint64_t)j;
+                const int b = jv.b;
+                const uint64_t m2 = (1ull << (2 * b)) - 1ull;
+                cand.lo = (cand.lo & ~m2) | ((uint64_t)v << b) | (uint64_t)d;
                 q_word[wq][slot] = to_u4(cand);
-                q_role[wq][slot] = role_tab[job][s0 + j];
+                q_role[wq][slot] = role_tab[job][spre + v + d];
                 q_job[wq][slot] = (uint8_t)job;
             }
             qlen += __popc(want);
             if (qlen >= kFlushAt) flush();
         }
-        // every 8 steps: leave a window whose job reached its soft capacity
-        // (by the count loaded 8 steps ago), then load the count afresh
-        if ((step & 7) == 0 && active && have) {
+        // every kCapCheck steps: leave a window whose job reached its soft
+        // capacity (by the count loaded kCapCheck steps ago), then load the
+        // count afresh
+        if ((step & (kCapCheck - 1)) == 0 && active && have) {
             if (seen_job == job && (int64_t)seen_count >= jobs[job].soft_cap) {
                 a.cur[win] = to_u4(w);
                 have = false;

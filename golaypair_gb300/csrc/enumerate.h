@@ -14,7 +14,10 @@ namespace gp {
 
 constexpr int kMaxDigitSum = 1023;
 constexpr int kMaxEnumJobs = 8;
-constexpr int kEnumQueue = 272;  // candidates a warp queues in shared memory (written out from 240; static shared memory stays under 48 KB)
+// Steps between a lane's checks of its job's candidate count against the
+// soft capacity (a step is a block of up to k^2 words; see enumerate.cu).
+constexpr int kCapCheck = 2;
+constexpr int kEnumQueue = 264;  // candidates a warp queues in shared memory (written out from 232; static shared memory stays under 48 KB)
 
 struct U128p {
     uint64_t lo, hi;
