@@ -10,10 +10,13 @@
 // windows; each thread starts at the first prenecklace >= its window's first
 // word and steps the FKM successor
 //     i = last position whose digit is not maximal; a_i += 1;
-//     a_j = a_{j-i} for j > i  (period i)
+//     a_j = a_{j-(i+1)} for j > i  (period i + 1)
 // until it leaves the window.  Words are packed (see rows.cuh), so the
-// successor is a handful of 128-bit bit operations.  Necklaces whose digit
-// sum matches a decomposition's row sum are appended (warp-aggregated) to a
+// successor is a handful of 64- or 128-bit bit operations.  One step takes a
+// block: the successors that only change the last two digits follow a fixed
+// pattern (rows of Lyndon words, see the kernel), so a block's necklaces are
+// counted row by row without visiting them.  Necklaces whose digit sum
+// matches a decomposition's row sum are appended (warp-aggregated) to a
 // candidate buffer with their A/B role bits.
 //
 // One launch serves several jobs (orders / compressions, each with its own
