@@ -18,15 +18,19 @@ float guard_band(int order) { return (float)(2e-3 * order); }
 
 }  // namespace
 
-const void* gp_ctx::twiddle_image(int L) {
-    auto it = twiddles.find(L);
+const void* gp_ctx::twiddle_image(int L, bool int8_rows, int* shift) {
+    const bool sh = int8_rows && gp::tc_i8_shifted(L);
+    if (shift) *shift = sh ? 1 : 0;
+    const int wrap = sh ? gp::tc_i8_wrap_rows(L) : 0;
+    const int key = 4 * L + wrap;
+    auto it = twiddles.find(key);
     if (it != twiddles.end()) return it->second.p;
     const int K = gp::tc_k_for_len(L);
     if (!K) return nullptr;
-    const size_t bytes = gp::build_twiddle_image(L, K, nullptr);
+    const size_t bytes = gp::build_twiddle_image(L, K, nullptr, wrap);
     std::vector<uint8_t> img(bytes);
-    gp::build_twiddle_image(L, K, img.data());
-    DevBuf& b = twiddles[L];
+    gp::build_twiddle_image(L, K, img.data(), wrap);
+    DevBuf& b = twiddles[key];
     if (!b.ensure(bytes)) return nullptr;
     if (cudaMemcpy(b.p, img.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
     return b.p;
@@ -57,12 +61,14 @@ int gp_ctx::enqueue_filter(const gp::RowSrc& src, int64_t n, int order, int paf,
         time_end(st, tb);
         return GP_OK;
     }
-    const void* img = twiddle_image(L);
+    int shift = 0;
+    const void* img = twiddle_image(L, src.seqs != nullptr, &shift);
     if (!img) return fail(GP_ERR_UNSUPPORTED, "tensor-core filter: unsupported length %d", L);
     if (src.words && !gp::tc_packed_supported(L, src.pack_bits))
         return fail(GP_ERR_UNSUPPORTED, "tensor-core filter: packed length %d x %d bits", L, src.pack_bits);
     GP_CUDA_TRY(this, cudaMemsetAsync(d_ucount, 0, sizeof(unsigned long long), st));
     gp::PsdTcArgs a;
+    a.i8_shift = shift;
     a.seqs = src.seqs;
     a.words = src.words;
     a.pack_bits = src.pack_bits;
@@ -94,11 +100,13 @@ int gp_ctx::enqueue_filter_dev(const gp::RowSrc& src, int64_t cap, const unsigne
                                int grid_per_sm, cudaStream_t st) {
     const int L = src.L;
     const double* tw = twiddle64(L);
-    const void* img = twiddle_image(L);
+    int shift = 0;
+    const void* img = twiddle_image(L, src.seqs != nullptr, &shift);
     if (!tw || !img) return fail(GP_ERR_UNSUPPORTED, "tensor-core filter: unsupported length %d", L);
     if (src.words && !gp::tc_packed_supported(L, src.pack_bits))
         return fail(GP_ERR_UNSUPPORTED, "tensor-core filter: packed length %d x %d bits", L, src.pack_bits);
     gp::PsdTcArgs a;
+    a.i8_shift = shift;
     a.seqs = src.seqs;
     a.words = src.words;
     a.pack_bits = src.pack_bits;
@@ -523,10 +531,12 @@ int gp_psd_tc_values(gp_ctx* c, const int8_t* seqs, int64_t n, int L, float* out
         !dp.ensure((size_t)n * (K / 2) * 4))
         return c->fail(GP_ERR_NOMEM, "allocation failed");
     GP_CUDA_TRY(c, cudaMemcpy(ds.p, seqs, (size_t)n * L, cudaMemcpyHostToDevice));
-    const void* img = c->twiddle_image(L);
+    int shift = 0;
+    const void* img = c->twiddle_image(L, true, &shift);
     if (!img) return c->fail(GP_ERR_UNSUPPORTED, "length %d", L);
     GP_CUDA_TRY(c, cudaMemset(c->counts.p, 0, sizeof(unsigned long long)));
     gp::PsdTcArgs a;
+    a.i8_shift = shift;
     a.seqs = ds.as<int8_t>();
     a.words = nullptr;
     a.pack_bits = 0;

@@ -114,7 +114,7 @@ struct gp_ctx {
     DevBuf seq_buf[2];
     DevBuf mask_buf[2];
     DevBuf unsure_buf[2];
-    std::map<int, DevBuf> twiddles;    // tensor-core B images, by L
+    std::map<int, DevBuf> twiddles;    // tensor-core B images, by 4 L + wrapped rows
     std::map<int, DevBuf> twiddles64;  // FP64 (cos, sin) tables, by L
     // optional CUDA-event timing of the main filter kernel (profiling)
     bool timing = false;
@@ -162,7 +162,9 @@ struct gp_ctx {
         return fail(GP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     }
     // device twiddle image for length L (tensor-core filter)
-    const void* twiddle_image(int L);
+    // tensor-core B image of length L: with the wrapped rows of shifted int8
+    // loads when int8_rows and the length takes them (*shift set to 1)
+    const void* twiddle_image(int L, bool int8_rows = false, int* shift = nullptr);
     // Multi-job tensor-core filter of device batches (packed words) followed
     // by the FP64 recheck of every job's unsure rows: two launches on st for
     // up to eight jobs, each job's tiles at its own padded K.  Per job as

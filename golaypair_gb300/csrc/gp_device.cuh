@@ -292,10 +292,10 @@ __host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
            | ((uint32_t)(M >> 4) << 24);      // M / 16
 }
 
-// int8 x4 -> two half2 (exact), via the 1024-bias trick: the half with bits
-// 0x64XX is 1024 + XX; biasing the byte by 128 keeps it in [1024, 1280).
-__device__ __forceinline__ void i8x4_to_h2x2(uint32_t w, uint32_t& lo, uint32_t& hi) {
-    const uint32_t u = w ^ 0x80808080u;
+// Four bytes x + 128 (x ^ 0x80 of signed bytes x) -> two fp16 pairs of x
+// (exact), via the 1024-bias trick: the half with bits 0x64XX is 1024 + XX,
+// and the biased byte keeps it in [1024, 1280).
+__device__ __forceinline__ void biased_u8x4_to_h2x2(uint32_t u, uint32_t& lo, uint32_t& hi) {
     uint32_t a = __byte_perm(u, 0x64646464u, 0x4140u);
     uint32_t b = __byte_perm(u, 0x64646464u, 0x4342u);
     const __half2 bias = __half2half2(__ushort_as_half((unsigned short)0x6480u));  // 1152
@@ -303,6 +303,11 @@ __device__ __forceinline__ void i8x4_to_h2x2(uint32_t w, uint32_t& lo, uint32_t&
     __half2 hb = __hsub2(*reinterpret_cast<__half2*>(&b), bias);
     lo = *reinterpret_cast<uint32_t*>(&ha);
     hi = *reinterpret_cast<uint32_t*>(&hb);
+}
+
+// int8 x4 -> two half2 (exact)
+__device__ __forceinline__ void i8x4_to_h2x2(uint32_t w, uint32_t& lo, uint32_t& hi) {
+    biased_u8x4_to_h2x2(w ^ 0x80808080u, lo, hi);
 }
 
 }  // namespace gp

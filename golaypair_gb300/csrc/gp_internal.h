@@ -36,6 +36,11 @@ struct PsdTcArgs {
     unsigned long long* unsure_count;
     int64_t unsure_cap;
     float* psd_out;          // optional n x (K/2) PSD values
+    // int8 rows: 1 = each row is read from the 4-byte boundary at or below
+    // its first byte and sits s = (row * L) mod 4 columns along A, the bytes
+    // of neighbouring rows masked; the image then carries tc_i8_wrap_rows(L)
+    // wrapped twiddle rows past L (tc_i8_shifted(L) must hold)
+    int i8_shift = 0;
     int* status;
     unsigned long long* trace;  // optional per-role cycle counters (diagnostics)
 };
@@ -55,9 +60,21 @@ enum TcTrace {
 };
 
 // Builds the B-operand image (hi and lo twiddles) for length L, K = padded L.
-// Returns its size in bytes; writes it to out when out != nullptr.
-size_t build_twiddle_image(int L, int K, void* out);
+// Rows j = L .. L + wrap - 1 of the sequence axis hold the twiddles of
+// j - L (the DFT's period), for int8 rows loaded with a shift; every other
+// row past L is zero.  Returns its size in bytes; writes it to out when
+// out != nullptr.
+size_t build_twiddle_image(int L, int K, void* out, int wrap = 0);
 int tc_k_for_len(int L);               // padded K (multiple of 16, > L), or 0 if unsupported
+
+// Shifted loads of int8 rows (PsdTcArgs::i8_shift).  A row of length L that
+// starts s bytes past a 4-byte boundary (s = (row * L) mod 4: 0 when L is a
+// multiple of 4, 0 or 2 when L = 2 mod 4, 0..3 when L is odd) is placed s
+// columns along A; shifting a sequence multiplies X_k by a unit phase, so
+// the PSD is unchanged when the twiddle rows continue periodically past L.
+// Applies when K <= 64 and L + max s <= K.
+bool tc_i8_shifted(int L);
+int tc_i8_wrap_rows(int L);  // wrapped image rows for the shifted loads (max s), 0 if they do not apply
 
 // Where twiddle row `nrow` (0..K-1), column j (0..K-1), part (0 hi, 1 lo)
 // sits in the B image, as an index of fp16 elements.  The image is a 2K x K

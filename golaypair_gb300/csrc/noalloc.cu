@@ -52,8 +52,9 @@ constexpr size_t kNoAllocScratchBytes = kOffUnsure + (size_t)kNoAllocMaxRows * 4
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Twiddles built on the device: the tensor-core image in the same canonical
-// layout as build_twiddle_image, and the FP64 (cos, sin) table.
-__global__ void noalloc_twiddles_kernel(unsigned char* scratch, int L, int K) {
+// layout as build_twiddle_image (wrap: rows L .. L + wrap - 1 continue the
+// period, for shifted int8 loads), and the FP64 (cos, sin) table.
+__global__ void noalloc_twiddles_kernel(unsigned char* scratch, int L, int K, int wrap) {
     uint16_t* img = reinterpret_cast<uint16_t*>(scratch + kOffImage);
     double* tw = reinterpret_cast<double*>(scratch + kOffTw64);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < K * K; e += gridDim.x * blockDim.x) {
@@ -61,8 +62,8 @@ __global__ void noalloc_twiddles_kernel(unsigned char* scratch, int L, int K) {
         int bin = 0;
         const int kind = tc_row_kind(nrow, L, K, &bin);
         double w = 0.0;
-        if (kind != 0 && j < L) {
-            const int m = (int)(((long long)j * bin) % L);
+        if (kind != 0 && j < L + wrap) {
+            const int m = (int)(((long long)(j % L) * bin) % L);
             double s, c;
             sincospi(2.0 * (double)m / (double)L, &s, &c);
             w = kind == 3 ? 1.0 : kind == 2 ? s : c;
@@ -131,7 +132,7 @@ extern "C" int gp_psd_filter_noalloc(const int8_t* d_seqs, int64_t n, int L, int
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // clear what the kernels count from zero; the rest is overwritten
     if (cudaMemsetAsync(s + kOffStatus, 0, 512, st) != cudaSuccess) return GP_ERR_CUDA;
-    noalloc_twiddles_kernel<<<64, 256, 0, st>>>(s, L, K);
+    noalloc_twiddles_kernel<<<64, 256, 0, st>>>(s, L, K, tc_i8_wrap_rows(L));
     if (cudaGetLastError() != cudaSuccess) return GP_ERR_CUDA;
     const double thr = 2.0 * order - paf + 0.001;
     PsdTcArgs a;
@@ -142,6 +143,7 @@ extern "C" int gp_psd_filter_noalloc(const int8_t* d_seqs, int64_t n, int L, int
     a.n = n;
     a.L = L;
     a.bimage = s + kOffImage;
+    a.i8_shift = tc_i8_shifted(L) ? 1 : 0;
     a.thr = (float)thr;
     a.guard_cfg = (float)(2e-3 * order);
     a.err_coef = tc_err_coef(K);

@@ -9,7 +9,12 @@
 //
 // Row n < K/2 of W is the cosine of bin n+1, row K/2 + n the sine of bin
 // n+1; bins above L/2 and columns j >= L are zero, so the padding columns of
-// X never contribute.  K = L + 1 rounded up to 16, so the last cosine row
+// X never contribute.  The exception: int8 rows of a length whose rows start
+// off 4-byte boundaries are read from the boundary below and placed s <= 3
+// columns along (s = (row L) mod 4, no byte realignment per row); columns
+// j = L .. L + 2 then hold the twiddles of j - L, so the shifted row's X_k
+// gains a unit phase and its PSD is unchanged, and the converters clear
+// the neighbouring rows' bytes.  K = L + 1 rounded up to 16, so the last cosine row
 // (bin K/2) is always beyond L/2: it holds ones instead, and that column of
 // D is the row sum X_0 (exact).  By Parseval, L sum x^2 = X_0^2 + 2 sum_k p_k
 // (bin L/2 of an even L counted twice: an upper bound) <= X_0^2 + 2 (L/2)
@@ -61,10 +66,13 @@ namespace gp {
 
 namespace {
 
-template <int K, int B, bool WRITE_PSD, bool TR>
+template <int K, int B, bool WRITE_PSD, bool TR, bool SH>
 __global__ void __launch_bounds__(kThreads, TcCfg<K>::MIN_BLOCKS) psd_tc_kernel(PsdTcArgs a, SmemLayout lay) {
-    tc_body<K, B, WRITE_PSD, TR>(a, lay, blockIdx.x, gridDim.x);
+    tc_body<K, B, WRITE_PSD, TR, SH>(a, lay, blockIdx.x, gridDim.x);
 }
+
+// largest padded K with shifted int8 loads (one mask register per 4 bytes)
+constexpr int kMaxShiftK = 64;
 
 template <int K, int B, bool WP>
 cudaError_t launch_kb(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
@@ -73,10 +81,16 @@ cudaError_t launch_kb(const PsdTcArgs& a, int num_sms, cudaStream_t st) {
     const int64_t ntiles = (a.n + kTileM - 1) / kTileM;
     if (ntiles == 0) return cudaSuccess;
     if (a.n >= (int64_t(1) << 31)) return cudaErrorInvalidValue;  // 32-bit row indices
+    if (a.i8_shift && (B != 0 || !tc_i8_shifted(a.L))) return cudaErrorInvalidValue;
     // the counting variant exists for the int8 input only (diagnostics)
-    auto kern = psd_tc_kernel<K, B, WP, false>;
-    if constexpr (B == 0 && !WP)
-        if (a.trace) kern = psd_tc_kernel<K, B, WP, true>;
+    auto kern = psd_tc_kernel<K, B, WP, false, false>;
+    if constexpr (B == 0 && K <= kMaxShiftK)
+        if (a.i8_shift) kern = psd_tc_kernel<K, B, WP, false, true>;
+    if constexpr (B == 0 && !WP) {
+        if (a.trace) kern = psd_tc_kernel<K, B, WP, true, false>;
+        if constexpr (K <= kMaxShiftK)
+            if (a.trace && a.i8_shift) kern = psd_tc_kernel<K, B, WP, true, true>;
+    }
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
     if (e != cudaSuccess) return e;
     const int per_sm = a.grid_per_sm > 0 && a.grid_per_sm < C::MIN_BLOCKS ? a.grid_per_sm : C::MIN_BLOCKS;
@@ -152,6 +166,17 @@ int tc_k_for_len(int L) {
     return K <= kMaxTcK ? K : 0;
 }
 
+namespace {
+int i8_max_shift(int L) { return L % 4 == 0 ? 0 : L % 2 == 0 ? 2 : 3; }
+}  // namespace
+
+bool tc_i8_shifted(int L) {
+    const int K = tc_k_for_len(L);
+    return K != 0 && K <= kMaxShiftK && L + i8_max_shift(L) <= K;
+}
+
+int tc_i8_wrap_rows(int L) { return tc_i8_shifted(L) ? i8_max_shift(L) : 0; }
+
 bool tc_packed_supported(int L, int b) {
     const int K = tc_k_for_len(L);
     if (!K || b < 1 || b > 4 || b * L > 128) return false;
@@ -170,17 +195,18 @@ float tc_err_coef(int K) {
     return (float)(std::sqrt(2.0) * (std::ldexp(1.0, -24) + steps * 17.0 * std::ldexp(1.0, -22)));
 }
 
-size_t build_twiddle_image(int L, int K, void* out) {
+size_t build_twiddle_image(int L, int K, void* out, int wrap) {
     const size_t bytes = (size_t)2 * K * K * 2;
     if (!out) return bytes;
     std::vector<uint16_t> img((size_t)2 * K * K, 0);
     const double two_pi = 6.283185307179586476925286766559;
+    const int jend = L + wrap < K ? L + wrap : K;
     for (int nrow = 0; nrow < K; ++nrow) {
         int bin = 0;
         const int kind = tc_row_kind(nrow, L, K, &bin);
         if (kind == 0) continue;
-        for (int j = 0; j < L; ++j) {
-            const int m = (int)(((long long)j * bin) % L);
+        for (int j = 0; j < jend; ++j) {
+            const int m = (int)(((long long)(j % L) * bin) % L);
             const double w = kind == 3 ? 1.0 : kind == 2 ? std::sin(two_pi * m / L) : std::cos(two_pi * m / L);
             const uint16_t h = half_bits(w);
             const uint16_t l = half_bits(w - half_value(h));

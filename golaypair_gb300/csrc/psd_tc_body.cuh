@@ -305,10 +305,12 @@ __device__ __noinline__ float2 exact_pass(uint32_t taddr, float* psd_row) {
 }
 
 // TR: per-role cycle counters (diagnostics build of the kernel).
+// SH: int8 rows read from the 4-byte boundary at or below their first byte
+// (PsdTcArgs::i8_shift; the image carries the wrapped twiddle rows).
 // The whole kernel for one job: roles, rings and TMEM of TcCfg<K>, input
 // words (B = 1..4) or int8 rows (B = 0), over the tiles first, first +
 // stride, ... of the job (the one-job kernel: its CTA index and grid size).
-template <int K, int B, bool WRITE_PSD, bool TR>
+template <int K, int B, bool WRITE_PSD, bool TR, bool SH = false>
 __device__ __forceinline__ void tc_body(const PsdTcArgs& a, const SmemLayout& lay, int first, int stride) {
     using C = TcCfg<K>;
     extern __shared__ uint8_t smem_raw_base[];
@@ -380,12 +382,30 @@ __device__ __forceinline__ void tc_body(const PsdTcArgs& a, const SmemLayout& la
 
     if (warp < kConvWarps) {
         // ------------------------------------------------ converters
-        // Row r's bytes L..K-1 in a full tile are the next row's first
-        // bytes: they land in A columns whose B rows are all zero, so they
-        // add nothing and are not masked.
+        // Without SH, row r's bytes L..K-1 in a full tile are the next
+        // row's first bytes: they land in A columns whose B rows are all
+        // zero, so they add nothing and are not masked.
         const int r = threadIdx.x;  // row of the tile = TMEM lane
         const int norm = 128 - B * L;  // packed: left shift that puts digit 0 at bit 127
         const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16) + (uint32_t)C::A_COL0;
+        // SH: the row's bytes sit at columns [s, s + L) of the K bytes read
+        // from the 4-byte boundary below it (the tile starts on one, so s is
+        // the same for every tile); mk keeps those bytes and clears the
+        // neighbouring rows' (a cleared byte converts to 0)
+        uint32_t mk[SH ? K / 4 : 1];
+        if constexpr (SH) {
+            const int s = (r * L) & 3;
+#pragma unroll
+            for (int i = 0; i < K / 4; ++i) {
+                uint32_t m = 0u;
+#pragma unroll
+                for (int bb = 0; bb < 4; ++bb) {
+                    const int col = 4 * i + bb;
+                    if (col >= s && col < s + L) m |= 0xFFu << (8 * bb);
+                }
+                mk[i] = m;
+            }
+        }
         int it = 0;
         Ring raw, ast;
         unsigned long long tr0 = 0, tr1 = 0, tr2 = 0, tr3 = 0, tr4 = 0;
@@ -415,16 +435,26 @@ __device__ __forceinline__ void tc_body(const PsdTcArgs& a, const SmemLayout& la
                     const uint8_t* raw = sRaw + rs * lay.raw_stride;
                     const int off = r * L;
                     const uint32_t* wp = reinterpret_cast<const uint32_t*>(raw + (off & ~3));
-                    const uint32_t sh = (uint32_t)(off & 3) * 8u;
-                    uint32_t wv[C::KW];
+                    if constexpr (SH) {
+                        // mask and sign bias in one logic op per word
 #pragma unroll
-                    for (int i = 0; i < C::KW; ++i) wv[i] = wp[i];
+                        for (int c = 0; c < C::KCH; ++c) {
+                            biased_u8x4_to_h2x2((wp[2 * c] & mk[2 * c]) ^ 0x80808080u, h[4 * c], h[4 * c + 1]);
+                            biased_u8x4_to_h2x2((wp[2 * c + 1] & mk[2 * c + 1]) ^ 0x80808080u, h[4 * c + 2],
+                                                h[4 * c + 3]);
+                        }
+                    } else {
+                        const uint32_t sh = (uint32_t)(off & 3) * 8u;
+                        uint32_t wv[C::KW];
 #pragma unroll
-                    for (int c = 0; c < C::KCH; ++c) {
-                        const uint32_t lo = __funnelshift_r(wv[2 * c], wv[2 * c + 1], sh);
-                        const uint32_t hi = __funnelshift_r(wv[2 * c + 1], wv[2 * c + 2], sh);
-                        i8x4_to_h2x2(lo, h[4 * c], h[4 * c + 1]);
-                        i8x4_to_h2x2(hi, h[4 * c + 2], h[4 * c + 3]);
+                        for (int i = 0; i < C::KW; ++i) wv[i] = wp[i];
+#pragma unroll
+                        for (int c = 0; c < C::KCH; ++c) {
+                            const uint32_t lo = __funnelshift_r(wv[2 * c], wv[2 * c + 1], sh);
+                            const uint32_t hi = __funnelshift_r(wv[2 * c + 1], wv[2 * c + 2], sh);
+                            i8x4_to_h2x2(lo, h[4 * c], h[4 * c + 1]);
+                            i8x4_to_h2x2(hi, h[4 * c + 2], h[4 * c + 3]);
+                        }
                     }
                 } else {
                     partial_row_store<K>(a.seqs, row, n32, L, aaddr);

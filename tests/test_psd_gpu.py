@@ -37,6 +37,11 @@ CASES = [  # (order, compress, paf)
     (16, 2, 0), (26, 2, 0), (34, 2, 0), (50, 2, 0), (58, 2, 0), (68, 2, 0), (90, 2, 0), (90, 5, 0),
     (57, 3, -2), (57, 1, -2), (16, 1, 0), (26, 1, 0), (38, 1, 0), (98, 1, 0), (126, 1, 0), (252, 2, 0),
     (70, 1, 0), (86, 1, 0), (170, 2, 0),  # padded lengths K = 80 and 96
+    # int8 rows of a length not a multiple of 4 are read from the 4-byte
+    # boundary below them and placed 1-3 columns along when L + max shift
+    # <= K (K <= 64): L = 46 fills K = 48 exactly; L = 31, 47, 63 (L + 3 > K)
+    # keep the byte-realigning loads; L = 54, 60 at K = 64
+    (92, 2, 0), (62, 2, 0), (94, 2, 0), (126, 2, 0), (54, 1, 0), (60, 1, 0),
 ]
 
 
@@ -91,7 +96,7 @@ def test_psd_filter_cfg4_distribution(ctx, oracle_lib):
 
 
 @pytest.mark.parametrize("order,compress,paf", [(16, 2, 0), (26, 2, 0), (57, 3, -2), (90, 2, 0), (90, 5, 0),
-                                                (57, 1, -2), (126, 1, 0)])
+                                                (57, 1, -2), (126, 1, 0), (62, 2, 0), (92, 2, 0)])
 def test_tc_psd_error_within_guard(ctx, oracle_lib, order, compress, paf):
     L = order // compress
     rng = np.random.default_rng(5)

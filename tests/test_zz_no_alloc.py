@@ -43,6 +43,7 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
     cases = [
         (26, 2, 0, 100_000),    # L 13, K 16
         (57, 3, -2, 200_003),   # L 19, K 32
+        (62, 2, 0, 60_000),     # L 31, K 32 (no shifted loads: 31 + 3 > 32)
         (90, 2, 0, 300_000),    # L 45, K 48
         (57, 1, -2, 100_000),   # L 57, K 64
         (72, 1, 0, 60_000),     # L 72, K 80
