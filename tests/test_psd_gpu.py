@@ -137,3 +137,27 @@ def test_bounded_wait_gives_up_and_context_stays_usable(ctx, oracle_lib):
     oracle_lib.gpo_psd_filter_batch(seqs.ctypes.data, len(seqs), 8, 16, 0, want.ctypes.data, 1)
     got, _ = ctx.psd_filter(seqs, 16, 0, gp.GP_PSD_TC_GUARDED)
     assert np.array_equal(got.astype(bool), want.astype(bool))
+
+
+@pytest.mark.parametrize("L", [45, 47])
+def test_device_rows_at_any_byte_offset(ctx, oracle_lib, L):
+    """gp_psd_filter_device on rows that start at byte offsets 0, 16 (whole
+    tiles bulk-copied; length 45 takes the shifted loads, 47 the
+    byte-realigning ones) and 1, 3, 45 (not 16-byte aligned: every row read
+    by plain loads); the verdicts equal the oracle's in every case."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(L)
+    n = 20_000 + 45  # a tail tile and a partial mask word
+    seqs = rng.choice(np.array([-2, 0, 2], dtype=np.int8), size=(n, L))
+    want = oracle_verdicts(oracle_lib, seqs, 2 * L, 0)
+    flat = torch.from_numpy(seqs.reshape(-1))
+    for off in (0, 16, 1, 3, 45):
+        buf = torch.zeros(n * L + 64, dtype=torch.int8, device="cuda")
+        buf[off:off + n * L] = flat.cuda()
+        mask = torch.full(((n + 31) // 32,), -1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        ctx.psd_filter_device(buf.data_ptr() + off, n, L, 2 * L, 0, gp.GP_PSD_TC_GUARDED, mask.data_ptr(), None)
+        ctx.check_stream(None)
+        bits = mask.cpu().numpy().view(np.uint32)
+        got = ((bits[np.arange(n) // 32] >> (np.arange(n) % 32)) & 1).astype(bool)
+        assert np.array_equal(got, want), f"offset {off}: {np.sum(got != want)} verdicts differ"
