@@ -26,7 +26,9 @@
 //    precomputed sums over the trailing free positions (the "suffix", up to a
 //    few hundred combinations in shared memory): one packed fp32 add per bin
 //    and |X|^2 per expansion.  A rigorous bound of the fp32 rounding error
-//    sorts every expansion into sure pass, sure reject, or unsure.
+//    sorts every expansion into sure pass, sure reject, or unsure.  A batch
+//    scans each distinct side once: a side repeats in the pairs of its
+//    signature group, and its survivors do not depend on the pair or role.
 // 3. ux_recheck_kernel: unsure expansions in FP64 (one warp per expansion,
 //    lanes over bins), the reference's filter psd[k] <= 2n - paf + 0.001.
 // 4. The join.  For a complementary pair, PAF_a(s) + PAF_b(s) = paf * c'
@@ -34,7 +36,8 @@
 //    every k != 0, so the a-side's inverted signature equals the b-side's
 //    plain one: every pair the reference writes joins on the exact integer
 //    PAF vectors (a: paf*c' - PAF_a, b: PAF_b).  ux_key_kernel hashes those
-//    vectors and buckets the survivors by (pair, hash bits);
+//    vectors and buckets the survivors by (pair, hash bits), one entry per
+//    pair and role that uses the survivor's side;
 //    ux_join_kernel matches each bucket in a shared-memory hash table and
 //    verifies the PAF sums exactly.  No signature is computed on the device.
 // 5. Host: the few matched pairs get their FP64 signatures; a pair is kept
@@ -51,6 +54,7 @@
 #include <set>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <type_traits>
 #include <vector>
 
@@ -64,7 +68,7 @@ constexpr int kMaxL = 64;          // compressed length
 constexpr int kMaxLnew = 128;      // uncompressed length
 constexpr int kMaxRows = 32;       // letters + first-entry lists
 constexpr int kScanThreads = 256;  // prefixes per scan unit
-constexpr int kRankBits = 40;      // survivor word: side << 40 | rank
+constexpr int kRankBits = 40;      // survivor word: side << 40 | rank (the batch's distinct side)
 constexpr uint64_t kRankMask = (uint64_t(1) << kRankBits) - 1;
 constexpr int kMaxSidesPerBatch = 1 << 23;
 constexpr int kBucketTarget = 512;  // survivors per join bucket (mean)
@@ -543,12 +547,10 @@ __device__ __forceinline__ uint64_t mix64(uint64_t h) {
     return h;
 }
 
-// join key of a survivor: a-sides (even side index) hash paf*c' - PAF_a(s),
-// b-sides PAF_b(s); complementary pairs have equal keys
-__device__ __forceinline__ uint64_t join_key(const LevelDev& lv, uint64_t val) {
-    int paf[kMaxLnew / 2];
-    expansion_paf(lv, val, paf);
-    const bool is_a = ((val >> kRankBits) & 1) == 0;
+// join key of a survivor's PAF vector in its role: as the a-side of a pair
+// it hashes paf*c' - PAF_a(s), as the b-side PAF_b(s); complementary pairs
+// have equal keys
+__device__ __forceinline__ uint64_t join_key(const LevelDev& lv, const int* paf, bool is_a) {
     uint64_t h = 0x243f6a8885a308d3ull;
     for (int s = 0; s < lv.H; ++s) {
         const int v = is_a ? lv.target - paf[s] : paf[s];
@@ -557,42 +559,64 @@ __device__ __forceinline__ uint64_t join_key(const LevelDev& lv, uint64_t val) {
     return mix64(h);
 }
 
+// Survivor words carry the batch's unique side index: equal compressed
+// sides (a side repeats in the pairs of its signature group) are expanded
+// and filtered once.  Each survivor yields one join entry per use of its
+// side, a use being (pair, role) with role 1 for the b-side.
 struct KeyArgs {
     LevelDev lv;
     const uint64_t* surv;
     uint64_t n;
+    const uint32_t* use_beg;    // [unique sides + 1] first use of each side
+    const uint32_t* uses;       // pair << 1 | role
     const uint8_t* pair_lg;     // [pairs] log2 buckets of the pair (255: pair skipped)
     const uint32_t* pair_base;  // [pairs] first bucket of the pair
-    uint64_t* keys;
-    uint32_t* bucket;
+    uint64_t* keys;             // [entries]
+    uint32_t* bucket;           // [entries]
+    uint32_t* eidx;             // [entries] survivor index | role << 31
+    uint64_t entry_cap;
+    unsigned long long* ecount;
     uint32_t* bcount;
+    int* status;
 };
 
 __global__ void ux_key_kernel(KeyArgs a) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t v = a.surv[i];
-        const uint32_t pair = (uint32_t)(v >> (kRankBits + 1));
-        const int lg = a.pair_lg[pair];
-        if (lg == 255) {
-            a.bucket[i] = 0xFFFFFFFFu;
-            continue;
+        const uint32_t u = (uint32_t)(v >> kRankBits);
+        const uint32_t j0 = a.use_beg[u], j1 = a.use_beg[u + 1];
+        int paf[kMaxLnew / 2];
+        bool have = false;
+        for (uint32_t j = j0; j < j1; ++j) {
+            const uint32_t code = a.uses[j], pair = code >> 1, role = code & 1u;
+            const int lg = a.pair_lg[pair];
+            if (lg == 255) continue;
+            if (!have) {
+                expansion_paf(a.lv, v, paf);
+                have = true;
+            }
+            const uint64_t h = join_key(a.lv, paf, role == 0);
+            const uint32_t b = a.pair_base[pair] + (lg ? (uint32_t)(h >> (64 - lg)) : 0u);
+            const unsigned long long e = atomicAdd(a.ecount, 1ull);
+            if (e >= a.entry_cap) {
+                flag_overflow(a.status);
+                continue;
+            }
+            a.keys[e] = h;
+            a.bucket[e] = b;
+            a.eidx[e] = (uint32_t)i | (role << 31);
+            atomicAdd(&a.bcount[b], 1u);
         }
-        const uint64_t h = join_key(a.lv, v);
-        const uint32_t b = a.pair_base[pair] + (lg ? (uint32_t)(h >> (64 - lg)) : 0u);
-        a.keys[i] = h;
-        a.bucket[i] = b;
-        atomicAdd(&a.bcount[b], 1u);
     }
 }
 
-__global__ void ux_scatter_kernel(const uint64_t* surv, const uint64_t* keys, const uint32_t* bucket, uint64_t n,
+__global__ void ux_scatter_kernel(const uint64_t* keys, const uint32_t* bucket, const uint32_t* eidx, uint64_t n,
                                   const uint32_t* boff, uint32_t* bcur, uint64_t* ent_h, uint32_t* ent_i) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t b = bucket[i];
-        if (b == 0xFFFFFFFFu) continue;
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = bucket[e];
         const uint32_t pos = boff[b] + atomicAdd(&bcur[b], 1u);
-        ent_h[pos] = keys[i];
-        ent_i[pos] = (uint32_t)i | ((uint32_t)((surv[i] >> kRankBits) & 1) << 31);  // bit 31: b-side
+        ent_h[pos] = keys[e];
+        ent_i[pos] = eidx[e];  // bit 31: b-side
     }
 }
 
@@ -604,13 +628,29 @@ struct JoinArgs {
     const uint32_t* boff;
     const uint32_t* bcount;
     uint32_t n_buckets;
-    uint64_t* matches;  // (a survivor word, b survivor word)
+    const uint32_t* pair_base;  // [pairs] first bucket (non-decreasing; a skipped pair has none)
+    uint32_t n_pairs;
+    uint64_t* matches;  // (a survivor word, b survivor word), side fields 2 pair and 2 pair + 1
     uint64_t match_cap;
     unsigned long long* counters;
     int* status;
 };
 
-__device__ __forceinline__ void verify_and_emit(const JoinArgs& a, uint32_t ia, uint32_t ib) {
+// the pair that owns bucket bk: the last pair whose first bucket is <= bk
+// (a skipped pair shares its base with the next pair and owns no bucket)
+__device__ __forceinline__ uint32_t bucket_pair(const JoinArgs& a, uint32_t bk) {
+    uint32_t lo = 0, hi = a.n_pairs;  // answer in [lo, hi)
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (a.pair_base[mid] <= bk)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void verify_and_emit(const JoinArgs& a, uint32_t ia, uint32_t ib, uint32_t pair) {
     int pa[kMaxLnew / 2], pb[kMaxLnew / 2];
     const uint64_t va = a.surv[ia], vb = a.surv[ib];
     expansion_paf(a.lv, va, pa);
@@ -619,8 +659,8 @@ __device__ __forceinline__ void verify_and_emit(const JoinArgs& a, uint32_t ia, 
         if (pa[s] + pb[s] != a.lv.target) return;
     const unsigned long long pos = atomicAdd(&a.counters[2], 1ull);
     if (pos < a.match_cap) {
-        a.matches[2 * pos] = va;
-        a.matches[2 * pos + 1] = vb;
+        a.matches[2 * pos] = ((uint64_t)(2 * pair) << kRankBits) | (va & kRankMask);
+        a.matches[2 * pos + 1] = ((uint64_t)(2 * pair + 1) << kRankBits) | (vb & kRankMask);
     } else {
         flag_overflow(a.status);
     }
@@ -633,13 +673,14 @@ __global__ void __launch_bounds__(256) ux_join_kernel(JoinArgs a) {
     __shared__ uint32_t tab[kJoinTab];
     for (uint32_t bk = blockIdx.x; bk < a.n_buckets; bk += gridDim.x) {
         const uint32_t n = a.bcount[bk], base = a.boff[bk];
+        const uint32_t pair = n ? bucket_pair(a, bk) : 0u;
         __syncthreads();
         if (n > kJoinMaxB) {  // rare: quadratic over the bucket
             for (uint64_t w = threadIdx.x; w < (uint64_t)n * n; w += blockDim.x) {
                 const uint32_t e = (uint32_t)(w / n), f = (uint32_t)(w % n);
                 const uint32_t ie = a.ent_i[base + e], jf = a.ent_i[base + f];
                 if ((ie >> 31) || !(jf >> 31) || a.ent_h[base + e] != a.ent_h[base + f]) continue;
-                verify_and_emit(a, ie & 0x7FFFFFFFu, jf & 0x7FFFFFFFu);
+                verify_and_emit(a, ie & 0x7FFFFFFFu, jf & 0x7FFFFFFFu, pair);
             }
             continue;
         }
@@ -657,7 +698,7 @@ __global__ void __launch_bounds__(256) ux_join_kernel(JoinArgs a) {
             const uint64_t h = a.ent_h[base + e];
             uint32_t slot = (uint32_t)h & (kJoinTab - 1);
             for (uint32_t t; (t = tab[slot]) != 0u; slot = (slot + 1) & (kJoinTab - 1))
-                if (a.ent_h[base + t - 1] == h) verify_and_emit(a, ie, a.ent_i[base + t - 1] & 0x7FFFFFFFu);
+                if (a.ent_h[base + t - 1] == h) verify_and_emit(a, ie, a.ent_i[base + t - 1] & 0x7FFFFFFFu, pair);
         }
     }
 }
@@ -1138,7 +1179,8 @@ struct Batcher {
     gp_ctx* c;
     const Level& lv;
     const LevelDev& ld;
-    const std::vector<Side>& sides;  // 2 per pair: a, b
+    const std::vector<Side>& sides;    // 2 per pair: a, b
+    const std::vector<uint8_t>& seqs;  // the sides' letter indices, L per side
     cudaStream_t s;
     ScanKernel scan;
     int scan_blocks = 0;
@@ -1155,22 +1197,45 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     *overflowed = false;
     const int L = lv.L;
     const int64_t np_ = p1 - p0, ns = 2 * np_;
-    std::vector<uint8_t> rows((size_t)ns * L);
-    std::vector<uint64_t> ubeg(ns + 1), pcnt(ns);
-    std::vector<uint32_t> nsuf(ns);
+    // the batch's distinct sides (equal letters expand and filter the same
+    // way, whatever the pair or role): scanned once each
+    std::vector<uint32_t> uid(ns);
+    std::vector<int64_t> urep;  // unique side -> its first batch side
+    {
+        std::unordered_map<std::string, uint32_t> seen;
+        seen.reserve((size_t)ns * 2);
+        for (int64_t k = 0; k < ns; ++k) {
+            std::string key(reinterpret_cast<const char*>(&seqs[(size_t)(2 * p0 + k) * L]), L);
+            auto it = seen.emplace(std::move(key), (uint32_t)urep.size());
+            if (it.second) urep.push_back(k);
+            uid[k] = it.first->second;
+        }
+    }
+    const int64_t nu = (int64_t)urep.size();
+    // uses of each unique side: pair << 1 | role, in batch-side order
+    std::vector<uint32_t> use_beg(nu + 1, 0), uses(ns);
+    for (int64_t k = 0; k < ns; ++k) ++use_beg[uid[k] + 1];
+    for (int64_t u = 0; u < nu; ++u) use_beg[u + 1] += use_beg[u];
+    {
+        std::vector<uint32_t> fill(use_beg.begin(), use_beg.end() - 1);
+        for (int64_t k = 0; k < ns; ++k) uses[fill[uid[k]]++] = (uint32_t)k;  // k = 2 pair + role
+    }
+    std::vector<uint8_t> rows((size_t)nu * L);
+    std::vector<uint64_t> ubeg(nu + 1), pcnt(nu);
+    std::vector<uint32_t> nsuf(nu);
     uint64_t units = 0, total = 0;
-    for (int64_t k = 0; k < ns; ++k) {
-        const Side& sd = sides[2 * p0 + k];
-        memcpy(&rows[(size_t)k * L], sd.rows.data(), L);
-        ubeg[k] = units;
-        pcnt[k] = sd.total ? sd.prefix_count : 0;
-        nsuf[k] = sd.nsuf;
+    for (int64_t u = 0; u < nu; ++u) {
+        const Side& sd = sides[2 * p0 + urep[u]];
+        memcpy(&rows[(size_t)u * L], sd.rows.data(), L);
+        ubeg[u] = units;
+        pcnt[u] = sd.total ? sd.prefix_count : 0;
+        nsuf[u] = sd.nsuf;
         if (sd.total) {
             units += (sd.prefix_count + kScanThreads - 1) / kScanThreads;
             total += sd.total;
         }
     }
-    ubeg[ns] = units;
+    ubeg[nu] = units;
     out.assign(np_, {});
     if (units == 0) return GP_OK;
     // capacities: every expansion could pass at small sizes; at large ones
@@ -1184,14 +1249,14 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
            &dsurv = c->ux[9], &duns = c->ux[10], &dside = c->ux[11];
     if (!drows.ensure(rows.size()) || !dubeg.ensure(ubeg.size() * 8) || !dpcnt.ensure(pcnt.size() * 8) ||
         !dnsuf.ensure(nsuf.size() * 4) || !dcnt.ensure(64) || !dsurv.ensure(surv_cap * 8) ||
-        !duns.ensure(unsure_cap * 8) || !dside.ensure((size_t)ns * 4))
+        !duns.ensure(unsure_cap * 8) || !dside.ensure((size_t)nu * 4))
         return c->fail(GP_ERR_NOMEM, "uncompress: batch buffers");
     GP_CUDA_TRY(c, cudaMemcpyAsync(drows.p, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(dubeg.p, ubeg.data(), ubeg.size() * 8, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(dpcnt.p, pcnt.data(), pcnt.size() * 8, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(dnsuf.p, nsuf.data(), nsuf.size() * 4, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemsetAsync(dcnt.p, 0, 64, s));
-    GP_CUDA_TRY(c, cudaMemsetAsync(dside.p, 0, (size_t)ns * 4, s));
+    GP_CUDA_TRY(c, cudaMemsetAsync(dside.p, 0, (size_t)nu * 4, s));
     unsigned long long* counters = dcnt.as<unsigned long long>();
     LevelDev d = ld;
     d.side_rows = drows.as<uint8_t>();
@@ -1200,7 +1265,7 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     sa.unit_begin = dubeg.as<uint64_t>();
     sa.prefix_count = dpcnt.as<uint64_t>();
     sa.nsuf = dnsuf.as<uint32_t>();
-    sa.n_sides = (int)ns;
+    sa.n_sides = (int)nu;
     sa.n_units = units;
     sa.thr_lo = lv.thr_lo;
     sa.thr_hi = lv.thr_hi;
@@ -1227,9 +1292,9 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     ux_recheck_kernel<<<(unsigned)c->num_sms * 8, kRecheckWarps * 32, 0, s>>>(ra);
     GP_CUDA_TRY(c, cudaGetLastError());
     std::vector<unsigned long long> hc(8);
-    std::vector<uint32_t> side_count(ns);
+    std::vector<uint32_t> side_count(nu);
     GP_CUDA_TRY(c, cudaMemcpyAsync(hc.data(), counters, 64, cudaMemcpyDeviceToHost, s));
-    GP_CUDA_TRY(c, cudaMemcpyAsync(side_count.data(), sa.side_count, (size_t)ns * 4, cudaMemcpyDeviceToHost, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(side_count.data(), sa.side_count, (size_t)nu * 4, cudaMemcpyDeviceToHost, s));
     GP_CUDA_TRY(c, cudaStreamSynchronize(s));
     if (hc[0] > surv_cap || hc[1] > unsure_cap) {
         cudaMemset(c->status.p, 0, sizeof(int));
@@ -1239,48 +1304,60 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     int rc = c->check_status("uncompress");
     if (rc) return rc;
     const uint64_t nsurv = hc[0];
-    // buckets: a pair with no survivor on one side cannot match
+    // buckets: a pair with no survivor on one side cannot match; its base
+    // is the next pair's (bases stay non-decreasing for the join's search)
     std::vector<uint8_t> lg(np_, 255);
     std::vector<uint32_t> pbase(np_, 0);
-    uint64_t nbk = 0;
+    uint64_t nbk = 0, entries = 0;
     for (int64_t p = 0; p < np_; ++p) {
-        const uint64_t na = side_count[2 * p], nbb = side_count[2 * p + 1];
+        const uint64_t na = side_count[uid[2 * p]], nbb = side_count[uid[2 * p + 1]];
+        pbase[p] = (uint32_t)std::min<uint64_t>(nbk, UINT32_MAX);
         if (!na || !nbb) continue;
         int l = 0;
         while (((uint64_t)kBucketTarget << l) < na + nbb && l < 30) ++l;
         lg[p] = (uint8_t)l;
-        pbase[p] = (uint32_t)nbk;
         nbk += uint64_t(1) << l;
+        entries += na + nbb;
     }
     if (nbk == 0 || nsurv == 0) return GP_OK;
     if (nbk >= (uint64_t(1) << 31)) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %llu join buckets", (unsigned long long)nbk);
+    if (entries >= (uint64_t(1) << 32)) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %llu join entries", (unsigned long long)entries);
     DevBuf &dlg = c->ux[12], &dpb = c->ux[13], &dkeys = c->ux[14], &dbkt = c->ux[15], &dbc = c->ux[16],
            &dbo = c->ux[17], &dbcur = c->ux[18], &dscan = c->ux[19], &deh = c->ux[20], &dei = c->ux[21],
-           &dm = c->ux[22];
-    const uint64_t match_cap = std::max<uint64_t>(1 << 16, nsurv / 16);
-    if (!dlg.ensure(np_) || !dpb.ensure((size_t)np_ * 4) || !dkeys.ensure(nsurv * 8) || !dbkt.ensure(nsurv * 4) ||
+           &dm = c->ux[22], &dub = c->ux[31], &duse = c->ux[32], &deix = c->ux[33];
+    const uint64_t match_cap = std::max<uint64_t>(1 << 16, entries / 16);
+    if (!dlg.ensure(np_) || !dpb.ensure((size_t)np_ * 4) || !dkeys.ensure(entries * 8) || !dbkt.ensure(entries * 4) ||
+        !deix.ensure(entries * 4) || !dub.ensure(use_beg.size() * 4) || !duse.ensure(uses.size() * 4) ||
         !dbc.ensure(nbk * 4) || !dbo.ensure(nbk * 4 + 4) || !dbcur.ensure(nbk * 4) ||
-        !dscan.ensure(gp::scan_tmp_bytes((int64_t)nbk)) || !deh.ensure(nsurv * 8) || !dei.ensure(nsurv * 4) ||
+        !dscan.ensure(gp::scan_tmp_bytes((int64_t)nbk)) || !deh.ensure(entries * 8) || !dei.ensure(entries * 4) ||
         !dm.ensure(match_cap * 16))
         return c->fail(GP_ERR_NOMEM, "uncompress: join buffers");
     GP_CUDA_TRY(c, cudaMemcpyAsync(dlg.p, lg.data(), np_, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemcpyAsync(dpb.p, pbase.data(), (size_t)np_ * 4, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(dub.p, use_beg.data(), use_beg.size() * 4, cudaMemcpyHostToDevice, s));
+    GP_CUDA_TRY(c, cudaMemcpyAsync(duse.p, uses.data(), uses.size() * 4, cudaMemcpyHostToDevice, s));
     GP_CUDA_TRY(c, cudaMemsetAsync(dbc.p, 0, nbk * 4, s));
     GP_CUDA_TRY(c, cudaMemsetAsync(dbcur.p, 0, nbk * 4, s));
     KeyArgs ka{};
     ka.lv = d;
     ka.surv = sa.surv;
     ka.n = nsurv;
+    ka.use_beg = dub.as<uint32_t>();
+    ka.uses = duse.as<uint32_t>();
     ka.pair_lg = dlg.as<uint8_t>();
     ka.pair_base = dpb.as<uint32_t>();
     ka.keys = dkeys.as<uint64_t>();
     ka.bucket = dbkt.as<uint32_t>();
+    ka.eidx = deix.as<uint32_t>();
+    ka.entry_cap = entries;
+    ka.ecount = counters + 3;
     ka.bcount = dbc.as<uint32_t>();
+    ka.status = sa.status;
     ux_key_kernel<<<grid_for(nsurv, (unsigned)c->num_sms * 16), 256, 0, s>>>(ka);
     GP_CUDA_TRY(c, cudaGetLastError());
     GP_CUDA_TRY(c, gp::exclusive_scan_u32(dbc.as<uint32_t>(), dbo.as<uint32_t>(), (int64_t)nbk, dscan.as<uint32_t>(), s));
-    ux_scatter_kernel<<<grid_for(nsurv, (unsigned)c->num_sms * 16), 256, 0, s>>>(
-        sa.surv, ka.keys, ka.bucket, nsurv, dbo.as<uint32_t>(), dbcur.as<uint32_t>(), deh.as<uint64_t>(),
+    ux_scatter_kernel<<<grid_for(entries, (unsigned)c->num_sms * 16), 256, 0, s>>>(
+        ka.keys, ka.bucket, ka.eidx, entries, dbo.as<uint32_t>(), dbcur.as<uint32_t>(), deh.as<uint64_t>(),
         dei.as<uint32_t>());
     GP_CUDA_TRY(c, cudaGetLastError());
     JoinArgs ja{};
@@ -1291,6 +1368,8 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     ja.boff = dbo.as<uint32_t>();
     ja.bcount = dbc.as<uint32_t>();
     ja.n_buckets = (uint32_t)nbk;
+    ja.pair_base = dpb.as<uint32_t>();
+    ja.n_pairs = (uint32_t)np_;
     ja.matches = dm.as<uint64_t>();
     ja.match_cap = match_cap;
     ja.counters = counters;
@@ -1410,7 +1489,7 @@ int run_level(gp_ctx* c, const Level& lv, const std::vector<uint8_t>& seqs, FILE
     LevelDev ld{};
     rc = upload_level(c, lv, ld, s);
     if (rc) return rc;
-    Batcher bt{c, lv, ld, sides, s, scan_kernel_for(lv.np), 0, 0, {}};
+    Batcher bt{c, lv, ld, sides, seqs, s, scan_kernel_for(lv.np), 0, 0, {}};
     {
         // shared memory of the scan: the largest suffix table and term table
         // any side of this call needs (a few tens of KB: several CTAs per SM)
