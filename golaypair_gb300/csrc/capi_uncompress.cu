@@ -580,32 +580,61 @@ struct KeyArgs {
     int* status;
 };
 
+// Entry i is survivor i's first use (bucket ~0 when its side has none in a
+// pair that can match); further uses, rare, take slots from n on, reserved
+// once per warp.
 __global__ void ux_key_kernel(KeyArgs a) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t v = a.surv[i];
-        const uint32_t u = (uint32_t)(v >> kRankBits);
-        const uint32_t j0 = a.use_beg[u], j1 = a.use_beg[u + 1];
+    const int lane = threadIdx.x & 31;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < a.n; i0 += stride) {
+        const uint64_t i = i0 + lane;
+        uint64_t v = 0;
+        uint32_t j0 = 0, j1 = 0, cnt = 0;
+        if (i < a.n) {
+            v = a.surv[i];
+            const uint32_t u = (uint32_t)(v >> kRankBits);
+            j0 = a.use_beg[u];
+            j1 = a.use_beg[u + 1];
+            for (uint32_t j = j0; j < j1; ++j) cnt += a.pair_lg[a.uses[j] >> 1] != 255 ? 1u : 0u;
+        }
+        uint64_t extra = 0;  // slot of this lane's second use
+        if (__any_sync(0xFFFFFFFFu, cnt > 1)) {
+            const uint32_t mine = cnt > 1 ? cnt - 1 : 0u;
+            uint32_t incl = mine;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+                if (lane >= d) incl += t;
+            }
+            const uint32_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            unsigned long long base = 0;
+            if (lane == 31) base = atomicAdd(a.ecount, (unsigned long long)tot);
+            base = __shfl_sync(0xFFFFFFFFu, base, 31);
+            extra = a.n + base + (incl - mine);
+        }
+        if (i >= a.n) continue;
+        if (!cnt) {
+            a.bucket[i] = 0xFFFFFFFFu;
+            continue;
+        }
         int paf[kMaxLnew / 2];
-        bool have = false;
+        expansion_paf(a.lv, v, paf);
+        uint64_t e = i;
         for (uint32_t j = j0; j < j1; ++j) {
             const uint32_t code = a.uses[j], pair = code >> 1, role = code & 1u;
             const int lg = a.pair_lg[pair];
             if (lg == 255) continue;
-            if (!have) {
-                expansion_paf(a.lv, v, paf);
-                have = true;
+            if (e >= a.entry_cap) {
+                flag_overflow(a.status);
+                break;
             }
             const uint64_t h = join_key(a.lv, paf, role == 0);
             const uint32_t b = a.pair_base[pair] + (lg ? (uint32_t)(h >> (64 - lg)) : 0u);
-            const unsigned long long e = atomicAdd(a.ecount, 1ull);
-            if (e >= a.entry_cap) {
-                flag_overflow(a.status);
-                continue;
-            }
             a.keys[e] = h;
             a.bucket[e] = b;
             a.eidx[e] = (uint32_t)i | (role << 31);
             atomicAdd(&a.bcount[b], 1u);
+            e = e == i ? extra : e + 1;
         }
     }
 }
@@ -614,6 +643,7 @@ __global__ void ux_scatter_kernel(const uint64_t* keys, const uint32_t* bucket, 
                                   const uint32_t* boff, uint32_t* bcur, uint64_t* ent_h, uint32_t* ent_i) {
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t b = bucket[e];
+        if (b == 0xFFFFFFFFu) continue;
         const uint32_t pos = boff[b] + atomicAdd(&bcur[b], 1u);
         ent_h[pos] = keys[e];
         ent_i[pos] = eidx[e];  // bit 31: b-side
@@ -1308,7 +1338,8 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
     // is the next pair's (bases stay non-decreasing for the join's search)
     std::vector<uint8_t> lg(np_, 255);
     std::vector<uint32_t> pbase(np_, 0);
-    uint64_t nbk = 0, entries = 0;
+    uint64_t nbk = 0;
+    std::vector<uint32_t> uses_ok(nu, 0);  // uses of each distinct side in pairs that can match
     for (int64_t p = 0; p < np_; ++p) {
         const uint64_t na = side_count[uid[2 * p]], nbb = side_count[uid[2 * p + 1]];
         pbase[p] = (uint32_t)std::min<uint64_t>(nbk, UINT32_MAX);
@@ -1317,9 +1348,14 @@ int Batcher::run(int64_t p0, int64_t p1, bool* overflowed) {
         while (((uint64_t)kBucketTarget << l) < na + nbb && l < 30) ++l;
         lg[p] = (uint8_t)l;
         nbk += uint64_t(1) << l;
-        entries += na + nbb;
+        ++uses_ok[uid[2 * p]];
+        ++uses_ok[uid[2 * p + 1]];
     }
     if (nbk == 0 || nsurv == 0) return GP_OK;
+    // join entries: one slot per survivor (its first use), then the further uses
+    uint64_t entries = nsurv;
+    for (int64_t u = 0; u < nu; ++u)
+        if (uses_ok[u] > 1) entries += (uint64_t)side_count[u] * (uses_ok[u] - 1);
     if (nbk >= (uint64_t(1) << 31)) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %llu join buckets", (unsigned long long)nbk);
     if (entries >= (uint64_t(1) << 32)) return c->fail(GP_ERR_UNSUPPORTED, "uncompress: %llu join entries", (unsigned long long)entries);
     DevBuf &dlg = c->ux[12], &dpb = c->ux[13], &dkeys = c->ux[14], &dbkt = c->ux[15], &dbc = c->ux[16],
