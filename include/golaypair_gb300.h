@@ -72,7 +72,10 @@ int gp_psd_filter(gp_ctx* ctx, const int8_t* seqs, int64_t n, int L, int order, 
  * up (GP_ERR_TIMEOUT) or an overflow (GP_ERR_OVERFLOW) of this call; until
  * then the error stays pending in the context.  The unsure list and counters
  * of the FP64 recheck belong to the context: calls on one context must not
- * overlap on the GPU (enqueue them on one stream, or wait in between). */
+ * overlap on the GPU (enqueue them on one stream, or wait in between).
+ * d_seqs may start at any byte; the tensor-core filter streams whole tiles
+ * through the bulk-copy engine only when it is 16-byte aligned, and reads
+ * the rows with plain loads otherwise (same verdicts, slower). */
 int gp_psd_filter_device(gp_ctx* ctx, const int8_t* d_seqs, int64_t n, int L, int order, int paf, int mode,
                          uint32_t* d_pass_mask, void* stream, gp_psd_stats* stats);
 
